@@ -1,0 +1,271 @@
+// Scalar (NSTOKES=1) discrete-ordinate solar radiative transfer for one
+// atmospheric column in one observation geometry, written for one CUDA thread
+// per (column, wavelength) solve.
+//
+// Why one thread per solve: on GB300 the FP64 pipe issues at a small fraction
+// of the FP32 rate, so the plain-FP64 solve is bound by FP64 instruction issue.
+// Mapping one solve to one thread keeps every lane of every FP64 instruction
+// busy (a warp works on 32 independent columns in lock-step) instead of
+// leaving most lanes idle on 8x8 matrix work.  Layer-sized state lives in
+// per-thread local memory (L1-cached); the per-layer factors that the
+// boundary-value sweep needs on the way back up live in a global scratch
+// buffer laid out element-major / thread-minor so that a warp's accesses to
+// the same element are one coalesced transaction.
+//
+// The physics is the reference's VLIDORT 2.8.3 regular solar path as driven by
+// AeroApps (paths relative to the reference project root):
+//   src/Components/rtms/RTSI/VLIDORT2p8p3/VLIDORT_ScatMod.F90:975-1247  (layer mixing, output)
+//   .../vlidort_main/regular/vlidort_geometry.f90:119-317              (Chapman factors)
+//   .../vlidort_main/regular/vlidort_miscsetups.f90:370-1292,2273,3187 (delta-M, beam, PI functions)
+//   .../vlidort_main/regular/vlidort_solutions.f90:150-3073            (homogeneous + Green's solutions)
+//   .../vlidort_main/regular/vlidort_bvproblem.f90:147-2311            (boundary-value problem)
+//   .../vlidort_main/regular/vlidort_intensity.f90:145, PostProcessing.f90:139 (TOA source recursion)
+//   .../vlidort_main/regular/vlidort_converge.f90:825-1236             (Fourier convergence)
+//   .../vlidort_focode/*.f90                                           (first-order single scatter)
+// The numerical methods differ where GB300 favours another formulation (see
+// sym_eigen_layer and the block sweep in fourier_term); results agree with the
+// reference algorithm to round-off.
+#pragma once
+
+#ifdef __CUDACC__
+#define RT_HD __host__ __device__ __forceinline__
+#define RT_HDN __host__ __device__
+#else
+#include <cmath>
+#include <algorithm>
+#define RT_HD inline
+#define RT_HDN
+using std::sqrt; using std::exp; using std::fabs; using std::asin; using std::sin; using std::cos;
+using std::atan; using std::acos; using std::copysign;
+#endif
+
+namespace aerort {
+
+// VLIDORT parameters (vlidort_def/vlidort_pars.f90:386-444).  DEG_TO_RAD is the
+// reference's truncated constant, kept so that angles map identically.
+constexpr double kDTR = 1.7453292519943e-02;
+constexpr double kPIE = 180.0 * kDTR;
+constexpr double kPI4 = 4.0 * kPIE;
+constexpr double kTaylorSmall = 1.0e-4;
+constexpr double kMaxTau = 32.0;      // MAX_TAU_SPATH / UPATH / QPATH
+constexpr double kFoCutoff = 88.0;    // FO_VectorSS_RTCalcs_I.f90:325
+constexpr int kMaxFine = 4;           // MAXFINELAYERS
+constexpr int kMaxLayers = 72;        // MAXLAYERS
+
+// Per-solve status codes (0 = radiance valid).
+enum RtStatus : int {
+  RT_OK = 0,
+  RT_EIGEN_FAIL = 1,      // layer eigenproblem: factorisation or QR iteration failed
+  RT_BVP_SINGULAR = 2,    // zero pivot in the boundary-value sweep
+  RT_BAD_INPUT = 3,       // inputs outside the solver's domain (e.g. tau_ext <= 0)
+  RT_FO_FAIL = 4,         // single-scatter geometry failed
+};
+
+// Options shared by every solve of a batch (VLIDORT_Init settings).
+struct RtOptions {
+  int do_focorr;           // first-order single-scatter + direct-bounce correction
+  int do_deltam;           // delta-M scaling
+  int do_plane_parallel;   // plane-parallel beam attenuation
+  int do_double_convtest;  // two consecutive converged Fourier terms end the series
+  int nfine;               // fine layers of the enhanced-PS line-of-sight quadrature
+  int taylor_order;        // Taylor series order near the exponential singularities
+  double accuracy;         // Fourier convergence threshold
+  double earth_radius;     // km
+  double flux_factor;      // solar flux
+  int max_fourier;         // -1: up to NMOMENTS (reference); otherwise cap (testing)
+};
+
+// Strided per-thread view of the global scratch buffer.
+struct Scratch {
+  double* base;
+  long stride;
+  RT_HD double& operator[](long e) const { return base[e * stride]; }
+};
+
+// ---------------------------------------------------------------------------------- Taylor
+// Series for (exp(-a d) - exp(-b d))/(b - a) near a == b (vlidort_Taylor.f90:101-219).
+RT_HD double taylor1(int order, double eps, double delta, double udel, double sm) {
+  double d = 1.0, mult = 0.0, power = 1.0;
+  for (int m = 1; m <= order + 1; ++m) {
+    d = delta * d / (double)m;
+    if (m == 1) mult = d;
+    else { power *= eps; mult += power * d; }
+  }
+  return mult * udel * sm;
+}
+
+RT_HD double taylor2(int order, double eps, double y, double delta, double fac1, double fac2, double sm) {
+  double d[10];
+  int mterms = order + 1;
+  const bool small = fabs(y) < kTaylorSmall;
+  if (small) mterms += 1;
+  d[0] = 1.0;
+  for (int m = 1; m <= mterms; ++m) d[m] = delta * d[m - 1] / (double)m;
+  if (small) {
+    double power = 1.0, power2 = 1.0, mult = d[2];
+    for (int m = 3; m <= mterms; ++m) {
+      power = power * (eps - y);
+      power2 = power - y * power2;
+      mult += d[m] * power2;
+    }
+    return mult * fac1 * sm;
+  }
+  double y1 = 1.0 / y, ac[10];
+  ac[0] = 1.0;
+  for (int m = 1; m <= mterms; ++m) ac[m] = y1 * ac[m - 1];
+  double mult = 0.0, power = 1.0;
+  for (int m = 1; m <= mterms; ++m) {
+    double cc = 0.0;
+    for (int j = 0; j <= m; ++j) cc += ac[j] * d[m - j];
+    double term = fac1 * ac[m] - fac2 * cc;
+    if (m == 1) mult = term;
+    else { power *= eps; mult += power * term; }
+  }
+  return mult * sm * y1;
+}
+
+// ---------------------------------------------------------------------------------- dense kernels
+// Cholesky A = L L^T of an n x n SPD matrix (column-major, lower triangle
+// overwritten with L).  Returns false if a pivot is not positive.
+template <int NS>
+RT_HD bool cholesky(int n, double* A) {
+  for (int j = 0; j < n; ++j) {
+    double s = A[j + NS * j];
+    for (int k = 0; k < j; ++k) s -= A[j + NS * k] * A[j + NS * k];
+    if (!(s > 0.0)) return false;
+    double ljj = sqrt(s);
+    A[j + NS * j] = ljj;
+    double inv = 1.0 / ljj;
+    for (int i = j + 1; i < n; ++i) {
+      double t = A[i + NS * j];
+      for (int k = 0; k < j; ++k) t -= A[i + NS * k] * A[j + NS * k];
+      A[i + NS * j] = t * inv;
+    }
+  }
+  return true;
+}
+
+// Symmetric eigendecomposition H = V diag(lam) V^T of an n x n matrix stored
+// column-major with leading dimension NS: Householder reduction to
+// tridiagonal form with the transformations accumulated in V, then implicit
+// QR sweeps with Wilkinson shifts applied as Givens rotations.  H is
+// destroyed.  Returns false if the iteration budget is exhausted.
+template <int NS>
+RT_HD bool sym_eigen(int n, double* H, double* V, double* lam) {
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) V[i + NS * j] = (i == j) ? 1.0 : 0.0;
+  double v[NS], p[NS];
+  for (int k = 0; k + 2 < n; ++k) {
+    // Householder vector for column k below the subdiagonal
+    double alpha2 = 0.0;
+    for (int i = k + 1; i < n; ++i) alpha2 += H[i + NS * k] * H[i + NS * k];
+    if (alpha2 == 0.0) continue;
+    double x0 = H[(k + 1) + NS * k];
+    double alpha = -copysign(sqrt(alpha2), x0);
+    for (int i = k + 1; i < n; ++i) v[i] = H[i + NS * k];
+    v[k + 1] = x0 - alpha;
+    double vtv = alpha2 - x0 * x0 + v[k + 1] * v[k + 1];
+    if (vtv == 0.0) continue;
+    double beta = 2.0 / vtv;
+    // p = beta * H22 v ; w = p - (beta/2)(p.v) v ; H22 -= v w^T + w v^T
+    double pv = 0.0;
+    for (int i = k + 1; i < n; ++i) {
+      double s = 0.0;
+      for (int j = k + 1; j < n; ++j) s += H[i + NS * j] * v[j];
+      p[i] = beta * s;
+      pv += p[i] * v[i];
+    }
+    double half = 0.5 * beta * pv;
+    for (int i = k + 1; i < n; ++i) p[i] -= half * v[i];
+    for (int j = k + 1; j < n; ++j)
+      for (int i = k + 1; i < n; ++i) H[i + NS * j] -= v[i] * p[j] + p[i] * v[j];
+    H[(k + 1) + NS * k] = alpha;
+    H[k + NS * (k + 1)] = alpha;
+    for (int i = k + 2; i < n; ++i) { H[i + NS * k] = 0.0; H[k + NS * i] = 0.0; }
+    // V <- V (I - beta v v^T)
+    for (int i = 0; i < n; ++i) {
+      double s = 0.0;
+      for (int j = k + 1; j < n; ++j) s += V[i + NS * j] * v[j];
+      s *= beta;
+      for (int j = k + 1; j < n; ++j) V[i + NS * j] -= s * v[j];
+    }
+  }
+  double d[NS], e[NS];  // e[i] couples i and i+1
+  for (int i = 0; i < n; ++i) d[i] = H[i + NS * i];
+  for (int i = 0; i + 1 < n; ++i) e[i] = H[(i + 1) + NS * i];
+  const double eps = 2.220446049250313e-16;
+  int q = n - 1, sweeps = 0;
+  while (q > 0) {
+    // deflate negligible couplings at the bottom of the active block
+    if (fabs(e[q - 1]) <= eps * (fabs(d[q - 1]) + fabs(d[q]))) { e[q - 1] = 0.0; --q; continue; }
+    int p0 = q - 1;
+    while (p0 > 0 && fabs(e[p0 - 1]) > eps * (fabs(d[p0 - 1]) + fabs(d[p0]))) --p0;
+    if (p0 > 0) e[p0 - 1] = 0.0;
+    if (++sweeps > 40 * n) return false;
+    // Wilkinson shift from the trailing 2x2 block
+    double dd = 0.5 * (d[q - 1] - d[q]);
+    double eq = e[q - 1];
+    double den = dd + copysign(sqrt(dd * dd + eq * eq), dd);
+    double mu = d[q] - (den != 0.0 ? eq * eq / den : 0.0);
+    double x = d[p0] - mu, z = e[p0];
+    double bulge = 0.0;
+    for (int k = p0; k < q; ++k) {
+      double r = sqrt(x * x + z * z);
+      double c = (r == 0.0) ? 1.0 : x / r, s = (r == 0.0) ? 0.0 : z / r;
+      // rotate rows/columns k, k+1 of the tridiagonal (with bulge below it)
+      if (k > p0) e[k - 1] = r;
+      double dk = d[k], dk1 = d[k + 1], ek = e[k];
+      d[k] = c * c * dk + 2.0 * c * s * ek + s * s * dk1;
+      d[k + 1] = s * s * dk - 2.0 * c * s * ek + c * c * dk1;
+      e[k] = c * s * (dk1 - dk) + (c * c - s * s) * ek;
+      if (k + 1 < q) {
+        bulge = s * e[k + 1];
+        e[k + 1] = c * e[k + 1];
+        x = e[k];
+        z = bulge;
+      }
+      for (int i = 0; i < n; ++i) {
+        double a = V[i + NS * k], b = V[i + NS * (k + 1)];
+        V[i + NS * k] = c * a + s * b;
+        V[i + NS * (k + 1)] = -s * a + c * b;
+      }
+    }
+  }
+  for (int i = 0; i < n; ++i) lam[i] = d[i];
+  return true;
+}
+
+// In-place LU with partial pivoting of an n x n matrix (leading dimension LD)
+// and solution of nrhs right-hand sides B (n x nrhs, leading dimension LD).
+template <int LD>
+RT_HD bool lu_solve(int n, double* A, double* B, int nrhs) {
+  for (int k = 0; k < n; ++k) {
+    int piv = k;
+    double amax = fabs(A[k + LD * k]);
+    for (int i = k + 1; i < n; ++i) {
+      double a = fabs(A[i + LD * k]);
+      if (a > amax) { amax = a; piv = i; }
+    }
+    if (amax == 0.0) return false;
+    if (piv != k) {
+      for (int j = 0; j < n; ++j) { double t = A[k + LD * j]; A[k + LD * j] = A[piv + LD * j]; A[piv + LD * j] = t; }
+      for (int j = 0; j < nrhs; ++j) { double t = B[k + LD * j]; B[k + LD * j] = B[piv + LD * j]; B[piv + LD * j] = t; }
+    }
+    double inv = 1.0 / A[k + LD * k];
+    for (int i = k + 1; i < n; ++i) {
+      double f = A[i + LD * k] * inv;
+      A[i + LD * k] = f;
+      for (int j = k + 1; j < n; ++j) A[i + LD * j] -= f * A[k + LD * j];
+      for (int j = 0; j < nrhs; ++j) B[i + LD * j] -= f * B[k + LD * j];
+    }
+  }
+  for (int j = 0; j < nrhs; ++j)
+    for (int i = n - 1; i >= 0; --i) {
+      double s = B[i + LD * j];
+      for (int k = i + 1; k < n; ++k) s -= A[i + LD * k] * B[k + LD * j];
+      B[i + LD * j] = s / A[i + LD * i];
+    }
+  return true;
+}
+
+}  // namespace aerort
