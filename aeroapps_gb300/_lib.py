@@ -1,0 +1,82 @@
+"""ctypes binding of libaerort.so (the C ABI in include/aerort.h).
+
+The library is built in-tree by aeroapps_gb300.build.build().  There is no CPU
+fallback: if the library is missing or fails to load, every entry point raises.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+_lib = None
+
+c_int = ctypes.c_int
+c_double = ctypes.c_double
+c_void_p = ctypes.c_void_p
+P_f = ctypes.POINTER(ctypes.c_float)
+P_d = ctypes.POINTER(ctypes.c_double)
+P_i = ctypes.POINTER(ctypes.c_int)
+
+
+class MieTableDesc(ctypes.Structure):
+    """aerort_mie_table_desc."""
+    _fields_ = [("nrh", c_int), ("nbin", c_int), ("nmom", c_int), ("npol", c_int),
+                ("rh", P_f), ("bext", P_f), ("bsca", P_f), ("g", P_f), ("pmom", P_f)]
+
+
+_SIGNATURES = {
+    "aerort_mie_create": (c_int, [c_int, ctypes.POINTER(MieTableDesc), c_int, P_f, ctypes.POINTER(c_void_p)]),
+    "aerort_mie_destroy": (c_int, [c_void_p]),
+    "aerort_get_aop_vector": (c_int, [c_void_p, c_int, c_int, c_int, c_int, P_f, P_i, P_i, P_f, P_f, c_int, c_int,
+                                      P_f, P_f, P_f, P_f]),
+    "aerort_get_aop_vector_dev": (c_int, [c_void_p, c_int, c_int, c_int, c_int, P_f, P_i, P_i, c_void_p, c_void_p,
+                                          c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "aerort_vlidort_scalar_lambert": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 13 +
+                                      [c_double, c_int, P_d, P_d]),
+    "aerort_vlidort_scalar_lambert_ex": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 13 +
+                                         [c_double, c_int, P_d, P_d, P_i, P_i]),
+    "aerort_vlidort_scalar_lambert_dev": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int] + [c_void_p] * 10 +
+                                          [c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "aerort_vlidort_scalar_lambert_batch_dev": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int] + [c_void_p] * 14 +
+                                                [c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "aerort_vlidort_scalar_lambert_batch": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, P_i] + [P_d] * 10 +
+                                            [c_double, P_d, P_d, P_i, P_i]),
+    "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
+    "aerort_last_error": (ctypes.c_char_p, []),
+    "aerort_version": (c_int, []),
+    "aerort_release": (c_int, []),
+    "aerort_miegen_lognormal": (c_int, [c_int, P_d, c_int, P_d, c_int, P_d, P_d, c_double, c_double, c_int, c_double,
+                                        c_int, c_int, P_f, P_f, P_f, P_f]),
+}
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load (building if needed) and return the ctypes handle of libaerort.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("libaerort.so is not built (%s); run aeroapps_gb300.build.build()" % path)
+    handle = ctypes.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = handle
+    return _lib
+
+
+def last_error():
+    return lib().aerort_last_error().decode(errors="replace")
+
+
+def ptr(a, kind):
+    """Pointer to the data of a contiguous numpy array."""
+    return a.ctypes.data_as(kind)

@@ -1,0 +1,57 @@
+// Internal declarations shared by the aerort translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/aerort.h"
+#include "rt_solve.cuh"
+
+namespace aerort_internal {
+
+int set_error(int rc, const std::string& msg);
+
+#define CUDA_TRY(expr)                                                                                   \
+  do {                                                                                                   \
+    cudaError_t e_ = (expr);                                                                             \
+    if (e_ != cudaSuccess)                                                                               \
+      return ::aerort_internal::set_error(AERORT_RC_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t n);
+  void release();
+};
+
+// Library context: stream, scratch, staging buffers.  One per process; calls
+// are serialised by the mutex (the reference library is serial per process).
+struct Context {
+  std::mutex mu;
+  bool init = false;
+  int device = -1, num_sms = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf scratch, counter, stage[24];
+  int setup();
+  void release();
+};
+
+Context& ctx();
+
+// Gauss-Legendre nodes/weights on (0,1), ascending (as VLIDORT's GETQUAD2).
+void gauss_legendre01(int n, double* x, double* w);
+
+struct Quad {
+  double qx[16], qw[16], tu[aerort::kMaxFine], wu[aerort::kMaxFine];
+};
+
+template <int NS>
+int launch_scalar_lambert(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
+                          double* refl, int* nf, int* st, cudaStream_t s);
+
+}  // namespace aerort_internal

@@ -1,0 +1,73 @@
+// Scalar RT kernel and launcher, instantiated once per stream count in
+// rt_ns{4,6,8,12,16}.cu so the instantiations compile in parallel.
+#pragma once
+#include "aerort_internal.cuh"
+
+namespace aerort_internal {
+using namespace aerort;
+
+// Sticky nadir-FO flag (VLIDORT_ScatMod.F90:1123-1126 as reached from
+// VLIDORT_LAMBERT.F90:106-165): first pixel whose angles are valid, whose
+// solar zenith is exactly 0 and that has at least one valid albedo.
+__global__ void k_nadir_first(int nobs, int nch, const double* sza, const double* raa, const double* vza,
+                              const double* albedo, double missing, int* first);
+// counter <- 0, first <- nobs (device-side, so launches need no host staging)
+__global__ void k_init_sched(int* counter, int* first, int nobs);
+
+template <int NS>
+__global__ void __launch_bounds__(64) k_scalar_lambert(RtOptions opt, LambertInputs in, Quad q, double* scratch,
+                                                        long nthreads, int nsolve, int* counter, double* rad,
+                                                        double* refl, int* nf, int* st) {
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const Scratch S{scratch + tid, nthreads};
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= nsolve) break;
+    const int s = base + lane;
+    if (s < nsolve) solve_lambert<NS>(opt, in, s, q.qx, q.qw, q.tu, q.wu, S, rad, refl, nf, st);
+    __syncwarp();
+  }
+}
+
+template <int NS>
+int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
+                          int* nf, int* st, cudaStream_t s) {
+  const int nsolve = in.nobs * in.nch;
+  if (nsolve == 0) return 0;
+  Quad q;
+  std::memset(&q, 0, sizeof(q));
+  gauss_legendre01(NS, q.qx, q.qw);
+  if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
+  int bs = 64, per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS>, bs, 0));
+  if (per_sm < 1) per_sm = 1;
+  long maxblocks = (long)per_sm * c.num_sms;
+  long nblocks = (nsolve + bs - 1) / bs;
+  if (nblocks > maxblocks) nblocks = maxblocks;
+  const long nthreads = nblocks * bs;
+  const ScratchLayout<NS> lay(in.km);
+  if (int rc = c.scratch.ensure(sizeof(double) * (size_t)lay.total * nthreads)) return rc;
+  if (int rc = c.counter.ensure(2 * sizeof(int))) return rc;
+  int* counter = (int*)c.counter.p;
+  int* first = counter + 1;
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+  k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
+                                                       first);
+  CUDA_TRY(cudaGetLastError());
+  LambertInputs in2 = in;
+  in2.nadir_first = first;
+  k_scalar_lambert<NS><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, (double*)c.scratch.p, nthreads, nsolve, counter,
+                                                        rad, refl, nf, st);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace aerort_internal
+
+#define AERORT_INSTANTIATE_RT(NS)                                                                            \
+  template int aerort_internal::launch_scalar_lambert<NS>(aerort_internal::Context&, const aerort::RtOptions&, \
+                                                          const aerort::LambertInputs&, double*, double*, int*, \
+                                                          int*, cudaStream_t);

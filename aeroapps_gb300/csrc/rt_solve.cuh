@@ -21,7 +21,15 @@ struct LambertInputs {
   const double* sza;     // (nobs)
   const double* raa;     // (nobs)
   const double* vza;     // (nobs)
-  const unsigned char* nadir_fo;  // (nobs) sticky nadir-FO flag resolved in loop order
+  // Optional extensions (null = reference behaviour):
+  const int* nlay;       // (nobs) layers of each column, <= km; the column uses the first nlay entries
+  const float* tau_f;    // FP32 optics straight from VLIDORT_getAOPvector (replaces tau/ssa/pmom;
+  const float* ssa_f;    //   the conversion to FP64 is the driver's dble(), geo_vlidort.F90:598-601)
+  const float* pmom_f;
+  // Sticky nadir-FO flag (VLIDORT_ScatMod.F90:1123-1126): index of the first
+  // pixel in loop order that reaches the solver with solar_zenith == 0; every
+  // pixel from there on uses the nadir (regular pseudo-spherical) correction.
+  const int* nadir_first;  // device scalar, nobs if never triggered; may be null
   double missing;
 };
 
@@ -646,8 +654,8 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
                           double* reflectance, int* nfourier, int* status) {
   const int nch = in.nch, j = sidx / nch, i = sidx % nch;
   const long o = (long)j + (long)in.nobs * i;
-  const int L = in.km, ngreek = in.nmom;
-  const ScratchLayout<NS> lay(L);
+  const int L = in.nlay ? in.nlay[j] : in.km, ngreek = in.nmom;
+  const ScratchLayout<NS> lay(in.km);
   auto is_missing = [&](double x) { return fabs(x / in.missing - 1.0) < 0.001; };
   const double sza = in.sza[j], vza = in.vza[j], raa = in.raa[j], alb = in.albedo[o];
   if (nfourier) nfourier[o] = -1;
@@ -667,7 +675,7 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
   c.sec_u = 1.0 / c.mu_u;
   c.cos_sza = cos(sza * kDTR);
   const int NM = c.NM;
-  const bool nadir_fo = in.nadir_fo ? (in.nadir_fo[j] != 0) : false;
+  const bool nadir_fo = in.nadir_first ? (j >= *in.nadir_first) : false;
   // scattering angle for the exact single-scatter phase function
   double cosscat;
   {
@@ -688,11 +696,12 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
   const double dep = in.depol[i];
   const double raysmom2 = (1.0 - dep) / (2.0 + dep);
   const long nk = (long)in.km * in.nch * in.nobs;
-  for (int k = 0; k <= L; ++k) S[lay.hgt + k] = in.he[k + (long)(L + 1) * j] * kHeightScale;
+  for (int k = 0; k <= L; ++k) S[lay.hgt + k] = in.he[k + (long)(in.km + 1) * j] * kHeightScale;
   for (int k = 0; k < L; ++k) {
     const double ray = in.rot[k + (long)in.km * (j + (long)in.nobs * i)];
     const long a = k + (long)in.km * (i + (long)in.nch * j);
-    const double tl = in.tau[a], sl = in.ssa[a];
+    const double tl = in.tau_f ? (double)in.tau_f[a] : in.tau[a];
+    const double sl = in.ssa_f ? (double)in.ssa_f[a] : in.ssa[a];
     const double tau_ext = 0.0 + ray + tl;
     const double tau_scat = ray + sl * tl;
     if (!(tau_ext > 0.0) || !(tau_scat > 0.0)) {
@@ -705,7 +714,8 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
     const double aerswt = sl * tl / tau_scat, rayswt = ray / tau_scat;
     auto beta_in = [&](int l) -> double {  // GREEKMAT_TOTAL_INPUT(l, k, 1)
       if (l == 0) return 1.0;
-      double am = (l < ngreek) ? in.pmom[a + nk * (long)l] : 0.0;
+      double am = 0.0;
+      if (l < ngreek) am = in.pmom_f ? (double)in.pmom_f[a + nk * (long)l] : in.pmom[a + nk * (long)l];
       if (l == 2) return raysmom2 * rayswt + am * aerswt;
       return (l <= ngreek) ? am * aerswt : 0.0;
     };

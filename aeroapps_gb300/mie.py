@@ -1,0 +1,182 @@
+"""Mie tables (Chem_Mie) and the aerosol-optics mixing (VLIDORT_getAOPvector).
+
+Mirrors the reference interface of
+  src/Shared/GMAO_Shared/Chem_Base/Chem_MieMod.F90      (Chem_MieCreate, Chem_MieQueryIdx,
+                                                         Chem_MieQuery, Chem_MieDestroy)
+  src/Components/rtms/geo_vlidort/VLIDORT_MieMod.F90    (VLIDORT_getAOPvector)
+with the tables held on the GPU.  Table data come from
+`generate_tables` (a Lorenz-Mie series over lognormal size distributions),
+since the GEOS optics_*.nc files are not part of this project.
+"""
+import ctypes
+import dataclasses
+import hashlib
+import os
+
+import numpy as np
+
+from . import _lib
+
+# Five GOCART-like species: name prefix, refractive index (n, k) of the dry
+# aerosol, dry density [kg m-3], hygroscopic growth (dust does not grow).
+SPECIES = [
+    ("su", 1.43, 0.0, 1700.0, True),      # sulfate
+    ("du", 1.53, 0.003, 2650.0, False),   # dust
+    ("ss", 1.50, 1.0e-8, 2200.0, True),   # sea salt
+    ("oc", 1.53, 0.006, 1800.0, True),    # organic carbon
+    ("bc", 1.75, 0.44, 1000.0, True),     # black carbon
+]
+NBIN = 4
+# dry number-mode radius and geometric width of the 4 size bins: log-spaced
+# 0.05..1.0 um, sigma_g 1.6..2.0
+BIN_RG_UM = tuple(0.05 * 20.0 ** (b / 3.0) for b in range(NBIN))
+BIN_SIGMA = tuple(1.6 + 0.4 * b / 3.0 for b in range(NBIN))
+NRH = 36
+
+
+@dataclasses.dataclass
+class MieTable:
+    """One species table in Chem_MieTable layout (Fortran order, REAL*4)."""
+    name: str
+    rh: np.ndarray      # (nrh,)
+    bext: np.ndarray    # (nrh, nch, nbin)
+    bsca: np.ndarray
+    g: np.ndarray
+    pmom: np.ndarray    # (nrh, nch, nbin, nmom, npol)
+
+
+@dataclasses.dataclass
+class MieTableSet:
+    channels_m: np.ndarray  # (nch,) wavelengths [m]
+    tables: list
+
+    def tracer_names(self):
+        return ["%s%03d" % (t.name, b + 1) for t in self.tables for b in range(t.bext.shape[2])]
+
+
+def _cache_dir():
+    d = os.environ.get("AERORT_CACHE")
+    if d:
+        return d
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "mie_cache")
+
+
+def generate_tables(channels_nm, nmom=64, nrh=NRH, nradii=160, use_cache=True):
+    """Synthetic GEOS-style Mie tables at the requested channels [nm].
+
+    RH nodes: nrh values evenly spaced on [0, 0.99] (REAL*4).  Wet particles:
+    radius x (1-RH)^-0.2, refractive index volume-mixed with water.
+    """
+    channels_nm = np.asarray(channels_nm, dtype=np.float64)
+    key = hashlib.sha256(repr((channels_nm.tolist(), nmom, nrh, nradii, SPECIES, BIN_RG_UM, BIN_SIGMA)).encode()).hexdigest()[:16]
+    path = os.path.join(_cache_dir(), "mie_%s.npz" % key)
+    rh = np.linspace(0.0, 0.99, nrh).astype(np.float32)
+    if use_cache and os.path.exists(path):
+        z = np.load(path)
+        tabs = []
+        for s in SPECIES:
+            n = s[0]
+            tabs.append(MieTable(n, rh, np.asfortranarray(z[n + "_bext"]), np.asfortranarray(z[n + "_bsca"]),
+                                 np.asfortranarray(z[n + "_g"]), np.asfortranarray(z[n + "_pmom"])))
+        return MieTableSet((channels_nm * 1e-9).astype(np.float32), tabs)
+    L = _lib.lib()
+    nch = len(channels_nm)
+    lam = np.ascontiguousarray(channels_nm * 1e-3)
+    rh64 = rh.astype(np.float64)
+    rg = np.array(BIN_RG_UM)
+    sg = np.array(BIN_SIGMA)
+    tabs = []
+    save = {}
+    for (name, nr, ni, rho, hyg) in SPECIES:
+        bext = np.zeros((nrh, nch, NBIN), np.float32, order="F")
+        bsca = np.zeros_like(bext)
+        g = np.zeros_like(bext)
+        pm = np.zeros((nrh, nch, NBIN, nmom), np.float32, order="F")
+        rc = L.aerort_miegen_lognormal(nch, _lib.ptr(lam, _lib.P_d), nrh, _lib.ptr(rh64, _lib.P_d), NBIN,
+                                       _lib.ptr(rg, _lib.P_d), _lib.ptr(sg, _lib.P_d), nr, ni, int(hyg), rho, nmom,
+                                       nradii, _lib.ptr(bext, _lib.P_f), _lib.ptr(bsca, _lib.P_f),
+                                       _lib.ptr(g, _lib.P_f), _lib.ptr(pm, _lib.P_f))
+        if rc != 0:
+            raise RuntimeError("Mie table generation failed for %s" % name)
+        pm = np.asfortranarray(pm.reshape(nrh, nch, NBIN, nmom, 1, order="F"))
+        tabs.append(MieTable(name, rh, bext, bsca, g, pm))
+        save.update({name + "_bext": bext, name + "_bsca": bsca, name + "_g": g, name + "_pmom": pm})
+    if use_cache:
+        os.makedirs(_cache_dir(), exist_ok=True)
+        tmp = path + ".tmp.npz"
+        np.savez(tmp, **save)
+        os.replace(tmp, path)
+    return MieTableSet((channels_nm * 1e-9).astype(np.float32), tabs)
+
+
+class ChemMie:
+    """Device-resident Chem_Mie object (Chem_MieMod.F90:41-47)."""
+
+    def __init__(self, tableset):
+        self.tableset = tableset
+        self.names = [t.name for t in tableset.tables]
+        descs = (_lib.MieTableDesc * len(tableset.tables))()
+        self._keep = []
+        for i, t in enumerate(tableset.tables):
+            arrs = [np.asfortranarray(t.rh, np.float32), np.asfortranarray(t.bext, np.float32),
+                    np.asfortranarray(t.bsca, np.float32), np.asfortranarray(t.g, np.float32),
+                    np.asfortranarray(t.pmom, np.float32)]
+            self._keep += arrs
+            descs[i].nrh = t.rh.shape[0]
+            descs[i].nbin = t.bext.shape[2]
+            descs[i].nmom = t.pmom.shape[3]
+            descs[i].npol = t.pmom.shape[4]
+            descs[i].rh, descs[i].bext, descs[i].bsca, descs[i].g, descs[i].pmom = [_lib.ptr(a, _lib.P_f) for a in arrs]
+        ch = np.ascontiguousarray(tableset.channels_m, np.float32)
+        h = ctypes.c_void_p()
+        rc = _lib.lib().aerort_mie_create(len(tableset.tables), descs, len(ch), _lib.ptr(ch, _lib.P_f), ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError("aerort_mie_create rc=%d: %s" % (rc, _lib.last_error()))
+        self.handle = h
+        self.channels = ch
+
+    def query_idx(self, vname):
+        """Chem_MieQueryIdx (Chem_MieMod.F90:720-777): tracer name -> (table, bin) or (-1, -1)."""
+        v = vname.strip().lower()
+        for ti, t in enumerate(self.tableset.tables):
+            for b in range(t.bext.shape[2]):
+                if v == "%s%03d" % (t.name, b + 1):
+                    return ti, b
+        return -1, -1
+
+    def destroy(self):
+        if self.handle:
+            _lib.lib().aerort_mie_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def get_aop_vector(mie, km, nobs, nch, nq, channels, vname, verbose, qm, rh, nMom, nPol):
+    """VLIDORT_getAOPvector (VLIDORT_MieMod.F90:124-336).
+
+    Returns (tau, ssa, g, pmom, rc) with the reference shapes
+    tau/ssa/g (km,nch,nobs), pmom (km,nch,nobs,nMom,nPol), FP32, Fortran order.
+    """
+    qtab = np.empty(nq, np.int32)
+    qbin = np.empty(nq, np.int32)
+    for iq in range(nq):
+        qtab[iq], qbin[iq] = mie.query_idx(vname[iq])
+    ch = np.ascontiguousarray(channels, np.float32)
+    qm = np.asfortranarray(qm, np.float32)
+    rh = np.asfortranarray(rh, np.float32)
+    tau = np.zeros((km, nch, nobs), np.float32, order="F")
+    ssa = np.zeros_like(tau)
+    g = np.zeros_like(tau)
+    pmom = np.zeros((km, nch, nobs, nMom, nPol), np.float32, order="F")
+    rc = _lib.lib().aerort_get_aop_vector(mie.handle, km, nobs, nch, nq, _lib.ptr(ch, _lib.P_f), _lib.ptr(qtab, _lib.P_i),
+                                          _lib.ptr(qbin, _lib.P_i), _lib.ptr(qm, _lib.P_f), _lib.ptr(rh, _lib.P_f),
+                                          nMom, nPol, _lib.ptr(tau, _lib.P_f), _lib.ptr(ssa, _lib.P_f),
+                                          _lib.ptr(g, _lib.P_f), _lib.ptr(pmom, _lib.P_f))
+    if rc not in (0, 99, 666, 777):
+        raise RuntimeError("aerort_get_aop_vector rc=%d: %s" % (rc, _lib.last_error()))
+    return tau, ssa, g, pmom, rc

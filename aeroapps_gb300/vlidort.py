@@ -1,0 +1,87 @@
+"""VLIDORT_Scalar_Lambert on the GPU, with the reference's argument list.
+
+Mirrors src/Components/rtms/geo_vlidort/VLIDORT_LAMBERT.F90:34-168 (and its
+f2py exposure, src/Components/rtms/leo_vlidort/VLIDORT_POLAR_py.F90): every
+array has the reference's shape and Fortran order; the return value is
+(radiance_VL, reflectance_VL, rc) as the f2py wrapper returns it.
+"""
+import numpy as np
+
+from . import _lib
+
+MISSING = -1.0e15
+STREAMS = (4, 6, 8, 12, 16)
+
+
+def _f64(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def vlidort_scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g,
+                           pmom, pe, he, te, albedo, solar_zenith, relat_azymuth, sensor_zenith, MISSING=MISSING,
+                           verbose=0, diagnostics=False):
+    """Scalar TOA radiance/reflectance for nobs pixels x nch channels.
+
+    Shapes: channels(nch) [nm], ROT(km,nobs,nch), depol(nch), tau/ssa/g(km,nch,nobs),
+    pmom(km,nch,nobs,nMom,nPol), pe/he/te(km+1,nobs), albedo(nobs,nch), angles(nobs).
+    With diagnostics=True also returns nfourier(nobs,nch) and status(nobs,nch).
+    """
+    arrs = [_f64(channels), _f64(ROT), _f64(depol), _f64(tau), _f64(ssa), _f64(g), _f64(pmom), _f64(pe), _f64(he),
+            _f64(te), _f64(albedo), _f64(solar_zenith), _f64(relat_azymuth), _f64(sensor_zenith)]
+    ch, ROT, depol, tau, ssa, g, pmom, pe, he, te, albedo, sza, raa, vza = arrs
+    if ROT.shape != (km, nobs, nch) or tau.shape != (km, nch, nobs) or he.shape != (km + 1, nobs):
+        raise ValueError("array shapes do not match (km, nch, nobs) = (%d, %d, %d)" % (km, nch, nobs))
+    if pmom.ndim != 5 or pmom.shape[:4] != (km, nch, nobs, nMom):
+        raise ValueError("pmom must have shape (km, nch, nobs, nMom, nPol)")
+    rad = np.zeros((nobs, nch), np.float64, order="F")
+    refl = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    P = lambda a: _lib.ptr(a, _lib.P_d)
+    rc = _lib.lib().aerort_vlidort_scalar_lambert_ex(
+        km, nch, nobs, P(ch), nstreams, int(bool(plane_parallel)), nMom, nPol, P(ROT), P(depol), P(tau), P(ssa), P(g),
+        P(pmom), P(pe), P(he), P(te), P(albedo), P(sza), P(raa), P(vza), float(MISSING), int(verbose), P(rad),
+        P(refl), _lib.ptr(nf, _lib.P_i), _lib.ptr(st, _lib.P_i))
+    if rc >= 1000:
+        raise RuntimeError("aerort_vlidort_scalar_lambert rc=%d: %s" % (rc, _lib.last_error()))
+    if diagnostics:
+        return rad, refl, rc, nf, st
+    return rad, refl, rc
+
+
+def vlidort_scalar_lambert_dev(km, nch, nobs, nstreams, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith,
+                               relat_azymuth, sensor_zenith, radiance, reflectance, nfourier=None, status=None,
+                               MISSING=MISSING, plane_parallel=False, stream=0):
+    """Device-pointer form: every array argument is a CUDA device address (int)."""
+    rc = _lib.lib().aerort_vlidort_scalar_lambert_dev(
+        km, nch, nobs, nstreams, int(bool(plane_parallel)), nMom, ROT, depol, tau, ssa, pmom, he, albedo,
+        solar_zenith, relat_azymuth, sensor_zenith, float(MISSING), radiance, reflectance, nfourier or 0,
+        status or 0, stream)
+    if rc != 0:
+        raise RuntimeError("aerort_vlidort_scalar_lambert_dev rc=%d: %s" % (rc, _lib.last_error()))
+    return rc
+
+
+def vlidort_scalar_lambert_batch(km, nch, nobs, nstreams, nMom, nlay, ROT, depol, tau, ssa, pmom, he, albedo,
+                                 solar_zenith, relat_azymuth, sensor_zenith, MISSING=MISSING, plane_parallel=False):
+    """Batched host call for columns of different layer counts (nlay(nobs), each <= km).
+
+    Same arrays as vlidort_scalar_lambert (pmom: the P11 moments, (km,nch,nobs,nMom));
+    returns (radiance, reflectance, rc, nfourier, status)."""
+    ROT, depol, tau, ssa, pmom, he, albedo, sza, raa, vza = [_f64(a) for a in (ROT, depol, tau, ssa, pmom, he, albedo,
+                                                                               solar_zenith, relat_azymuth,
+                                                                               sensor_zenith)]
+    nl = np.ascontiguousarray(nlay, np.int32)
+    rad = np.zeros((nobs, nch), np.float64, order="F")
+    refl = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    P = lambda a: _lib.ptr(a, _lib.P_d)
+    rc = _lib.lib().aerort_vlidort_scalar_lambert_batch(
+        km, nch, nobs, nstreams, int(bool(plane_parallel)), nMom, _lib.ptr(nl, _lib.P_i), P(ROT), P(depol), P(tau),
+        P(ssa), P(pmom), P(he), P(albedo), P(sza), P(raa), P(vza), float(MISSING), P(rad), P(refl),
+        _lib.ptr(nf, _lib.P_i), _lib.ptr(st, _lib.P_i))
+    if rc >= 1000:
+        raise RuntimeError("aerort_vlidort_scalar_lambert_batch rc=%d: %s" % (rc, _lib.last_error()))
+    return rad, refl, rc, nf, st
+

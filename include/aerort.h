@@ -1,0 +1,163 @@
+/* aerort: GB300-native aerosol optics + scalar VLIDORT-style radiative transfer.
+ *
+ * C ABI of the drop-in replacement for AeroApps' per-column hot path.  Every
+ * entry point takes plain pointers and sizes, Fortran column-major arrays with
+ * exactly the shapes of the reference routine it replaces, and returns the
+ * reference's integer rc.  Reference paths are relative to the AeroApps tree.
+ *
+ * Host-pointer entry points copy inputs to the GPU, run, and copy results
+ * back (a drop-in for the Fortran/f2py caller).  The *_dev variants take
+ * device pointers and a cudaStream_t (passed as void*) and never synchronise
+ * the host; they are the building blocks of batched/fused pipelines.
+ */
+#ifndef AERORT_H
+#define AERORT_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* rc values shared with the reference */
+#define AERORT_OK 0
+#define AERORT_RC_NSTREAMS 2       /* VLIDORT_Mod.F90:366  NSTREAMS > MAXSTREAMS (25)  */
+#define AERORT_RC_NLAYERS 3        /* VLIDORT_Mod.F90:367  NLAYERS  > MAXLAYERS  (72)  */
+#define AERORT_RC_NMOMENTS 5       /* VLIDORT_ScatMod.F90:1050  nmom > MAXMOMENTS_INPUT */
+#define AERORT_RC_CHANNEL 99       /* VLIDORT_MieMod.F90:219-224 channel not in the Mie table */
+#define AERORT_RC_MOMENTS 666      /* VLIDORT_MieMod.F90:237-241 table has too few moments */
+#define AERORT_RC_NPOL 777         /* VLIDORT_MieMod.F90:243-255 inconsistent nPol */
+/* rc values of this library (not produced by the reference) */
+#define AERORT_RC_CUDA 1001        /* CUDA runtime error (message via aerort_last_error) */
+#define AERORT_RC_ARG 1002         /* invalid argument (null pointer, non-positive size) */
+#define AERORT_RC_UNSUPPORTED 1003 /* configuration not built (e.g. nstreams not in {4,6,8,12,16}) */
+
+/* per-pixel status written by the *_ex / *_dev RT entry points */
+#define AERORT_ST_OK 0
+#define AERORT_ST_EIGEN 1          /* layer eigenproblem failed (reference: ASYMTX error, rc 4)   */
+#define AERORT_ST_BVP 2            /* singular boundary-value system (reference: DGBTRF info > 0) */
+#define AERORT_ST_INPUT 3          /* non-positive extinction / scattering optical depth          */
+
+/* ------------------------------------------------------------------------------------------
+ * Mie tables (Chem_Mie object).
+ * Replaces Chem_MieCreate / Chem_MieTableRead (Chem_Base/Chem_MieMod.F90:124-411,
+ * Chem_MieTableMod.F90:238-719) once the tables are in memory: uploads the
+ * per-species tables, already on the requested channels, and builds the RH map
+ * (Chem_MieTableMod.F90:612-627).  Arrays are REAL*4, Fortran order:
+ *   rh(nrh); bext,bsca,g (nrh,nch,nbin); pmom (nrh,nch,nbin,nmom,npol).
+ * channels_m(nch): table wavelengths in metres (as Chem_Mie%channels).
+ */
+typedef struct aerort_mie aerort_mie;
+
+typedef struct {
+  int nrh, nbin, nmom, npol;
+  const float* rh;
+  const float* bext;
+  const float* bsca;
+  const float* g;
+  const float* pmom;
+} aerort_mie_table_desc;
+
+int aerort_mie_create(int ntables, const aerort_mie_table_desc* tables, int nch, const float* channels_m,
+                      aerort_mie** out);
+int aerort_mie_destroy(aerort_mie* mie);
+
+/* VLIDORT_getAOPvector (geo_vlidort/VLIDORT_MieMod.F90:124-336) with
+ * Chem_MieQuery (Chem_MieMod.F90:789-965) for every tracer.  The tracer names
+ * vname(nq,16) of the reference are resolved by the caller (Chem_MieQueryIdx,
+ * Chem_MieMod.F90:720-777) into q_table(nq) (species table index, -1 = tracer
+ * without optics, skipped like the reference's idxTable == -1) and q_bin(nq)
+ * (0-based size bin).  Shapes: channels_nm(nch) [nm], qm(km,nq,nobs),
+ * rh(km,nobs), tau/ssa/g(km,nch,nobs), pmom(km,nch,nobs,nMom,nPol).  FP32,
+ * bit-identical to the reference arithmetic. */
+int aerort_get_aop_vector(aerort_mie* mie, int km, int nobs, int nch, int nq, const float* channels_nm,
+                          const int* q_table, const int* q_bin, const float* qm, const float* rh, int nMom,
+                          int nPol, float* tau, float* ssa, float* g, float* pmom);
+int aerort_get_aop_vector_dev(aerort_mie* mie, int km, int nobs, int nch, int nq, const float* channels_nm_host,
+                              const int* q_table_host, const int* q_bin_host, const float* qm_dev,
+                              const float* rh_dev, int nMom, int nPol, float* tau_dev, float* ssa_dev,
+                              float* g_dev, float* pmom_dev, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * VLIDORT_Scalar_Lambert (geo_vlidort/VLIDORT_LAMBERT.F90:34-168): scalar TOA
+ * radiance and reflectance for nobs pixels x nch channels, observation
+ * geometry, Lambertian surface, with the VLIDORT_Init settings of
+ * VLIDORT2p8p3/VLIDORT_Mod.F90:65-383 (FO outgoing correction, delta-M,
+ * pseudo-spherical, double convergence test at accuracy 1e-4) and the layer
+ * mixing of VLIDORT_Run_Scalar (VLIDORT_ScatMod.F90:975-1247).
+ * Shapes: channels(nch) [nm], ROT(km,nobs,nch), depol(nch), tau/ssa/g(km,nch,nobs),
+ * pmom(km,nch,nobs,nMom,nPol), pe/he/te(km+1,nobs) [Pa, m, K], albedo(nobs,nch),
+ * solar_zenith/relat_azymuth/sensor_zenith(nobs) [deg], radiance_VL/reflectance_VL(nobs,nch).
+ * Pixels whose angles or albedo are MISSING (|x/MISSING-1| < 1e-3), or whose
+ * solve fails, get MISSING, as in the reference.  FP64.  nstreams must be one
+ * of 4, 6, 8, 12, 16 (the compiled stream counts). */
+int aerort_vlidort_scalar_lambert(int km, int nch, int nobs, const double* channels, int nstreams,
+                                  int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                  const double* tau, const double* ssa, const double* g, const double* pmom,
+                                  const double* pe, const double* he, const double* te, const double* albedo,
+                                  const double* solar_zenith, const double* relat_azymuth,
+                                  const double* sensor_zenith, double MISSING, int verbose, double* radiance_VL,
+                                  double* reflectance_VL);
+
+/* Same, plus per-pixel diagnostics: nfourier(nobs,nch) = last Fourier term
+ * summed, status(nobs,nch) = AERORT_ST_* (either may be NULL). */
+int aerort_vlidort_scalar_lambert_ex(int km, int nch, int nobs, const double* channels, int nstreams,
+                                     int plane_parallel, int nMom, int nPol, const double* ROT,
+                                     const double* depol, const double* tau, const double* ssa, const double* g,
+                                     const double* pmom, const double* pe, const double* he, const double* te,
+                                     const double* albedo, const double* solar_zenith,
+                                     const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                     int verbose, double* radiance_VL, double* reflectance_VL, int* nfourier,
+                                     int* status);
+
+/* Device-pointer form of aerort_vlidort_scalar_lambert_ex (all array arguments
+ * are device pointers, channels/pe/te unused).  Enqueued on `stream`. */
+int aerort_vlidort_scalar_lambert_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                      const double* ROT, const double* depol, const double* tau,
+                                      const double* ssa, const double* pmom, const double* he,
+                                      const double* albedo, const double* solar_zenith,
+                                      const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                      double* radiance_VL, double* reflectance_VL, int* nfourier, int* status,
+                                      void* stream);
+
+/* Batched device form for mixed column shapes (one launch per stream count):
+ * nlay(nobs) (device, may be NULL = all km) gives the layer count of each
+ * column, which uses the first nlay entries of its km-dimensioned arrays
+ * (layer 1 = top); the optics may be given as FP32 device arrays straight
+ * from aerort_get_aop_vector_dev (tau_f, ssa_f, pmom_f; pass NULL for the FP64
+ * tau, ssa, pmom), in which case the FP64 conversion the reference driver does
+ * (dble(), geo_vlidort.F90:598-601) happens on load.  No counterpart routine in
+ * the reference: it batches many VLIDORT_Scalar_Lambert calls into one launch. */
+int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                            const int* nlay, const double* ROT, const double* depol,
+                                            const double* tau, const double* ssa, const double* pmom,
+                                            const float* tau_f, const float* ssa_f, const float* pmom_f,
+                                            const double* he, const double* albedo, const double* solar_zenith,
+                                            const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                            double* radiance_VL, double* reflectance_VL, int* nfourier, int* status,
+                                            void* stream);
+
+/* Host-pointer form of the batched call (same extension as above, FP64
+ * optics, nlay(nobs) host array or NULL).  No counterpart routine in the
+ * reference: it replaces a loop of VLIDORT_Scalar_Lambert calls over columns
+ * of different layer counts with one launch. */
+int aerort_vlidort_scalar_lambert_batch(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                        const int* nlay, const double* ROT, const double* depol, const double* tau,
+                                        const double* ssa, const double* pmom, const double* he,
+                                        const double* albedo, const double* solar_zenith,
+                                        const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                        double* radiance_VL, double* reflectance_VL, int* nfourier, int* status);
+
+/* ------------------------------------------------------------------------------------------ misc */
+/* Diagnostic, no counterpart in the reference: enqueue blocks x threads
+ * threads each running 8 independent FP64 FMA chains for `iters` rounds
+ * (16 * iters flops per thread); timing it gives the FP64 pipe rate. */
+int aerort_probe_dfma(int blocks, int threads, int iters, double* out_dev, void* stream);
+
+const char* aerort_last_error(void);  /* last error message of the calling thread */
+int aerort_version(void);             /* 100 * major + minor */
+/* Release the library's cached device buffers and streams (optional). */
+int aerort_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AERORT_H */

@@ -1,0 +1,115 @@
+"""ctypes access to the CPU oracle (test infrastructure only: imported by tests/,
+__graft_entry__.smoke() and the cpu_baseline / reference arm of bench.py)."""
+import ctypes
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+P_d = ctypes.POINTER(ctypes.c_double)
+P_f = ctypes.POINTER(ctypes.c_float)
+P_i = ctypes.POINTER(ctypes.c_int)
+
+
+class OracleOpts(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("do_focorr", "do_focorr_nadir", "do_focorr_outgoing", "do_deltam",
+                                              "do_plane_parallel", "do_double_convtest", "nfinelayers",
+                                              "taylor_order")] + \
+               [(n, ctypes.c_double) for n in ("accuracy", "asymtx_tol", "earth_radius", "flux_factor")]
+
+
+class OracleMieTable(ctypes.Structure):
+    _fields_ = [("nrh", ctypes.c_int), ("nch", ctypes.c_int), ("nbin", ctypes.c_int), ("nmom", ctypes.c_int),
+                ("npol", ctypes.c_int), ("rh", P_f), ("channels", P_f), ("bext", P_f), ("bsca", P_f), ("g", P_f),
+                ("pmom", P_f), ("rhi", P_i), ("rha", P_f)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(_build.build())
+        _lib.oracle_vlidort_solve.restype = ctypes.c_int
+        _lib.oracle_scalar_lambert.restype = ctypes.c_int
+        _lib.oracle_get_aop_vector.restype = ctypes.c_int
+    return _lib
+
+
+def _p(a, kind):
+    return a.ctypes.data_as(kind)
+
+
+def vlidort_solve(opts, heights, deltau, omega, greek, albedo, sza, vzas, raas, nstreams):
+    """Single-beam solve (lattice of vzas x raas). greek: (L, ngreek+1). Returns (out[nvza, nraa], nfourier, status)."""
+    heights = np.ascontiguousarray(heights, np.float64)
+    deltau = np.ascontiguousarray(deltau, np.float64)
+    omega = np.ascontiguousarray(omega, np.float64)
+    greek = np.ascontiguousarray(greek, np.float64)
+    L, g1 = greek.shape
+    vz = np.ascontiguousarray(vzas, np.float64)
+    ra = np.ascontiguousarray(raas, np.float64)
+    out = np.zeros(len(vz) * len(ra))
+    nf = ctypes.c_int(0)
+    st = lib().oracle_vlidort_solve(ctypes.byref(opts), L, nstreams, g1 - 1, _p(heights, P_d), _p(deltau, P_d),
+                                    _p(omega, P_d), _p(greek, P_d), ctypes.c_double(albedo), ctypes.c_double(sza),
+                                    len(vz), _p(vz, P_d), len(ra), _p(ra, P_d), _p(out, P_d), ctypes.byref(nf))
+    return out.reshape(len(vz), len(ra)), nf.value, st
+
+
+def scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g, pmom, pe, he,
+                   te, albedo, solar_zenith, relat_azymuth, sensor_zenith, MISSING, verbose=0, nlay=None):
+    """Oracle VLIDORT_Scalar_Lambert; returns (radiance, reflectance, rc, nfourier, status)."""
+    F = lambda a: np.asfortranarray(a, np.float64)
+    arr = [F(x) for x in (channels, ROT, depol, tau, ssa, g, pmom, pe, he, te, albedo, solar_zenith, relat_azymuth,
+                          sensor_zenith)]
+    rad = np.zeros((nobs, nch), order="F")
+    refl = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    c, rot, dep, ta, ss, gg, pm, p_e, h_e, t_e, al, sz, ra, vz = arr
+    rc = lib().oracle_scalar_lambert(km, nch, nobs, _p(c, P_d), nstreams, int(plane_parallel), nMom, nPol, _p(rot, P_d),
+                                     _p(dep, P_d), _p(ta, P_d), _p(ss, P_d), _p(gg, P_d), _p(pm, P_d), _p(p_e, P_d),
+                                     _p(h_e, P_d), _p(t_e, P_d), _p(al, P_d), _p(sz, P_d), _p(ra, P_d), _p(vz, P_d),
+                                     ctypes.c_double(MISSING), int(verbose), _p(rad, P_d), _p(refl, P_d),
+                                     _p(nf, P_i), _p(st, P_i),
+                                     None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
+    return rad, refl, rc, nf, st
+
+
+def rh_map(rh):
+    rh = np.ascontiguousarray(rh, np.float32)
+    rhi = np.zeros(991, np.int32)
+    rha = np.zeros(991, np.float32)
+    lib().oracle_mie_rhmap(len(rh), _p(rh, P_f), _p(rhi, P_i), _p(rha, P_f))
+    return rhi, rha
+
+
+def get_aop_vector(tableset, km, nobs, nch, nq, channels_nm, q_table, q_bin, qm, rh, nMom, nPol):
+    """Oracle VLIDORT_getAOPvector on a mie.MieTableSet; returns (tau, ssa, g, pmom, rc)."""
+    keep = []
+    tabs = (OracleMieTable * len(tableset.tables))()
+    ch = np.ascontiguousarray(tableset.channels_m, np.float32)
+    keep.append(ch)
+    for i, t in enumerate(tableset.tables):
+        arrs = [np.ascontiguousarray(t.rh, np.float32)] + [np.asfortranarray(x, np.float32) for x in (t.bext, t.bsca, t.g, t.pmom)]
+        rhi, rha = rh_map(t.rh)
+        keep += arrs + [rhi, rha]
+        tabs[i].nrh, tabs[i].nch, tabs[i].nbin = t.bext.shape
+        tabs[i].nmom, tabs[i].npol = t.pmom.shape[3], t.pmom.shape[4]
+        tabs[i].rh, tabs[i].bext, tabs[i].bsca, tabs[i].g, tabs[i].pmom = [_p(a, P_f) for a in arrs]
+        tabs[i].channels = _p(ch, P_f)
+        tabs[i].rhi = _p(rhi, P_i)
+        tabs[i].rha = _p(rha, P_f)
+    cn = np.ascontiguousarray(channels_nm, np.float32)
+    qt = np.ascontiguousarray(q_table, np.int32)
+    qb = np.ascontiguousarray(q_bin, np.int32)
+    qm = np.asfortranarray(qm, np.float32)
+    rh = np.asfortranarray(rh, np.float32)
+    tau = np.zeros((km, nch, nobs), np.float32, order="F")
+    ssa = np.zeros_like(tau)
+    g = np.zeros_like(tau)
+    pmom = np.zeros((km, nch, nobs, nMom, nPol), np.float32, order="F")
+    rc = lib().oracle_get_aop_vector(len(tableset.tables), tabs, km, nobs, nch, nq, _p(cn, P_f), _p(qt, P_i), _p(qb, P_i),
+                                     _p(qm, P_f), _p(rh, P_f), nMom, nPol, _p(tau, P_f), _p(ssa, P_f), _p(g, P_f),
+                                     _p(pmom, P_f))
+    return tau, ssa, g, pmom, rc

@@ -1370,7 +1370,7 @@ extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* ch
                                      const double* te, const double* albedo, const double* solar_zenith,
                                      const double* relat_azymuth, const double* sensor_zenith, double MISSING,
                                      int verbose, double* radiance, double* reflectance, int* nfourier,
-                                     int* status) {
+                                     int* status, const int* nlay) {
   (void)channels; (void)nPol; (void)pe; (void)te; (void)verbose; (void)g;
   // VLIDORT_Init error checks (VLIDORT_Mod.F90:365-374): MAXSTREAMS=25, MAXLAYERS=72
   if (nstreams > 25) return 2;
@@ -1405,10 +1405,11 @@ extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* ch
       radiance[o] = MISSING; reflectance[o] = MISSING;
       continue;
     }
-    std::vector<double> dt(km), om(km), gr((size_t)(nMom + 1) * km, 0.0), hg(km + 1);
+    const int L = nlay ? nlay[j] : km;  // column uses its first L layers (extension for ragged batches)
+    std::vector<double> dt(L), om(L), gr((size_t)(nMom + 1) * L, 0.0), hg(L + 1);
     const double dep = depol[i];
     const double raysmom2 = (1.0 - dep) / (2.0 + dep);
-    for (int k = 0; k < km; ++k) {
+    for (int k = 0; k < L; ++k) {
       double ray_l = ROT[k + (size_t)km * (j + (size_t)nobs * i)];
       size_t a = k + (size_t)km * (i + (size_t)nch * j);
       double tau_l = tau[a], ssa_l = ssa[a];
@@ -1427,7 +1428,7 @@ extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* ch
       G[2] = raysmom2 * rayswt + aersmom(2) * aerswt;
       for (int l = 3; l <= nMom; ++l) G[l] = aersmom(l) * aerswt;
     }
-    for (int k = 0; k <= km; ++k) hg[k] = he[k + (size_t)(km + 1) * j] * height_scale;
+    for (int k = 0; k <= L; ++k) hg[k] = he[k + (size_t)(km + 1) * j] * height_scale;
     OracleOpts op;
     op.do_focorr = 1;
     op.do_focorr_nadir = nadir[j] ? 1 : 0;
@@ -1443,7 +1444,7 @@ extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* ch
     op.flux_factor = 1.0;
     double sza = solar_zenith[j], vz = sensor_zenith[j], az = relat_azymuth[j], rad = 0.0;
     int nf = -1;
-    int rc = oracle_vlidort_solve(&op, km, nstreams, nMom, hg.data(), dt.data(), om.data(), gr.data(),
+    int rc = oracle_vlidort_solve(&op, L, nstreams, nMom, hg.data(), dt.data(), om.data(), gr.data(),
                                   albedo[o], sza, 1, &vz, 1, &az, &rad, &nf);
     if (nfourier) nfourier[o] = nf;
     if (status) status[o] = rc;

@@ -1,0 +1,28 @@
+"""Shared input builders for the RT parity tests."""
+import numpy as np
+
+from aeroapps_gb300 import synth
+
+MISSING = -1.0e15
+
+
+def random_aop_case(nstreams, km, nobs, nch=2, seed=0, ssa_range=(0.8, 1.0)):
+    """Columns from synth (grid, Rayleigh, geometry) with random Henyey-Greenstein-like aerosol optics."""
+    rng = np.random.default_rng(seed)
+    ch = [470.0, 550.0, 670.0, 865.0][:nch]
+    c = synth.make_columns(nobs, ch, seed=seed + 11, nlayers=km)
+    nmom = 2 * nstreams
+    tau = np.exp(rng.normal(-4.0, 1.5, (km, nch, nobs)))
+    ssa = rng.uniform(ssa_range[0], ssa_range[1], (km, nch, nobs))
+    g = rng.uniform(0.5, 0.8, (km, nch, nobs))
+    pmom = np.zeros((km, nch, nobs, nmom, 1))
+    for l in range(nmom):
+        pmom[..., l, 0] = (2 * l + 1) * g ** l
+    F = np.asfortranarray
+    c.update(tau=F(tau), ssa=F(ssa), g=F(g), pmom=F(pmom), nmom=nmom)
+    return c
+
+
+def rt_args(c, nstreams):
+    return (c["km"], c["nch"], c["ncol"], c["channels"], nstreams, False, c["nmom"], 1, c["ROT"], c["depol"], c["tau"],
+            c["ssa"], c["g"], c["pmom"], c["pe"], c["he"], c["te"], c["albedo"], c["sza"], c["raa"], c["vza"])

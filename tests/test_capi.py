@@ -1,0 +1,43 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every entry point
+declared in include/aerort.h (no GPU needed: nothing is called that touches CUDA)."""
+import ctypes
+import os
+import re
+
+from aeroapps_gb300 import _lib, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "aerort.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(aerort_\w+)\s*\(", src)))
+
+
+def test_library_builds_and_exports_header_symbols():
+    path = build.build()
+    assert os.path.exists(path)
+    h = ctypes.CDLL(path)
+    names = _declared()
+    assert "aerort_vlidort_scalar_lambert" in names and "aerort_get_aop_vector" in names
+    missing = [n for n in names if not hasattr(h, n)]
+    assert not missing, missing
+
+
+def test_version_and_error_string_without_gpu():
+    L = _lib.lib()
+    assert L.aerort_version() >= 10
+    assert isinstance(L.aerort_last_error(), bytes)
+
+
+def test_argument_checks_return_reference_rc_codes():
+    # VLIDORT_Init limits (VLIDORT_Mod.F90:365-374) are checked before any CUDA call
+    L = _lib.lib()
+    null = None
+    rc = L.aerort_vlidort_scalar_lambert(80, 1, 1, null, 8, 0, 16, 1, *([null] * 13), -1e15, 0, null, null)
+    assert rc == 3  # NLAYERS > MAXLAYERS
+    rc = L.aerort_vlidort_scalar_lambert(72, 1, 1, null, 30, 0, 16, 1, *([null] * 13), -1e15, 0, null, null)
+    assert rc == 2  # NSTREAMS > MAXSTREAMS
+    rc = L.aerort_vlidort_scalar_lambert(72, 1, 1, null, 8, 0, 2000, 1, *([null] * 13), -1e15, 0, null, null)
+    assert rc == 5  # nmom > MAXMOMENTS_INPUT

@@ -1,0 +1,55 @@
+"""The per-thread RT solver of the CUDA kernel (aeroapps_gb300/csrc/rt_solve.cuh),
+compiled for the host by this test only, against the oracle.  This checks the
+GPU formulation (symmetric eigen-reduction, block boundary-value sweep,
+top-down single-scatter integration) on the CPU; the GPU tests check the
+kernel itself."""
+import ctypes
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+from rt_cases import MISSING, random_aop_case, rt_args
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def host_lib():
+    d = tempfile.mkdtemp(prefix="aerort_host_")
+    so = os.path.join(d, "librthost.so")
+    subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-o", so,
+                    os.path.join(HERE, "host_harness", "rt_host.cpp")], check=True)
+    return ctypes.CDLL(so)
+
+
+def _host(lib, c, nstreams):
+    P = lambda a: np.asfortranarray(a, np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    keep = [np.asfortranarray(c[k], np.float64) for k in ("ROT", "depol", "tau", "ssa", "pmom", "he", "albedo", "sza",
+                                                            "raa", "vza")]
+    ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in keep]
+    nobs, nch = c["ncol"], c["nch"]
+    rad = np.zeros((nobs, nch), order="F")
+    refl = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    first = np.array([nobs], np.int32)
+    Ip = ctypes.POINTER(ctypes.c_int)
+    lib.host_scalar_lambert(c["km"], nch, nobs, nstreams, c["nmom"], *ptrs, first.ctypes.data_as(Ip),
+                            ctypes.c_double(MISSING), -1, rad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                            refl.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nf.ctypes.data_as(Ip),
+                            st.ctypes.data_as(Ip))
+    return rad, nf, st
+
+
+@pytest.mark.parametrize("nstreams,km", [(8, 72), (4, 20), (16, 12)])
+def test_host_build_of_kernel_matches_oracle(host_lib, nstreams, km):
+    c = random_aop_case(nstreams, km, nobs=4, nch=1, seed=km + nstreams)
+    rad, nf, st = _host(host_lib, c, nstreams)
+    orad, orefl, orc, onf, ost = oracle.scalar_lambert(*rt_args(c, nstreams), MISSING)
+    assert np.array_equal(nf, onf) and np.all(st == 0)
+    assert np.max(np.abs(rad / orad - 1)) < 1e-9
