@@ -163,18 +163,38 @@ RT_HD int layer_eigen(const SolveCtx<NS>& c, int m, double dtau, const double* o
       H[i + NS * j] = s; H[j + NS * i] = s;
     }
   if (!sym_eigen<NS>(N, H, V, lam)) return RT_EIGEN_FAIL;
+  // As = La La^T: the eigenvalues are recomputed as Rayleigh quotients
+  // lam = q^T R^T As R q = |La^T (R q)|^2, which keeps full relative accuracy
+  // for the small eigenvalues of nearly conservative layers (forming H
+  // explicitly leaves them an absolute error of order eps*|H|).
+  for (int j = 0; j < N; ++j)
+    for (int i = j; i < N; ++i) {
+      double a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
+      if (i == j) a += 1.0;
+      H[i + NS * j] = a;
+    }
+  if (!cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
   for (int a = 0; a < N; ++a) {
-    if (!(lam[a] > 0.0)) return RT_EIGEN_FAIL;
-    double k = sqrt(lam[a]);
-    kv[a] = k;
-    // sum vector x = W^-1/2 R q, unit 2-norm
-    double x[NS], nrm = 0.0;
+    // v = R q ; sum vector x = W^-1/2 v, unit 2-norm
+    double x[NS], v[NS], nrm = 0.0;
     for (int i = 0; i < N; ++i) {
       double s = 0.0;
       for (int j = 0; j <= i; ++j) s += Bs[i + NS * j] * V[j + NS * a];
+      v[i] = s;
       x[i] = s / c.sqw[i];
       nrm += x[i] * x[i];
     }
+    double qq = 0.0, lr = 0.0;
+    for (int i = 0; i < N; ++i) {
+      qq += V[i + NS * a] * V[i + NS * a];
+      double w = 0.0;
+      for (int j = i; j < N; ++j) w += H[j + NS * i] * v[j];
+      lr += w * w;
+    }
+    lr /= qq;
+    if (!(lr > 0.0)) return RT_EIGEN_FAIL;
+    double k = sqrt(lr);
+    kv[a] = k;
     nrm = 1.0 / sqrt(nrm);
     for (int i = 0; i < N; ++i) x[i] *= nrm;
     // difference vector SAB x / k ; SAB(i,j) = (delta_ij - w_j Sp(i,j)) / mu_i

@@ -32,6 +32,7 @@ def lib():
         _lib.oracle_vlidort_solve.restype = ctypes.c_int
         _lib.oracle_scalar_lambert.restype = ctypes.c_int
         _lib.oracle_get_aop_vector.restype = ctypes.c_int
+        _lib.oracle_set_asymtx_tol.restype = None
     return _lib
 
 
@@ -74,6 +75,11 @@ def scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol
                                      _p(nf, P_i), _p(st, P_i),
                                      None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
     return rad, refl, rc, nf, st
+
+
+def set_asymtx_tol(tol):
+    """Tolerance of the oracle's ASYMTX in scalar_lambert (reference: 1e-12)."""
+    lib().oracle_set_asymtx_tol(ctypes.c_double(tol))
 
 
 def rh_map(rh):

@@ -1363,6 +1363,12 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
 // Pixels are independent apart from the sticky nadir-FO flag, which is resolved
 // up front in loop order, so the loop runs with OpenMP over pixels.
 // nfourier (nobs,nch) and status (nobs,nch) are optional diagnostics.
+// ASYMTX tolerance used by oracle_scalar_lambert: AeroApps sets 1.0d-12
+// (VLIDORT2p8p3/VLIDORT_Mod.F90:355); tests may tighten it to check how far
+// that tolerance moves the reference algorithm from the converged solution.
+static double g_asymtx_tol = 1.0e-12;
+extern "C" void oracle_set_asymtx_tol(double tol) { g_asymtx_tol = tol; }
+
 extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* channels, int nstreams,
                                      int plane_parallel, int nMom, int nPol, const double* ROT,
                                      const double* depol, const double* tau, const double* ssa,
@@ -1439,7 +1445,7 @@ extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* ch
     op.nfinelayers = 3;
     op.taylor_order = 3;
     op.accuracy = (double)0.0001f;  // VLIDORT_Mod.F90: VLIDORT_ACCURACY = 0.0001 (REAL literal)
-    op.asymtx_tol = 1.0e-12;
+    op.asymtx_tol = g_asymtx_tol;
     op.earth_radius = 6371.0;
     op.flux_factor = 1.0;
     double sza = solar_zenith[j], vz = sensor_zenith[j], az = relat_azymuth[j], rad = 0.0;

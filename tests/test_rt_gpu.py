@@ -15,9 +15,14 @@ from rt_cases import MISSING, random_aop_case, rt_args
 RTOL = 1e-9
 
 
-def _compare(c, nstreams):
+def _compare(c, nstreams, rtol=RTOL, asymtx_tol=None):
     rad, refl, rc, nf, st = vlidort.vlidort_scalar_lambert(*rt_args(c, nstreams), MISSING=MISSING, diagnostics=True)
-    orad, orefl, orc, onf, ost = oracle.scalar_lambert(*rt_args(c, nstreams), MISSING)
+    if asymtx_tol is not None:
+        oracle.set_asymtx_tol(asymtx_tol)
+    try:
+        orad, orefl, orc, onf, ost = oracle.scalar_lambert(*rt_args(c, nstreams), MISSING)
+    finally:
+        oracle.set_asymtx_tol(1.0e-12)
     assert rc == 0 and orc == 0
     assert np.array_equal(st, ost)
     assert np.array_equal(nf, onf)
@@ -25,8 +30,8 @@ def _compare(c, nstreams):
     assert np.array_equal(rad == MISSING, ~ok)
     err = np.abs(rad[ok] / orad[ok] - 1.0)
     erf = np.abs(refl[ok] / orefl[ok] - 1.0)
-    assert err.max() <= RTOL, err.max()
-    assert erf.max() <= RTOL, erf.max()
+    assert err.max() <= rtol, err.max()
+    assert erf.max() <= rtol, erf.max()
     return rad, nf
 
 
@@ -39,9 +44,18 @@ def test_matches_oracle(nstreams, km):
 
 @pytest.mark.gpu
 def test_near_conservative_layers():
-    # layer SSA capped at 0.99999 by the wrapper (VLIDORT_ScatMod.F90:1169)
+    # Layer SSA capped at 0.99999 by the wrapper (VLIDORT_ScatMod.F90:1169).
+    # Here the reference algorithm itself is tolerance-limited: ASYMTX stops its
+    # QR iteration at the 1e-12 tolerance AeroApps sets (VLIDORT_Mod.F90:355),
+    # which leaves the smallest eigenvalue of a nearly conservative layer with a
+    # relative error that reaches the TOA radiance at the 3e-9 level.  The
+    # kernel (symmetric reduction + Rayleigh-quotient eigenvalues) is compared
+    # at 1e-9 with the oracle run to convergence (ASYMTX tolerance 1e-15, within
+    # 2e-11 of an 80-bit solution of the same case) and at 1e-8 with the oracle
+    # at the reference tolerance.
     c = random_aop_case(8, 72, nobs=32, nch=1, seed=5, ssa_range=(0.9999, 1.0))
-    _compare(c, 8)
+    _compare(c, 8, rtol=1e-9, asymtx_tol=1.0e-15)
+    _compare(c, 8, rtol=1e-8)
 
 
 @pytest.mark.gpu
