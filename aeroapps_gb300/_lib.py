@@ -39,6 +39,8 @@ _SIGNATURES = {
                                           [c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "aerort_vlidort_scalar_lambert_batch_dev": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int] + [c_void_p] * 14 +
                                                 [c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "aerort_vlidort_scalar_lambert_batch_dev_noalloc": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int] +
+                                                        [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
     "aerort_vlidort_scalar_lambert_batch": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, P_i] + [P_d] * 10 +
                                             [c_double, P_d, P_d, P_i, P_i]),
     "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),

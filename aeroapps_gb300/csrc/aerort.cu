@@ -473,6 +473,37 @@ extern "C" int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs
                           status, (cudaStream_t)stream);
 }
 
+extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
+    int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom, const int* nlay, const double* ROT,
+    const double* depol, const double* tau, const double* ssa, const double* pmom, const float* tau_f,
+    const float* ssa_f, const float* pmom_f, const double* he, const double* albedo, const double* solar_zenith,
+    const double* relat_azymuth, const double* sensor_zenith, double MISSING, double* radiance_VL,
+    double* reflectance_VL, int* nfourier, int* status, void* stream) {
+  if (int rc = lambert_checks(km, nch, nobs, nstreams, nMom)) return rc;
+  if ((!tau_f && (!tau || !ssa || !pmom)) || (tau_f && (!ssa_f || !pmom_f)))
+    return set_error(AERORT_RC_ARG, "scalar_lambert_noalloc: optics missing");
+  if ((long)nobs * nch > 0x7fffff00L) return set_error(AERORT_RC_ARG, "scalar_lambert_noalloc: nobs * nch too large");
+  double* arena = nullptr;
+  size_t arena_doubles = 0;
+  int* sched = nullptr;
+  int num_sms = 0;
+  if (int rc = static_arena(&arena, &arena_doubles, &sched, &num_sms)) return rc;
+  LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
+                   sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
+  const RtOptions opt = lambert_options(plane_parallel);
+  cudaStream_t s = (cudaStream_t)stream;
+  double* r = radiance_VL;
+  double* f = reflectance_VL;
+  switch (nstreams) {
+    case 4: return launch_scalar_lambert_fixed<4>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
+    case 6: return launch_scalar_lambert_fixed<6>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
+    case 8: return launch_scalar_lambert_fixed<8>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
+    case 12: return launch_scalar_lambert_fixed<12>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
+    case 16: return launch_scalar_lambert_fixed<16>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
+  }
+  return set_error(AERORT_RC_UNSUPPORTED, "nstreams must be one of 4, 6, 8, 12, 16");
+}
+
 extern "C" int aerort_vlidort_scalar_lambert_ex(int km, int nch, int nobs, const double* channels, int nstreams,
                                                 int plane_parallel, int nMom, int nPol, const double* ROT,
                                                 const double* depol, const double* tau, const double* ssa,

@@ -54,4 +54,13 @@ template <int NS>
 int launch_scalar_lambert(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
                           double* refl, int* nf, int* st, cudaStream_t s);
 
+template <int NS>
+int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* arena,
+                                size_t arena_doubles, int* sched, int num_sms, double* rad, double* refl, int* nf,
+                                int* st, cudaStream_t s);
+
+// Static device arena of the allocation-free entry point (rt_static.cu):
+// address of the calling thread's current device's copy, set up on first use.
+int static_arena(double** arena, size_t* arena_doubles, int** sched, int* num_sms);
+
 }  // namespace aerort_internal

@@ -65,9 +65,54 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   return 0;
 }
 
+// Same launch on caller-independent fixed storage: the per-thread scratch
+// comes from a static arena of arena_doubles doubles and the two scheduling
+// ints from sched (both reset or fully rewritten here, so neither needs to
+// start at zero).  The persistent grid is capped so that its threads' scratch
+// fits the arena; any nobs is then covered by the work queue.
+template <int NS>
+int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, double* arena, size_t arena_doubles,
+                                int* sched, int num_sms, double* rad, double* refl, int* nf, int* st,
+                                cudaStream_t s) {
+  const int nsolve = in.nobs * in.nch;
+  if (nsolve == 0) return 0;
+  const int bs = 64;
+  const ScratchLayout<NS> lay(in.km);
+  const long fit_blocks = (long)(arena_doubles / ((size_t)lay.total * bs));
+  if (fit_blocks < 1)
+    return set_error(AERORT_RC_ARG, "scalar_lambert_noalloc: one 64-thread block needs more scratch than the "
+                                    "static arena holds");
+  Quad q;
+  std::memset(&q, 0, sizeof(q));
+  gauss_legendre01(NS, q.qx, q.qw);
+  if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
+  int per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS>, bs, 0));
+  if (per_sm < 1) per_sm = 1;
+  long nblocks = (nsolve + bs - 1) / bs;
+  if (nblocks > (long)per_sm * num_sms) nblocks = (long)per_sm * num_sms;
+  if (nblocks > fit_blocks) nblocks = fit_blocks;
+  const long nthreads = nblocks * bs;
+  int* counter = sched;
+  int* first = sched + 1;
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+  k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
+                                                       first);
+  CUDA_TRY(cudaGetLastError());
+  LambertInputs in2 = in;
+  in2.nadir_first = first;
+  k_scalar_lambert<NS><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, arena, nthreads, nsolve, counter, rad, refl, nf,
+                                                        st);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
 }  // namespace aerort_internal
 
 #define AERORT_INSTANTIATE_RT(NS)                                                                            \
   template int aerort_internal::launch_scalar_lambert<NS>(aerort_internal::Context&, const aerort::RtOptions&, \
                                                           const aerort::LambertInputs&, double*, double*, int*, \
-                                                          int*, cudaStream_t);
+                                                          int*, cudaStream_t);                          \
+  template int aerort_internal::launch_scalar_lambert_fixed<NS>(                                               \
+      const aerort::RtOptions&, const aerort::LambertInputs&, double*, size_t, int*, int, double*, double*, int*, \
+      int*, cudaStream_t);

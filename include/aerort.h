@@ -135,6 +135,31 @@ int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstre
                                             double* radiance_VL, double* reflectance_VL, int* nfourier, int* status,
                                             void* stream);
 
+/* Allocation-free form of aerort_vlidort_scalar_lambert_batch_dev (same
+ * arguments, same results).  No counterpart in the reference: it exists for
+ * callers that must not have the library allocate or free device memory
+ * during a run (a model whose pool allocator owns the device memory, a loop
+ * with other streams in flight that cudaFree would synchronise).  It calls no
+ * cudaMalloc/cudaFree: its scratch is a static 256 MiB device arena (plus two
+ * ints) reserved when the library's CUDA module for it is loaded.  The first
+ * call on a device, made with that device current, does the set-up (symbol
+ * lookup, which may load that module); make it before any stream capture.
+ * Limits: the kernel's resident threads are capped so their scratch fits the
+ * arena (throughput drops at 12-16 streams); nobs * nch must stay below 2^31
+ * - 256; a configuration whose 64-thread block would not fit is rejected with
+ * AERORT_RC_ARG.  Nothing needs zeroing beforehand: the work counter is reset
+ * on the stream by each call and every output element is written.  Calls
+ * share the arena: two calls that may overlap (different streams, or threads
+ * on the same device) race; order them on one stream or with events. */
+int aerort_vlidort_scalar_lambert_batch_dev_noalloc(int km, int nch, int nobs, int nstreams, int plane_parallel,
+                                                    int nMom, const int* nlay, const double* ROT, const double* depol,
+                                                    const double* tau, const double* ssa, const double* pmom,
+                                                    const float* tau_f, const float* ssa_f, const float* pmom_f,
+                                                    const double* he, const double* albedo,
+                                                    const double* solar_zenith, const double* relat_azymuth,
+                                                    const double* sensor_zenith, double MISSING, double* radiance_VL,
+                                                    double* reflectance_VL, int* nfourier, int* status, void* stream);
+
 /* Host-pointer form of the batched call (same extension as above, FP64
  * optics, nlay(nobs) host array or NULL).  No counterpart routine in the
  * reference: it replaces a loop of VLIDORT_Scalar_Lambert calls over columns
