@@ -43,6 +43,12 @@ _SIGNATURES = {
                                                         [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
     "aerort_vlidort_scalar_lambert_batch": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, P_i] + [P_d] * 10 +
                                             [c_double, P_d, P_d, P_i, P_i]),
+    "aerort_vlidort_scalar_lambert_mixed_batch_dev": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int] +
+                                                      [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
+    "aerort_vlidort_scalar_lambert_mixed_batch": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, P_i] + [P_d] * 10 +
+                                                  [c_double, P_d, P_d, P_i, P_i]),
+    "aerort_set_schedule": (c_int, [c_int, c_int, c_int, c_int]),
+    "aerort_get_schedule": (c_int, [c_int, c_int, P_i, P_i]),
     "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_last_error": (ctypes.c_char_p, []),
     "aerort_version": (c_int, []),
@@ -50,6 +56,10 @@ _SIGNATURES = {
     "aerort_miegen_lognormal": (c_int, [c_int, P_d, c_int, P_d, c_int, P_d, P_d, c_double, c_double, c_int, c_double,
                                         c_int, c_int, P_f, P_f, P_f, P_f]),
 }
+
+
+PREC_FP64 = 0
+PREC_MIXED = 1
 
 
 def library_path():

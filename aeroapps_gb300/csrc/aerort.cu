@@ -73,6 +73,17 @@ Context& ctx() {
   return c;
 }
 
+int stream_index(int nstreams) {
+  switch (nstreams) {
+    case 4: return 0;
+    case 6: return 1;
+    case 8: return 2;
+    case 12: return 3;
+    case 16: return 4;
+  }
+  return -1;
+}
+
 void gauss_legendre01(int n, double* x, double* w) {
   for (int i = 0; i < n; ++i) {
     double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), dp = 0.0;
@@ -417,16 +428,24 @@ RtOptions lambert_options(int plane_parallel) {
   return o;
 }
 
-int dispatch_lambert(Context& c, int nstreams, const RtOptions& opt, const LambertInputs& in, double* rad,
-                     double* refl, int* nf, int* st, cudaStream_t s) {
+template <typename T>
+int dispatch_lambert_t(Context& c, int nstreams, const RtOptions& opt, const LambertInputs& in, double* rad,
+                       double* refl, int* nf, int* st, cudaStream_t s) {
   switch (nstreams) {
-    case 4: return launch_scalar_lambert<4>(c, opt, in, rad, refl, nf, st, s);
-    case 6: return launch_scalar_lambert<6>(c, opt, in, rad, refl, nf, st, s);
-    case 8: return launch_scalar_lambert<8>(c, opt, in, rad, refl, nf, st, s);
-    case 12: return launch_scalar_lambert<12>(c, opt, in, rad, refl, nf, st, s);
-    case 16: return launch_scalar_lambert<16>(c, opt, in, rad, refl, nf, st, s);
+    case 4: return launch_scalar_lambert<4, T>(c, opt, in, rad, refl, nf, st, s);
+    case 6: return launch_scalar_lambert<6, T>(c, opt, in, rad, refl, nf, st, s);
+    case 8: return launch_scalar_lambert<8, T>(c, opt, in, rad, refl, nf, st, s);
+    case 12: return launch_scalar_lambert<12, T>(c, opt, in, rad, refl, nf, st, s);
+    case 16: return launch_scalar_lambert<16, T>(c, opt, in, rad, refl, nf, st, s);
   }
   return set_error(AERORT_RC_UNSUPPORTED, "nstreams must be one of 4, 6, 8, 12, 16");
+}
+
+int dispatch_lambert(Context& c, int precision, int nstreams, const RtOptions& opt, const LambertInputs& in,
+                     double* rad, double* refl, int* nf, int* st, cudaStream_t s) {
+  if (precision == AERORT_PREC_MIXED) return dispatch_lambert_t<float>(c, nstreams, opt, in, rad, refl, nf, st, s);
+  if (precision == AERORT_PREC_FP64) return dispatch_lambert_t<double>(c, nstreams, opt, in, rad, refl, nf, st, s);
+  return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
 }
 
 int lambert_checks(int km, int nch, int nobs, int nstreams, int nMom) {
@@ -452,6 +471,26 @@ extern "C" int aerort_vlidort_scalar_lambert_dev(int km, int nch, int nobs, int 
                                                  nfourier, status, stream);
 }
 
+namespace {
+int lambert_batch_dev(int precision, int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                      const int* nlay, const double* ROT, const double* depol, const double* tau, const double* ssa,
+                      const double* pmom, const float* tau_f, const float* ssa_f, const float* pmom_f,
+                      const double* he, const double* albedo, const double* solar_zenith, const double* relat_azymuth,
+                      const double* sensor_zenith, double MISSING, double* radiance_VL, double* reflectance_VL,
+                      int* nfourier, int* status, void* stream) {
+  if (int rc = lambert_checks(km, nch, nobs, nstreams, nMom)) return rc;
+  if ((!tau_f && (!tau || !ssa || !pmom)) || (tau_f && (!ssa_f || !pmom_f)))
+    return set_error(AERORT_RC_ARG, "scalar_lambert_batch_dev: optics missing");
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lk(c.mu);
+  if (int rc = c.setup()) return rc;
+  LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
+                   sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
+  return dispatch_lambert(c, precision, nstreams, lambert_options(plane_parallel), in, radiance_VL, reflectance_VL,
+                          nfourier, status, (cudaStream_t)stream);
+}
+}  // namespace
+
 extern "C" int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel,
                                                        int nMom, const int* nlay, const double* ROT,
                                                        const double* depol, const double* tau, const double* ssa,
@@ -461,16 +500,46 @@ extern "C" int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs
                                                        const double* sensor_zenith, double MISSING,
                                                        double* radiance_VL, double* reflectance_VL, int* nfourier,
                                                        int* status, void* stream) {
-  if (int rc = lambert_checks(km, nch, nobs, nstreams, nMom)) return rc;
-  if ((!tau_f && (!tau || !ssa || !pmom)) || (tau_f && (!ssa_f || !pmom_f)))
-    return set_error(AERORT_RC_ARG, "scalar_lambert_batch_dev: optics missing");
+  return lambert_batch_dev(AERORT_PREC_FP64, km, nch, nobs, nstreams, plane_parallel, nMom, nlay, ROT, depol, tau,
+                           ssa, pmom, tau_f, ssa_f, pmom_f, he, albedo, solar_zenith, relat_azymuth, sensor_zenith,
+                           MISSING, radiance_VL, reflectance_VL, nfourier, status, stream);
+}
+
+extern "C" int aerort_vlidort_scalar_lambert_mixed_batch_dev(
+    int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom, const int* nlay, const double* ROT,
+    const double* depol, const double* tau, const double* ssa, const double* pmom, const float* tau_f,
+    const float* ssa_f, const float* pmom_f, const double* he, const double* albedo, const double* solar_zenith,
+    const double* relat_azymuth, const double* sensor_zenith, double MISSING, double* radiance_VL,
+    double* reflectance_VL, int* nfourier, int* status, void* stream) {
+  return lambert_batch_dev(AERORT_PREC_MIXED, km, nch, nobs, nstreams, plane_parallel, nMom, nlay, ROT, depol, tau,
+                           ssa, pmom, tau_f, ssa_f, pmom_f, he, albedo, solar_zenith, relat_azymuth, sensor_zenith,
+                           MISSING, radiance_VL, reflectance_VL, nfourier, status, stream);
+}
+
+extern "C" int aerort_set_schedule(int nstreams, int precision, int threads_per_block, int blocks_per_sm) {
+  const int si = stream_index(nstreams);
+  if (si < 0) return set_error(AERORT_RC_UNSUPPORTED, "set_schedule: nstreams must be one of 4, 6, 8, 12, 16");
+  if (precision != AERORT_PREC_FP64 && precision != AERORT_PREC_MIXED)
+    return set_error(AERORT_RC_ARG, "set_schedule: bad precision");
+  if (threads_per_block < 32 || threads_per_block > 128 || threads_per_block % 32 != 0 || blocks_per_sm < 0)
+    return set_error(AERORT_RC_ARG, "set_schedule: threads_per_block must be 32, 64, 96 or 128, blocks_per_sm >= 0");
   Context& c = ctx();
   std::lock_guard<std::mutex> lk(c.mu);
-  if (int rc = c.setup()) return rc;
-  LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
-                   sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
-  return dispatch_lambert(c, nstreams, lambert_options(plane_parallel), in, radiance_VL, reflectance_VL, nfourier,
-                          status, (cudaStream_t)stream);
+  c.sched[precision][si].threads = threads_per_block;
+  c.sched[precision][si].blocks_per_sm = blocks_per_sm;
+  return AERORT_OK;
+}
+
+extern "C" int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int* blocks_per_sm) {
+  const int si = stream_index(nstreams);
+  if (si < 0 || (precision != AERORT_PREC_FP64 && precision != AERORT_PREC_MIXED) || !threads_per_block ||
+      !blocks_per_sm)
+    return set_error(AERORT_RC_ARG, "get_schedule: bad argument");
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lk(c.mu);
+  *threads_per_block = c.sched[precision][si].threads;
+  *blocks_per_sm = c.sched[precision][si].blocks_per_sm;
+  return AERORT_OK;
 }
 
 extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
@@ -541,7 +610,8 @@ extern "C" int aerort_vlidort_scalar_lambert_ex(int km, int nch, int nobs, const
   int* dst = dnf + nx;
   LambertInputs in{km, nch, nobs, nMom, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9],
                    nullptr, nullptr, nullptr, nullptr, nullptr, MISSING};
-  if (int rc = dispatch_lambert(c, nstreams, lambert_options(plane_parallel), in, drad, drefl, dnf, dst, s)) return rc;
+  if (int rc = dispatch_lambert(c, AERORT_PREC_FP64, nstreams, lambert_options(plane_parallel), in, drad, drefl, dnf, dst, s))
+    return rc;
   CUDA_TRY(cudaMemcpyAsync(radiance_VL, drad, 8 * nx, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaMemcpyAsync(reflectance_VL, drefl, 8 * nx, cudaMemcpyDeviceToHost, s));
   if (nfourier) CUDA_TRY(cudaMemcpyAsync(nfourier, dnf, 4 * nx, cudaMemcpyDeviceToHost, s));
@@ -550,13 +620,12 @@ extern "C" int aerort_vlidort_scalar_lambert_ex(int km, int nch, int nobs, const
   return AERORT_OK;
 }
 
-extern "C" int aerort_vlidort_scalar_lambert_batch(int km, int nch, int nobs, int nstreams, int plane_parallel,
-                                                   int nMom, const int* nlay, const double* ROT, const double* depol,
-                                                   const double* tau, const double* ssa, const double* pmom,
-                                                   const double* he, const double* albedo, const double* solar_zenith,
-                                                   const double* relat_azymuth, const double* sensor_zenith,
-                                                   double MISSING, double* radiance_VL, double* reflectance_VL,
-                                                   int* nfourier, int* status) {
+namespace {
+int lambert_batch_host(int precision, int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                       const int* nlay, const double* ROT, const double* depol, const double* tau, const double* ssa,
+                       const double* pmom, const double* he, const double* albedo, const double* solar_zenith,
+                       const double* relat_azymuth, const double* sensor_zenith, double MISSING, double* radiance_VL,
+                       double* reflectance_VL, int* nfourier, int* status) {
   if (int rc = lambert_checks(km, nch, nobs, nstreams, nMom)) return rc;
   if (!ROT || !depol || !tau || !ssa || !pmom || !he || !albedo || !solar_zenith || !relat_azymuth ||
       !sensor_zenith || !radiance_VL || !reflectance_VL)
@@ -587,7 +656,8 @@ extern "C" int aerort_vlidort_scalar_lambert_batch(int km, int nch, int nobs, in
                    (const double*)d[3], (const double*)d[4], (const double*)d[5], (const double*)d[6],
                    (const double*)d[7], (const double*)d[8], (const double*)d[9], (const int*)d[10], nullptr, nullptr,
                    nullptr, nullptr, MISSING};
-  if (int rc = dispatch_lambert(c, nstreams, lambert_options(plane_parallel), in, drad, drefl, dnf, dst, s)) return rc;
+  if (int rc = dispatch_lambert(c, precision, nstreams, lambert_options(plane_parallel), in, drad, drefl, dnf, dst, s))
+    return rc;
   CUDA_TRY(cudaMemcpyAsync(radiance_VL, drad, 8 * nx, cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaMemcpyAsync(reflectance_VL, drefl, 8 * nx, cudaMemcpyDeviceToHost, s));
   if (nfourier) CUDA_TRY(cudaMemcpyAsync(nfourier, dnf, 4 * nx, cudaMemcpyDeviceToHost, s));
@@ -595,6 +665,33 @@ extern "C" int aerort_vlidort_scalar_lambert_batch(int km, int nch, int nobs, in
   CUDA_TRY(cudaStreamSynchronize(s));
   return AERORT_OK;
 }
+}  // namespace
+
+extern "C" int aerort_vlidort_scalar_lambert_batch(int km, int nch, int nobs, int nstreams, int plane_parallel,
+                                                   int nMom, const int* nlay, const double* ROT, const double* depol,
+                                                   const double* tau, const double* ssa, const double* pmom,
+                                                   const double* he, const double* albedo, const double* solar_zenith,
+                                                   const double* relat_azymuth, const double* sensor_zenith,
+                                                   double MISSING, double* radiance_VL, double* reflectance_VL,
+                                                   int* nfourier, int* status) {
+  return lambert_batch_host(AERORT_PREC_FP64, km, nch, nobs, nstreams, plane_parallel, nMom, nlay, ROT, depol, tau,
+                            ssa, pmom, he, albedo, solar_zenith, relat_azymuth, sensor_zenith, MISSING, radiance_VL,
+                            reflectance_VL, nfourier, status);
+}
+
+extern "C" int aerort_vlidort_scalar_lambert_mixed_batch(int km, int nch, int nobs, int nstreams, int plane_parallel,
+                                                         int nMom, const int* nlay, const double* ROT,
+                                                         const double* depol, const double* tau, const double* ssa,
+                                                         const double* pmom, const double* he, const double* albedo,
+                                                         const double* solar_zenith, const double* relat_azymuth,
+                                                         const double* sensor_zenith, double MISSING,
+                                                         double* radiance_VL, double* reflectance_VL, int* nfourier,
+                                                         int* status) {
+  return lambert_batch_host(AERORT_PREC_MIXED, km, nch, nobs, nstreams, plane_parallel, nMom, nlay, ROT, depol, tau,
+                            ssa, pmom, he, albedo, solar_zenith, relat_azymuth, sensor_zenith, MISSING, radiance_VL,
+                            reflectance_VL, nfourier, status);
+}
+
 
 extern "C" int aerort_vlidort_scalar_lambert(int km, int nch, int nobs, const double* channels, int nstreams,
                                              int plane_parallel, int nMom, int nPol, const double* ROT,

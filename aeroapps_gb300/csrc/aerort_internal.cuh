@@ -29,6 +29,15 @@ struct DevBuf {
   void release();
 };
 
+// Launch schedule of the RT kernel for one (precision, stream count):
+// threads per block (a multiple of 32, <= 128) and resident blocks per SM
+// (0 = as many as the occupancy calculator allows).
+struct Schedule {
+  int threads = 64;
+  int blocks_per_sm = 0;
+};
+int stream_index(int nstreams);  // 0..4 for 4, 6, 8, 12, 16; -1 otherwise
+
 // Library context: stream, scratch, staging buffers.  One per process; calls
 // are serialised by the mutex (the reference library is serial per process).
 struct Context {
@@ -37,6 +46,7 @@ struct Context {
   int device = -1, num_sms = 0;
   cudaStream_t stream = nullptr;
   DevBuf scratch, counter, stage[24];
+  Schedule sched[2][5];  // [precision][stream index]
   int setup();
   void release();
 };
@@ -50,7 +60,7 @@ struct Quad {
   double qx[16], qw[16], tu[aerort::kMaxFine], wu[aerort::kMaxFine];
 };
 
-template <int NS>
+template <int NS, typename T>
 int launch_scalar_lambert(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
                           double* refl, int* nf, int* st, cudaStream_t s);
 

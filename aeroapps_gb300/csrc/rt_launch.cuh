@@ -14,12 +14,12 @@ __global__ void k_nadir_first(int nobs, int nch, const double* sza, const double
 // counter <- 0, first <- nobs (device-side, so launches need no host staging)
 __global__ void k_init_sched(int* counter, int* first, int nobs);
 
-template <int NS>
-__global__ void __launch_bounds__(64) k_scalar_lambert(RtOptions opt, LambertInputs in, Quad q, double* scratch,
+template <int NS, typename T>
+__global__ void __launch_bounds__(128) k_scalar_lambert(RtOptions opt, LambertInputs in, Quad q, void* scratch,
                                                         long nthreads, int nsolve, int* counter, double* rad,
                                                         double* refl, int* nf, int* st) {
   const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const Scratch S{scratch + tid, nthreads};
+  const SolveScratch<T> S = make_scratch<NS, T>(scratch, tid, nthreads, in.km);
   const int lane = threadIdx.x & 31;
   for (;;) {
     int base = 0;
@@ -27,12 +27,12 @@ __global__ void __launch_bounds__(64) k_scalar_lambert(RtOptions opt, LambertInp
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= nsolve) break;
     const int s = base + lane;
-    if (s < nsolve) solve_lambert<NS>(opt, in, s, q.qx, q.qw, q.tu, q.wu, S, rad, refl, nf, st);
+    if (s < nsolve) solve_lambert<NS, T>(opt, in, s, q.qx, q.qw, q.tu, q.wu, S, rad, refl, nf, st);
     __syncwarp();
   }
 }
 
-template <int NS>
+template <int NS, typename T>
 int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
                           int* nf, int* st, cudaStream_t s) {
   const int nsolve = in.nobs * in.nch;
@@ -41,15 +41,17 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   std::memset(&q, 0, sizeof(q));
   gauss_legendre01(NS, q.qx, q.qw);
   if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
-  int bs = 64, per_sm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS>, bs, 0));
+  const Schedule& sc = c.sched[sizeof(T) == sizeof(float) ? 1 : 0][stream_index(NS)];
+  int bs = sc.threads, per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS, T>, bs, 0));
   if (per_sm < 1) per_sm = 1;
+  if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
   long maxblocks = (long)per_sm * c.num_sms;
   long nblocks = (nsolve + bs - 1) / bs;
   if (nblocks > maxblocks) nblocks = maxblocks;
   const long nthreads = nblocks * bs;
   const ScratchLayout<NS> lay(in.km);
-  if (int rc = c.scratch.ensure(sizeof(double) * (size_t)lay.total * nthreads)) return rc;
+  if (int rc = c.scratch.ensure((size_t)lay.template bytes<T>() * nthreads)) return rc;
   if (int rc = c.counter.ensure(2 * sizeof(int))) return rc;
   int* counter = (int*)c.counter.p;
   int* first = counter + 1;
@@ -59,8 +61,8 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
-  k_scalar_lambert<NS><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, (double*)c.scratch.p, nthreads, nsolve, counter,
-                                                        rad, refl, nf, st);
+  k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, c.scratch.p, nthreads, nsolve, counter,
+                                                           rad, refl, nf, st);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -78,7 +80,7 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, d
   if (nsolve == 0) return 0;
   const int bs = 64;
   const ScratchLayout<NS> lay(in.km);
-  const long fit_blocks = (long)(arena_doubles / ((size_t)lay.total * bs));
+  const long fit_blocks = (long)(arena_doubles * sizeof(double) / ((size_t)lay.template bytes<double>() * bs));
   if (fit_blocks < 1)
     return set_error(AERORT_RC_ARG, "scalar_lambert_noalloc: one 64-thread block needs more scratch than the "
                                     "static arena holds");
@@ -87,7 +89,7 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, d
   gauss_legendre01(NS, q.qx, q.qw);
   if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
   int per_sm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS>, bs, 0));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS, double>, bs, 0));
   if (per_sm < 1) per_sm = 1;
   long nblocks = (nsolve + bs - 1) / bs;
   if (nblocks > (long)per_sm * num_sms) nblocks = (long)per_sm * num_sms;
@@ -101,18 +103,21 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, d
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
-  k_scalar_lambert<NS><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, arena, nthreads, nsolve, counter, rad, refl, nf,
-                                                        st);
+  k_scalar_lambert<NS, double><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, arena, nthreads, nsolve, counter, rad,
+                                                                refl, nf, st);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
 }  // namespace aerort_internal
 
-#define AERORT_INSTANTIATE_RT(NS)                                                                            \
-  template int aerort_internal::launch_scalar_lambert<NS>(aerort_internal::Context&, const aerort::RtOptions&, \
-                                                          const aerort::LambertInputs&, double*, double*, int*, \
-                                                          int*, cudaStream_t);                          \
+#define AERORT_INSTANTIATE_RT(NS)                                                                             \
+  template int aerort_internal::launch_scalar_lambert<NS, double>(                                             \
+      aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
+      int*, cudaStream_t);                                                                                      \
+  template int aerort_internal::launch_scalar_lambert<NS, float>(                                              \
+      aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
+      int*, cudaStream_t);                                                                                      \
   template int aerort_internal::launch_scalar_lambert_fixed<NS>(                                               \
       const aerort::RtOptions&, const aerort::LambertInputs&, double*, size_t, int*, int, double*, double*, int*, \
       int*, cudaStream_t);

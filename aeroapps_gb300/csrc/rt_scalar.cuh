@@ -36,7 +36,7 @@
 #define RT_HD inline
 #define RT_HDN
 using std::sqrt; using std::exp; using std::fabs; using std::asin; using std::sin; using std::cos;
-using std::atan; using std::acos; using std::copysign;
+using std::atan; using std::acos; using std::copysign; using std::expm1;
 #endif
 
 namespace aerort {
@@ -75,34 +75,39 @@ struct RtOptions {
   int max_fourier;         // -1: up to NMOMENTS (reference); otherwise cap (testing)
 };
 
-// Strided per-thread view of the global scratch buffer.
-struct Scratch {
-  double* base;
+// Strided per-thread view of a global scratch buffer (element e of this
+// thread at base[e * stride]; stride = number of threads sharing the buffer).
+template <typename T>
+struct ScratchT {
+  T* base;
   long stride;
-  RT_HD double& operator[](long e) const { return base[e * stride]; }
+  RT_HD T& operator[](long e) const { return base[e * stride]; }
 };
+using Scratch = ScratchT<double>;
 
 // ---------------------------------------------------------------------------------- Taylor
 // Series for (exp(-a d) - exp(-b d))/(b - a) near a == b (vlidort_Taylor.f90:101-219).
-RT_HD double taylor1(int order, double eps, double delta, double udel, double sm) {
-  double d = 1.0, mult = 0.0, power = 1.0;
+template <typename T>
+RT_HD T taylor1(int order, T eps, T delta, T udel, T sm) {
+  T d = 1.0, mult = 0.0, power = 1.0;
   for (int m = 1; m <= order + 1; ++m) {
-    d = delta * d / (double)m;
+    d = delta * d / (T)m;
     if (m == 1) mult = d;
     else { power *= eps; mult += power * d; }
   }
   return mult * udel * sm;
 }
 
-RT_HD double taylor2(int order, double eps, double y, double delta, double fac1, double fac2, double sm) {
-  double d[10];
+template <typename T>
+RT_HD T taylor2(int order, T eps, T y, T delta, T fac1, T fac2, T sm) {
+  T d[10];
   int mterms = order + 1;
-  const bool small = fabs(y) < kTaylorSmall;
+  const bool small = fabs(y) < (T)kTaylorSmall;
   if (small) mterms += 1;
   d[0] = 1.0;
-  for (int m = 1; m <= mterms; ++m) d[m] = delta * d[m - 1] / (double)m;
+  for (int m = 1; m <= mterms; ++m) d[m] = delta * d[m - 1] / (T)m;
   if (small) {
-    double power = 1.0, power2 = 1.0, mult = d[2];
+    T power = 1.0, power2 = 1.0, mult = d[2];
     for (int m = 3; m <= mterms; ++m) {
       power = power * (eps - y);
       power2 = power - y * power2;
@@ -110,14 +115,14 @@ RT_HD double taylor2(int order, double eps, double y, double delta, double fac1,
     }
     return mult * fac1 * sm;
   }
-  double y1 = 1.0 / y, ac[10];
+  T y1 = (T)1.0 / y, ac[10];
   ac[0] = 1.0;
   for (int m = 1; m <= mterms; ++m) ac[m] = y1 * ac[m - 1];
-  double mult = 0.0, power = 1.0;
+  T mult = 0.0, power = 1.0;
   for (int m = 1; m <= mterms; ++m) {
-    double cc = 0.0;
+    T cc = 0.0;
     for (int j = 0; j <= m; ++j) cc += ac[j] * d[m - j];
-    double term = fac1 * ac[m] - fac2 * cc;
+    T term = fac1 * ac[m] - fac2 * cc;
     if (m == 1) mult = term;
     else { power *= eps; mult += power * term; }
   }
@@ -127,17 +132,17 @@ RT_HD double taylor2(int order, double eps, double y, double delta, double fac1,
 // ---------------------------------------------------------------------------------- dense kernels
 // Cholesky A = L L^T of an n x n SPD matrix (column-major, lower triangle
 // overwritten with L).  Returns false if a pivot is not positive.
-template <int NS>
-RT_HD bool cholesky(int n, double* A) {
+template <int NS, typename T>
+RT_HD bool cholesky(int n, T* A) {
   for (int j = 0; j < n; ++j) {
-    double s = A[j + NS * j];
+    T s = A[j + NS * j];
     for (int k = 0; k < j; ++k) s -= A[j + NS * k] * A[j + NS * k];
-    if (!(s > 0.0)) return false;
-    double ljj = sqrt(s);
+    if (!(s > (T)0)) return false;
+    T ljj = sqrt(s);
     A[j + NS * j] = ljj;
-    double inv = 1.0 / ljj;
+    T inv = (T)1.0 / ljj;
     for (int i = j + 1; i < n; ++i) {
-      double t = A[i + NS * j];
+      T t = A[i + NS * j];
       for (int k = 0; k < j; ++k) t -= A[i + NS * k] * A[j + NS * k];
       A[i + NS * j] = t * inv;
     }
@@ -150,32 +155,36 @@ RT_HD bool cholesky(int n, double* A) {
 // tridiagonal form with the transformations accumulated in V, then implicit
 // QR sweeps with Wilkinson shifts applied as Givens rotations.  H is
 // destroyed.  Returns false if the iteration budget is exhausted.
-template <int NS>
-RT_HD bool sym_eigen(int n, double* H, double* V, double* lam) {
+template <typename T> struct Eps;
+template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
+template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; };
+
+template <int NS, typename T>
+RT_HD bool sym_eigen(int n, T* H, T* V, T* lam) {
   for (int j = 0; j < n; ++j)
     for (int i = 0; i < n; ++i) V[i + NS * j] = (i == j) ? 1.0 : 0.0;
-  double v[NS], p[NS];
+  T v[NS], p[NS];
   for (int k = 0; k + 2 < n; ++k) {
     // Householder vector for column k below the subdiagonal
-    double alpha2 = 0.0;
+    T alpha2 = 0.0;
     for (int i = k + 1; i < n; ++i) alpha2 += H[i + NS * k] * H[i + NS * k];
     if (alpha2 == 0.0) continue;
-    double x0 = H[(k + 1) + NS * k];
-    double alpha = -copysign(sqrt(alpha2), x0);
+    T x0 = H[(k + 1) + NS * k];
+    T alpha = -copysign(sqrt(alpha2), x0);
     for (int i = k + 1; i < n; ++i) v[i] = H[i + NS * k];
     v[k + 1] = x0 - alpha;
-    double vtv = alpha2 - x0 * x0 + v[k + 1] * v[k + 1];
+    T vtv = alpha2 - x0 * x0 + v[k + 1] * v[k + 1];
     if (vtv == 0.0) continue;
-    double beta = 2.0 / vtv;
+    T beta = (T)2 / vtv;
     // p = beta * H22 v ; w = p - (beta/2)(p.v) v ; H22 -= v w^T + w v^T
-    double pv = 0.0;
+    T pv = 0.0;
     for (int i = k + 1; i < n; ++i) {
-      double s = 0.0;
+      T s = 0.0;
       for (int j = k + 1; j < n; ++j) s += H[i + NS * j] * v[j];
       p[i] = beta * s;
       pv += p[i] * v[i];
     }
-    double half = 0.5 * beta * pv;
+    T half = (T)0.5 * beta * pv;
     for (int i = k + 1; i < n; ++i) p[i] -= half * v[i];
     for (int j = k + 1; j < n; ++j)
       for (int i = k + 1; i < n; ++i) H[i + NS * j] -= v[i] * p[j] + p[i] * v[j];
@@ -184,16 +193,16 @@ RT_HD bool sym_eigen(int n, double* H, double* V, double* lam) {
     for (int i = k + 2; i < n; ++i) { H[i + NS * k] = 0.0; H[k + NS * i] = 0.0; }
     // V <- V (I - beta v v^T)
     for (int i = 0; i < n; ++i) {
-      double s = 0.0;
+      T s = 0.0;
       for (int j = k + 1; j < n; ++j) s += V[i + NS * j] * v[j];
       s *= beta;
       for (int j = k + 1; j < n; ++j) V[i + NS * j] -= s * v[j];
     }
   }
-  double d[NS], e[NS];  // e[i] couples i and i+1
+  T d[NS], e[NS];  // e[i] couples i and i+1
   for (int i = 0; i < n; ++i) d[i] = H[i + NS * i];
   for (int i = 0; i + 1 < n; ++i) e[i] = H[(i + 1) + NS * i];
-  const double eps = 2.220446049250313e-16;
+  const T eps = Eps<T>::v;
   int q = n - 1, sweeps = 0;
   while (q > 0) {
     // deflate negligible couplings at the bottom of the active block
@@ -203,20 +212,20 @@ RT_HD bool sym_eigen(int n, double* H, double* V, double* lam) {
     if (p0 > 0) e[p0 - 1] = 0.0;
     if (++sweeps > 40 * n) return false;
     // Wilkinson shift from the trailing 2x2 block
-    double dd = 0.5 * (d[q - 1] - d[q]);
-    double eq = e[q - 1];
-    double den = dd + copysign(sqrt(dd * dd + eq * eq), dd);
-    double mu = d[q] - (den != 0.0 ? eq * eq / den : 0.0);
-    double x = d[p0] - mu, z = e[p0];
-    double bulge = 0.0;
+    T dd = (T)0.5 * (d[q - 1] - d[q]);
+    T eq = e[q - 1];
+    T den = dd + copysign(sqrt(dd * dd + eq * eq), dd);
+    T mu = d[q] - (den != (T)0 ? eq * eq / den : (T)0);
+    T x = d[p0] - mu, z = e[p0];
+    T bulge = 0.0;
     for (int k = p0; k < q; ++k) {
-      double r = sqrt(x * x + z * z);
-      double c = (r == 0.0) ? 1.0 : x / r, s = (r == 0.0) ? 0.0 : z / r;
+      T r = sqrt(x * x + z * z);
+      T c = (r == (T)0) ? (T)1 : x / r, s = (r == (T)0) ? (T)0 : z / r;
       // rotate rows/columns k, k+1 of the tridiagonal (with bulge below it)
       if (k > p0) e[k - 1] = r;
-      double dk = d[k], dk1 = d[k + 1], ek = e[k];
-      d[k] = c * c * dk + 2.0 * c * s * ek + s * s * dk1;
-      d[k + 1] = s * s * dk - 2.0 * c * s * ek + c * c * dk1;
+      T dk = d[k], dk1 = d[k + 1], ek = e[k];
+      d[k] = c * c * dk + (T)2 * c * s * ek + s * s * dk1;
+      d[k + 1] = s * s * dk - (T)2 * c * s * ek + c * c * dk1;
       e[k] = c * s * (dk1 - dk) + (c * c - s * s) * ek;
       if (k + 1 < q) {
         bulge = s * e[k + 1];
@@ -225,7 +234,7 @@ RT_HD bool sym_eigen(int n, double* H, double* V, double* lam) {
         z = bulge;
       }
       for (int i = 0; i < n; ++i) {
-        double a = V[i + NS * k], b = V[i + NS * (k + 1)];
+        T a = V[i + NS * k], b = V[i + NS * (k + 1)];
         V[i + NS * k] = c * a + s * b;
         V[i + NS * (k + 1)] = -s * a + c * b;
       }
@@ -235,25 +244,87 @@ RT_HD bool sym_eigen(int n, double* H, double* V, double* lam) {
   return true;
 }
 
+// A <- Q A Q for the reflector Q = I - beta v v^T (A symmetric, full storage,
+// column-major with leading dimension NS).
+template <int NS, typename T>
+RT_HD void apply_reflector_sym(int n, T* A, const T* v, T beta) {
+  // p = beta A v ; w = p - (beta/2)(p.v) v ; A -= v w^T + w v^T
+  T p[NS], pv = 0;
+  for (int i = 0; i < n; ++i) {
+    T s = 0;
+    for (int j = 0; j < n; ++j) s += A[i + NS * j] * v[j];
+    p[i] = beta * s;
+    pv += p[i] * v[i];
+  }
+  const T half = (T)0.5 * beta * pv;
+  for (int i = 0; i < n; ++i) p[i] -= half * v[i];
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) A[i + NS * j] -= v[i] * p[j] + p[i] * v[j];
+}
+
+// One-sided (Hestenes) Jacobi: orthogonalise the columns of the n x n matrix
+// G (column-major, leading dimension NS) by plane rotations accumulated in V,
+// until every pair of columns is orthogonal to working precision.  On return
+// sigma[a] = |G e_a| (the singular values, with the relative accuracy of a
+// column-graded G) and the columns of V are the right singular vectors, i.e.
+// the eigenvectors of G^T G.  Returns false if the sweep budget is exhausted.
+template <int NS, typename T>
+RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) V[i + NS * j] = (i == j) ? (T)1 : (T)0;
+  const T tol = Eps<T>::v * (T)n;
+  bool done = false;
+  for (int sweep = 0; sweep < 30 && !done; ++sweep) {
+    done = true;
+    for (int p = 0; p + 1 < n; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        T al = 0, be = 0, ga = 0;
+        for (int i = 0; i < n; ++i) {
+          const T gp = G[i + NS * p], gq = G[i + NS * q];
+          al += gp * gp; be += gq * gq; ga += gp * gq;
+        }
+        if (!(fabs(ga) > tol * sqrt(al * be))) continue;
+        done = false;
+        const T zeta = (be - al) / ((T)2 * ga);
+        const T t = copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+        const T cs = (T)1 / sqrt((T)1 + t * t), sn = cs * t;
+        for (int i = 0; i < n; ++i) {
+          const T gp = G[i + NS * p], gq = G[i + NS * q];
+          G[i + NS * p] = cs * gp - sn * gq;
+          G[i + NS * q] = sn * gp + cs * gq;
+          const T vp = V[i + NS * p], vq = V[i + NS * q];
+          V[i + NS * p] = cs * vp - sn * vq;
+          V[i + NS * q] = sn * vp + cs * vq;
+        }
+      }
+  }
+  for (int a = 0; a < n; ++a) {
+    T s = 0;
+    for (int i = 0; i < n; ++i) s += G[i + NS * a] * G[i + NS * a];
+    sigma[a] = sqrt(s);
+  }
+  return done;
+}
+
 // In-place LU with partial pivoting of an n x n matrix (leading dimension LD)
 // and solution of nrhs right-hand sides B (n x nrhs, leading dimension LD).
-template <int LD>
-RT_HD bool lu_solve(int n, double* A, double* B, int nrhs) {
+template <int LD, typename T>
+RT_HD bool lu_solve(int n, T* A, T* B, int nrhs) {
   for (int k = 0; k < n; ++k) {
     int piv = k;
-    double amax = fabs(A[k + LD * k]);
+    T amax = fabs(A[k + LD * k]);
     for (int i = k + 1; i < n; ++i) {
-      double a = fabs(A[i + LD * k]);
+      T a = fabs(A[i + LD * k]);
       if (a > amax) { amax = a; piv = i; }
     }
-    if (amax == 0.0) return false;
+    if (amax == (T)0) return false;
     if (piv != k) {
-      for (int j = 0; j < n; ++j) { double t = A[k + LD * j]; A[k + LD * j] = A[piv + LD * j]; A[piv + LD * j] = t; }
-      for (int j = 0; j < nrhs; ++j) { double t = B[k + LD * j]; B[k + LD * j] = B[piv + LD * j]; B[piv + LD * j] = t; }
+      for (int j = 0; j < n; ++j) { T t = A[k + LD * j]; A[k + LD * j] = A[piv + LD * j]; A[piv + LD * j] = t; }
+      for (int j = 0; j < nrhs; ++j) { T t = B[k + LD * j]; B[k + LD * j] = B[piv + LD * j]; B[piv + LD * j] = t; }
     }
-    double inv = 1.0 / A[k + LD * k];
+    T inv = (T)1.0 / A[k + LD * k];
     for (int i = k + 1; i < n; ++i) {
-      double f = A[i + LD * k] * inv;
+      T f = A[i + LD * k] * inv;
       A[i + LD * k] = f;
       for (int j = k + 1; j < n; ++j) A[i + LD * j] -= f * A[k + LD * j];
       for (int j = 0; j < nrhs; ++j) B[i + LD * j] -= f * B[k + LD * j];
@@ -261,7 +332,7 @@ RT_HD bool lu_solve(int n, double* A, double* B, int nrhs) {
   }
   for (int j = 0; j < nrhs; ++j)
     for (int i = n - 1; i >= 0; --i) {
-      double s = B[i + LD * j];
+      T s = B[i + LD * j];
       for (int k = i + 1; k < n; ++k) s -= A[i + LD * k] * B[k + LD * j];
       B[i + LD * j] = s / A[i + LD * i];
     }

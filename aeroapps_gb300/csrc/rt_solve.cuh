@@ -1,6 +1,14 @@
 // One scalar solve (column x wavelength) in the AeroApps VLIDORT_Scalar_Lambert
 // configuration, executed by a single thread.  See rt_scalar.cuh for the
 // mapping rationale.  Reference routines are cited per block.
+//
+// Precision: the per-column set-up (layer mixing, delta-M, beam attenuation,
+// first-order single scatter) is FP64.  The Fourier series -- the O(N^3 L) part
+// -- runs in the working precision T: double for the plain method, float for
+// the mixed method.  Where a reference formula loses accuracy in FP32 (the
+// exp(-a d) - exp(-b d) differences of thin layers), the float instantiation
+// uses an algebraically equal form built on expm1; the double instantiation
+// keeps the reference's formulas.
 #pragma once
 #include "rt_scalar.cuh"
 
@@ -33,90 +41,173 @@ struct LambertInputs {
   double missing;
 };
 
-// Scratch element counts per thread for a solve with at most L layers.
+// Scratch element counts per thread for a solve with at most L layers: an
+// FP64 region (set-up, geometry, single scatter) and a region in the working
+// precision of the Fourier series.
 template <int NS>
 struct ScratchLayout {
   static constexpr int NMX = 2 * NS;  // NMOMENTS + 1 <= 2 NS
-  long og, lnz, dtau, avsec, itrans, tmubar, tuser, emult, ext, escat, hgt, F, f, C, c, a, b, s, total;
+  long hgt, ext, escat, dts, dtau, avsec, itrans, d_total;                              // FP64
+  long og, om1, lnz, tdtau, tavsec, titrans, tmubar, tuser, emult, F, f, C, c, a, b, s, t_total;  // working precision
   RT_HD explicit ScratchLayout(int L) {
     long o = 0;
+    hgt = o; o += L + 1; ext = o; o += L; escat = o; o += L; dts = o; o += L;
+    dtau = o; o += L; avsec = o; o += L; itrans = o; o += L;
+    d_total = o;
+    o = 0;
     og = o; o += (long)NMX * L;
+    om1 = o; o += L;
     lnz = o; o += L;
-    dtau = o; o += L; avsec = o; o += L; itrans = o; o += L; tmubar = o; o += L;
-    tuser = o; o += L; emult = o; o += L; ext = o; o += L; escat = o; o += L; hgt = o; o += L + 1;
+    tdtau = o; o += L; tavsec = o; o += L; titrans = o; o += L; tmubar = o; o += L;
+    tuser = o; o += L; emult = o; o += L;
     F = o; o += (long)NS * NS * L; f = o; o += (long)NS * L;
     C = o; o += (long)NS * NS * L; c = o; o += (long)NS * L;
     a = o; o += (long)NS * L; b = o; o += (long)NS * L; s = o; o += L;
-    total = o;
+    t_total = o;
   }
+  // bytes of scratch one thread needs with working precision T
+  template <typename T>
+  RT_HD long bytes() const { return d_total * (long)sizeof(double) + t_total * (long)sizeof(T); }
 };
 
-// Per-solve constants kept in registers / local memory.
-template <int NS>
+// The two scratch regions of one thread.  In a buffer shared by nthreads
+// threads, the FP64 region comes first (d_total x nthreads doubles, element
+// major), then the working-precision region (t_total x nthreads elements).
+template <typename T>
+struct SolveScratch {
+  Scratch D;
+  ScratchT<T> W;
+};
+
+template <int NS, typename T>
+RT_HD SolveScratch<T> make_scratch(void* buffer, long tid, long nthreads, int km) {
+  const ScratchLayout<NS> lay(km);
+  double* d = (double*)buffer;
+  T* w = (T*)(d + lay.d_total * nthreads);
+  return SolveScratch<T>{Scratch{d + tid, nthreads}, ScratchT<T>{w + tid, nthreads}};
+}
+
+// Per-solve constants of the Fourier series, in its working precision.
+template <int NS, typename T>
 struct SolveCtx {
   int L, NM, cutoff;
   bool msmode, refl_directbeam;
-  double qx[NS], qw[NS], sqw[NS];
-  double mu_u, sec_u, cos_sza, albedo, trans_solar_beam;
-  double pimm_q[NS], pimm_u, pimm_0;  // P_m^m recursion state carried across Fourier terms
+  T qx[NS], qw[NS], sqw[NS];
+  T mu_u, sec_u, cos_sza, albedo, trans_solar_beam;
+  T pimm_q[NS], pimm_u, pimm_0;  // normalised P_m^m carried across Fourier terms
 };
 
 // Homogeneous + particular solution of one layer for one Fourier term.
-template <int NS>
+template <int NS, typename T>
 struct LayerSol {
-  double P[NS * NS];  // eigenvector components, downwelling streams (X+ rows 1..N)
-  double Q[NS * NS];  // eigenvector components, upwelling streams   (X+ rows N+1..2N)
-  double t[NS];       // exp(-k dtau)
-  double wt[2 * NS];  // particular solution at layer top    (down 0..N-1, up N..2N-1)
-  double wb[2 * NS];  // particular solution at layer bottom
+  T P[NS * NS];  // eigenvector components, downwelling streams (X+ rows 1..N)
+  T Q[NS * NS];  // eigenvector components, upwelling streams   (X+ rows N+1..2N)
+  T t[NS];       // exp(-k dtau)
+  T wt[2 * NS];  // particular solution at layer top    (down 0..N-1, up N..2N-1)
+  T wb[2 * NS];  // particular solution at layer bottom
+};
+
+// Recurrence coefficients of the normalised associated Legendre functions
+// P~_l^m = sqrt((l-m)!/(l+m)!) P_l^m for one Fourier term m:
+// P~_l^m = ra[l] x P~_{l-1}^m - rb[l] P~_{l-2}^m  (l >= m+2).
+template <int NS, typename T>
+struct LegendreCoef {
+  T ra[2 * NS], rb[2 * NS], r1;
+  RT_HD void init(int m, int NM) {
+    r1 = sqrt((T)(2 * m + 1));
+    for (int l = m + 2; l <= NM; ++l) {
+      T d = (T)1 / sqrt((T)(l * l - m * m));
+      ra[l] = (T)(2 * l - 1) * d;
+      rb[l] = sqrt((T)((l - 1) * (l - 1) - m * m)) * d;
+    }
+  }
 };
 
 // Associated Legendre functions normalised as the reference's PI matrices
-// (vlidort_miscsetups.f90:2273-2932, NSTOKES = 1) for Fourier term m at
-// cosine x; out[l] for l = m..NM, zero below m.  pim carries P_m^m between
-// successive Fourier terms.
-RT_HD void legendre_m(int m, int NM, double x, double* pim, double* out) {
-  for (int l = 0; l < m && l <= NM; ++l) out[l] = 0.0;
+// (vlidort_miscsetups.f90:2273-2932, NSTOKES = 1: sqrt((l-m)!/(l+m)!) P_l^m,
+// no Condon-Shortley phase) for Fourier term m at cosine x; out[l] for
+// l = m..NM, zero below m.  The normalised recursion never forms the
+// factorials, so it is safe in FP32.  pim carries P~_m^m from term m-1 to m:
+// the calls for one x must come in the order m = 0, 1, 2, ...
+template <int NS, typename T>
+RT_HD void legendre_m(int m, int NM, const LegendreCoef<NS, T>& lc, T x, T* pim, T* out) {
+  for (int l = 0; l < m && l <= NM; ++l) out[l] = 0;
   if (m > NM) return;
-  double umxsq = 1.0 - x * x;
-  double rt = (x == 1.0) ? 0.0 : sqrt(umxsq);
-  double pm1 = 0.0, p = 0.0;
-  if (m == 0) {
-    pm1 = 1.0; out[0] = 1.0;
-    if (NM >= 1) { p = x; out[1] = x; }
-    if (NM >= 2) { pm1 = x; p = 0.5 * (3.0 * x * x - 1.0); out[2] = p; }
-    for (int l = 2; l <= NM - 1; ++l) {
-      double pn = (x * (double)(2 * l + 1) * p - (double)l * pm1) * (1.0 / (double)(l + 1));
-      pm1 = p; p = pn; out[l + 1] = pn;
-    }
-  } else if (m == 1) {
-    p = rt; out[1] = rt;
-    if (NM >= 2) { pm1 = rt; p = 3.0 * (rt * x); out[2] = p; }
-    for (int l = 2; l <= NM - 1; ++l) {
-      double pn = (x * (double)(2 * l + 1) * p - (double)(l + 1) * pm1) * (1.0 / (double)l);
-      pm1 = p; p = pn; out[l + 1] = pn;
-    }
-  } else {
-    if (m == 2) *pim = 3.0 * umxsq;
-    else *pim = (double)(2 * m - 1) * rt * (*pim);
-    p = *pim; out[m] = p;
-    if (m < NM) { pm1 = p; p = x * (double)(2 * m + 1) * p; out[m + 1] = p; }
-    for (int l = m + 1; l <= NM - 1; ++l) {
-      double pn = (x * (double)(2 * l + 1) * p - (double)(l + m) * pm1) * (1.0 / (double)(l + 1 - m));
-      pm1 = p; p = pn; out[l + 1] = pn;
-    }
-  }
-  // normalisation sqrt((l-m)!/(l+m)!)
-  double fac = 1.0;
-  for (int l = 1; l <= 2 * m; ++l) fac *= (double)l;
-  double phi = 1.0 / fac;
-  out[m] *= sqrt(phi);
-  for (int l = m + 1; l <= NM; ++l) {
-    phi = phi * ((double)(l - m) / (double)(l + m));
-    out[l] *= sqrt(phi);
-  }
+  const T s = (x == (T)1) ? (T)0 : sqrt((T)1 - x * x);
+  T pmm = (m == 0) ? (T)1 : *pim * s * sqrt((T)(2 * m - 1) / (T)(2 * m));
+  *pim = pmm;
+  out[m] = pmm;
+  if (m + 1 <= NM) out[m + 1] = x * lc.r1 * pmm;
+  for (int l = m + 2; l <= NM; ++l) out[l] = lc.ra[l] * x * out[l - 1] - lc.rb[l] * out[l - 2];
 }
 
+// ---------------------------------------------------------------- FP32 exponential multipliers
+// The layer multipliers of the Green's-function method are divided
+// differences of f(x) = exp(-x d) over the layer optical thickness d:
+//   first  (e^{-a d} - e^{-b d}) / (b - a)           = -f[a, b]
+//   second the user-angle particular sources sd, su  =  f[0, a, b]
+// The reference evaluates them from the exponentials directly, switching to
+// a Taylor series within 1e-4 of a resonance (vlidort_Taylor.f90); in FP32 the
+// direct forms cancel (thin layers, nearly equal nodes), so the float
+// instantiation evaluates the divided differences themselves:
+//   f[a, b]    = -d e^{-min d} E1(|b - a| d),           E1(z) = (1 - e^{-z}) / z
+//   f[0, a, b] = d^2 e^{-m0 d} H(u, v)  with the nodes shifted by their
+//                minimum m0 to {0, u, v} (in units of d),
+//   H(u, v)    = (E1(u) - E1(v)) / (v - u)
+//              = J1(w) + (v-u)^2/24 J3(w) + (v-u)^4/1920 J5(w) + ...,  w = (u+v)/2,
+//   J_n(w)     = int_0^1 s^n e^{-w s} ds.
+// All are exact rewritings; only the evaluation order changes.
+RT_HD float em1n(float z) {  // expm1(-z)
+#ifdef __CUDA_ARCH__
+  return expm1f(-z);
+#else
+  return std::expm1(-z);
+#endif
+}
+RT_HD float e1_fn(float z) {  // (1 - e^{-z}) / z, z >= 0
+  return (z < 1.0e-4f) ? 1.0f - 0.5f * z * (1.0f - z * (1.0f / 3.0f)) : -em1n(z) / z;
+}
+// J1, J3, J5 at w >= 0
+RT_HD void jn135(float w, float* j1, float* j3, float* j5) {
+  if (w < 2.0f) {
+    // J_n(w) = sum_k (-w)^k / (k! (n + k + 1))
+    float t = 1.0f, a1 = 0.0f, a3 = 0.0f, a5 = 0.0f;
+    for (int k = 0; k < 18; ++k) {
+      a1 += t / (float)(k + 2);
+      a3 += t / (float)(k + 4);
+      a5 += t / (float)(k + 6);
+      t *= -w / (float)(k + 1);
+    }
+    *j1 = a1; *j3 = a3; *j5 = a5;
+  } else {
+    // J_n = (n J_{n-1} - e^{-w}) / w, J_0 = E1(w)
+    const float e = expf(-w), iw = 1.0f / w;
+    float j = e1_fn(w);
+    j = (1.0f * j - e) * iw; *j1 = j;
+    j = (2.0f * j - e) * iw;
+    j = (3.0f * j - e) * iw; *j3 = j;
+    j = (4.0f * j - e) * iw;
+    j = (5.0f * j - e) * iw; *j5 = j;
+  }
+}
+RT_HD float h_fn(float u, float v) {  // (E1(u) - E1(v)) / (v - u), u, v >= 0
+  const float dl = v - u, w = 0.5f * (u + v);
+  if (fabsf(dl) > 0.1f * (1.0f + w)) return (e1_fn(u) - e1_fn(v)) / dl;
+  float j1, j3, j5;
+  jn135(w, &j1, &j3, &j5);
+  const float d2 = dl * dl;
+  return j1 + d2 * (1.0f / 24.0f) * (j3 + d2 * (1.0f / 80.0f) * j5);
+}
+// (e^{-a d} - e^{-b d}) / (b - a), a, b >= 0
+RT_HD float dd1_neg(float a, float b, float d) {
+  const float lo = fminf(a, b);
+  return d * expf(-lo * d) * e1_fn(fabsf(b - a) * d);
+}
+// f[0, a, b] for f(x) = e^{-x d}, a, b >= 0
+RT_HD float dd2(float a, float b, float d) {
+  // nodes {0, a, b}: minimum is 0
+  return d * d * h_fn(a * d, b * d);
+}
 // Layer eigen-solution (vlidort_solutions.f90:150-1047, VLIDORT_QHOM_SOLUTION).
 // The reference forms EIGENMAT = DAB*SAB and solves the nonsymmetric problem
 // with ASYMTX.  Here the same eigenpairs are found from a symmetric problem:
@@ -126,88 +217,213 @@ RT_HD void legendre_m(int m, int NM, double x, double* pim, double* out) {
 // H = R^T As R is symmetric with the same eigenvalues k^2, and an eigenvector
 // q of H maps to x = W^-1/2 R q.  Bs (odd-parity part) is well conditioned
 // even for conservative scattering, so its Cholesky factor is always safe.
-template <int NS>
-RT_HD int layer_eigen(const SolveCtx<NS>& c, int m, double dtau, const double* og, const double* piq,
-                      LayerSol<NS>& ls, double* kv, double* Sp) {
+//
+// Besides the eigenpairs (kv, X+ = (P; Q), transmittances t) it returns, per
+// eigenvector a, the Green's-function norm sum_j mu_j w_j (P_ja^2 - Q_ja^2)
+// and the user-angle homogeneous solutions (vlidort_solutions.f90:1167-1505),
+// both formed from the sum and difference vectors x = P + Q, dif = P - Q: that
+// is the same algebra without the cancellation of P^2 - Q^2 when P ~ Q (the
+// nearly conservative mode).
+template <int NS, typename T>
+RT_HD int layer_eigen(const SolveCtx<NS, T>& c, int m, T dtau, T om1, const T* og, const T* piq, const T* piu,
+                      LayerSol<NS, T>& ls, T* kv, T* Sp, T* norm, T* uh_dn, T* uh_up) {
   const int N = NS, NM = c.NM;
-  double Bs[NS * NS], H[NS * NS], V[NS * NS], lam[NS];
+  T Bs[NS * NS], H[NS * NS], V[NS * NS];
+  [[maybe_unused]] T lam[NS];
   // Sp (even l-m) and Sm (odd l-m) contractions of omega*beta_l P_l(mu_i) P_l(mu_j)
   for (int j = 0; j < N; ++j)
     for (int i = 0; i <= j; ++i) {
-      double se = 0.0, so = 0.0;
+      T se = 0, so = 0;
       for (int l = m; l <= NM; ++l) {
-        double t = og[l] * piq[l + 2 * NS * i] * piq[l + 2 * NS * j];
+        T t = og[l] * piq[l + 2 * NS * i] * piq[l + 2 * NS * j];
         if (((l - m) & 1) == 0) se += t; else so += t;
       }
       Sp[i + NS * j] = se; Sp[j + NS * i] = se;
-      double b = -c.sqw[i] * c.sqw[j] * so;
-      if (i == j) b += 1.0;
+      T b = -c.sqw[i] * c.sqw[j] * so;
+      if (i == j) b += (T)1;
       Bs[i + NS * j] = b; Bs[j + NS * i] = b;
     }
   if (!cholesky<NS>(N, Bs)) return RT_EIGEN_FAIL;
   // R = M^-1 Lb (lower triangular)
   for (int j = 0; j < N; ++j)
     for (int i = j; i < N; ++i) Bs[i + NS * j] /= c.qx[i];
-  // Y = As R with As = I - W^1/2 Sp W^1/2 ; H = R^T Y
-  for (int j = 0; j < N; ++j)
-    for (int i = 0; i < N; ++i) {
-      double y = Bs[i + NS * j] * ((i >= j) ? 1.0 : 0.0);
-      double s = 0.0;
-      for (int k = j; k < N; ++k) s += c.sqw[i] * Sp[i + NS * k] * c.sqw[k] * Bs[k + NS * j];
-      V[i + NS * j] = y - s;  // V used as temporary for Y
+  T kq[NS];  // k of each eigenvector column of V
+  [[maybe_unused]] T G[NS * NS];  // FP32 path: La u_a per eigenvector
+  if constexpr (sizeof(T) == sizeof(float)) {
+    // FP32: H = G^T G with G = La^T R (As = La La^T).  One-sided Jacobi
+    // (Hestenes) orthogonalises the columns of G by plane rotations V, so that
+    // the singular values k = |G V e_a| come with relative accuracy even
+    // though the k span four decades; the eigenvectors of H are the columns of V.
+    T rv[NS], rbeta = 0;
+    if (m == 0) {
+      // Fourier term 0: As has the exact eigenvector s = W^1/2 1 with
+      // eigenvalue 1 - omega (the half-range Gauss rule integrates every even
+      // moment l >= 2 to zero).  The reflector Q (Q s = -e_1 |s|) splits it
+      // off exactly; 1 - omega comes from FP64, so nearly conservative layers
+      // keep their small eigenvalue, and only the well-conditioned complement
+      // B = (Q As Q)[1:, 1:] is factorised in FP32.  La = Q diag(sqrt(1-omega), Lb_B).
+      T v[NS], vv = 0;
+      {
+        T ns = 0;
+        for (int i = 0; i < N; ++i) { v[i] = c.sqw[i]; ns += v[i] * v[i]; }
+        ns = sqrt(ns);
+        v[0] += ns;  // s has positive entries
+        for (int i = 0; i < N; ++i) vv += v[i] * v[i];
+      }
+      const T beta = (T)2 / vv;
+      rbeta = beta;
+      for (int i = 0; i < N; ++i) rv[i] = v[i];
+      // As (full) in H, then C = Q As Q
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          T a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
+          if (i == j) a += (T)1;
+          H[i + NS * j] = a;
+        }
+      apply_reflector_sym<NS>(N, H, v, beta);
+      H[0] = om1;
+      for (int i = 1; i < N; ++i) { H[i] = 0; H[NS * i] = 0; }
+      if (!(om1 > (T)0) || !cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
+      // G = La^T R = diag-block(L~)^T (Q R)
+      T QR[NS * NS];
+      for (int j = 0; j < N; ++j) {
+        T d = 0;
+        for (int k = j; k < N; ++k) d += v[k] * Bs[k + NS * j];
+        d *= beta;
+        for (int i = 0; i < N; ++i) QR[i + NS * j] = ((i >= j) ? Bs[i + NS * j] : (T)0) - d * v[i];
+      }
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          T s = 0;
+          for (int k = i; k < N; ++k) s += H[k + NS * i] * QR[k + NS * j];
+          G[i + NS * j] = s;
+        }
+    } else {
+      for (int j = 0; j < N; ++j)
+        for (int i = j; i < N; ++i) {
+          T a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
+          if (i == j) a += (T)1;
+          H[i + NS * j] = a;
+        }
+      if (!cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          T s = 0;
+          for (int k = (i > j ? i : j); k < N; ++k) s += H[k + NS * i] * Bs[k + NS * j];
+          G[i + NS * j] = s;
+        }
     }
-  for (int j = 0; j < N; ++j)
-    for (int i = 0; i <= j; ++i) {
-      double s = 0.0;
-      for (int k = i; k < N; ++k) s += Bs[k + NS * i] * V[k + NS * j];
-      H[i + NS * j] = s; H[j + NS * i] = s;
+    if (!jacobi_svd<NS>(N, G, V, kq)) return RT_EIGEN_FAIL;
+    // G now holds G V = U diag(k).  As v_a = La La^T R q_a = La (G V)e_a, so
+    // SAB x / k needs La u_a only (u_a = unit left singular vector): no
+    // cancellation for the small-k modes.  Overwrite G[:, a] with La u_a.
+    for (int a = 0; a < N; ++a) {
+      if (!(kq[a] > (T)0)) return RT_EIGEN_FAIL;
+      const T inv = (T)1 / kq[a];
+      T u[NS], y[NS];
+      for (int i = 0; i < N; ++i) u[i] = G[i + NS * a] * inv;
+      for (int i = 0; i < N; ++i) {
+        T s = 0;
+        for (int k = 0; k <= i; ++k) s += H[i + NS * k] * u[k];
+        y[i] = s;
+      }
+      if (m == 0) {
+        T d = 0;
+        for (int i = 0; i < N; ++i) d += rv[i] * y[i];
+        d *= rbeta;
+        for (int i = 0; i < N; ++i) y[i] -= d * rv[i];
+      }
+      for (int i = 0; i < N; ++i) G[i + NS * a] = y[i];
     }
-  if (!sym_eigen<NS>(N, H, V, lam)) return RT_EIGEN_FAIL;
-  // As = La La^T: the eigenvalues are recomputed as Rayleigh quotients
-  // lam = q^T R^T As R q = |La^T (R q)|^2, which keeps full relative accuracy
-  // for the small eigenvalues of nearly conservative layers (forming H
-  // explicitly leaves them an absolute error of order eps*|H|).
-  for (int j = 0; j < N; ++j)
-    for (int i = j; i < N; ++i) {
-      double a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
-      if (i == j) a += 1.0;
-      H[i + NS * j] = a;
+  } else {
+    // Y = As R with As = I - W^1/2 Sp W^1/2 ; H = R^T Y
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        T y = (i >= j) ? Bs[i + NS * j] : (T)0;
+        T s = 0;
+        for (int k = j; k < N; ++k) s += c.sqw[i] * Sp[i + NS * k] * c.sqw[k] * Bs[k + NS * j];
+        V[i + NS * j] = y - s;  // V used as temporary for Y
+      }
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i <= j; ++i) {
+        T s = 0;
+        for (int k = i; k < N; ++k) s += Bs[k + NS * i] * V[k + NS * j];
+        H[i + NS * j] = s; H[j + NS * i] = s;
+      }
+    if (!sym_eigen<NS>(N, H, V, lam)) return RT_EIGEN_FAIL;
+    // As = La La^T: the eigenvalues are recomputed as Rayleigh quotients
+    // lam = q^T R^T As R q = |La^T (R q)|^2, which keeps full relative accuracy
+    // for the small eigenvalues of nearly conservative layers (forming H
+    // explicitly leaves them an absolute error of order eps*|H|).
+    for (int j = 0; j < N; ++j)
+      for (int i = j; i < N; ++i) {
+        T a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
+        if (i == j) a += (T)1;
+        H[i + NS * j] = a;
+      }
+    if (!cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
+    for (int a = 0; a < N; ++a) {
+      T v[NS];
+      for (int i = 0; i < N; ++i) {
+        T s = 0;
+        for (int j = 0; j <= i; ++j) s += Bs[i + NS * j] * V[j + NS * a];
+        v[i] = s;
+      }
+      T qq = 0, lr = 0;
+      for (int i = 0; i < N; ++i) {
+        qq += V[i + NS * a] * V[i + NS * a];
+        T w = 0;
+        for (int j = i; j < N; ++j) w += H[j + NS * i] * v[j];
+        lr += w * w;
+      }
+      lr /= qq;
+      if (!(lr > (T)0)) return RT_EIGEN_FAIL;
+      kq[a] = sqrt(lr);
     }
-  if (!cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
+  }
   for (int a = 0; a < N; ++a) {
     // v = R q ; sum vector x = W^-1/2 v, unit 2-norm
-    double x[NS], v[NS], nrm = 0.0;
+    T x[NS], nrm = 0;
     for (int i = 0; i < N; ++i) {
-      double s = 0.0;
+      T s = 0;
       for (int j = 0; j <= i; ++j) s += Bs[i + NS * j] * V[j + NS * a];
-      v[i] = s;
       x[i] = s / c.sqw[i];
       nrm += x[i] * x[i];
     }
-    double qq = 0.0, lr = 0.0;
-    for (int i = 0; i < N; ++i) {
-      qq += V[i + NS * a] * V[i + NS * a];
-      double w = 0.0;
-      for (int j = i; j < N; ++j) w += H[j + NS * i] * v[j];
-      lr += w * w;
-    }
-    lr /= qq;
-    if (!(lr > 0.0)) return RT_EIGEN_FAIL;
-    double k = sqrt(lr);
+    const T k = kq[a];
+    if (!(k > (T)0)) return RT_EIGEN_FAIL;
     kv[a] = k;
-    nrm = 1.0 / sqrt(nrm);
+    nrm = (T)1 / sqrt(nrm);
     for (int i = 0; i < N; ++i) x[i] *= nrm;
     // difference vector SAB x / k ; SAB(i,j) = (delta_ij - w_j Sp(i,j)) / mu_i
-    double invk = 1.0 / k;
+    T invk = (T)1 / k, dif[NS], nr = 0;
     for (int i = 0; i < N; ++i) {
-      double s = 0.0;
-      for (int j = 0; j < N; ++j) s += c.qw[j] * Sp[i + NS * j] * x[j];
-      double dif = (x[i] - s) / c.qx[i] * invk;
-      ls.P[i + NS * a] = 0.5 * (x[i] + dif);
-      ls.Q[i + NS * a] = 0.5 * (x[i] - dif);
+      if constexpr (sizeof(T) == sizeof(float)) {
+        dif[i] = G[i + NS * a] / (c.qx[i] * c.sqw[i]) * nrm;
+      } else {
+        T s = 0;
+        for (int j = 0; j < N; ++j) s += c.qw[j] * Sp[i + NS * j] * x[j];
+        dif[i] = (x[i] - s) / c.qx[i] * invk;
+      }
+      ls.P[i + NS * a] = (T)0.5 * (x[i] + dif[i]);
+      ls.Q[i + NS * a] = (T)0.5 * (x[i] - dif[i]);
+      nr += c.qx[i] * c.qw[i] * x[i] * dif[i];
     }
-    double help = k * dtau;
-    ls.t[a] = help > kMaxTau ? 0.0 : exp(-help);
+    norm[a] = nr;
+    T help = k * dtau;
+    ls.t[a] = help > (T)kMaxTau ? (T)0 : exp(-help);
+    // user-angle homogeneous solutions: sum_j w_j P_l(mu_j) (P +- Q)_ja / 2
+    T dn = 0, up = 0;
+    for (int l = m; l <= NM; ++l) {
+      const bool even = ((l - m) & 1) == 0;
+      T sps = 0;
+      for (int j = 0; j < N; ++j) sps += c.qw[j] * piq[l + 2 * NS * j] * (even ? x[j] : dif[j]);
+      T h = (T)0.5 * og[l] * sps;
+      dn += (even ? piu[l] : -piu[l]) * h;
+      up += piu[l] * h;
+    }
+    uh_dn[a] = dn;
+    uh_up[a] = up;
   }
   return RT_OK;
 }
@@ -216,97 +432,99 @@ RT_HD int layer_eigen(const SolveCtx<NS>& c, int m, double dtau, const double* o
 // homogeneous and particular terms (vlidort_solutions.f90:1051-1163, 1167-1505,
 // 1651-1790, 2649-3073; PostProcessing.f90:139-451).  Writes the per-layer
 // source coefficients a, b, s (TOA radiance = sum_n Tcum_n (L.a + M.b + s)).
-template <int NS>
-RT_HD int layer_solution(const SolveCtx<NS>& c, const RtOptions& opt, int m, int n, bool laysc,
-                         const Scratch& S, const ScratchLayout<NS>& lay, const double* piq, const double* piu,
-                         const double* pi0, LayerSol<NS>& ls) {
-  const int N = NS, NM = c.NM, L = c.L;
-  double og[2 * NS], kv[NS], Sp[NS * NS];
-  for (int l = 0; l <= NM; ++l) og[l] = (l >= m) ? S[lay.og + l + 2 * NS * (long)n] : 0.0;
-  const double dtau = S[lay.dtau + n];
-  int st = layer_eigen<NS>(c, m, dtau, og, piq, ls, kv, Sp);
+template <int NS, typename T>
+RT_HD int layer_solution(const SolveCtx<NS, T>& c, const RtOptions& opt, int m, int n, bool laysc,
+                         const ScratchT<T>& W, const ScratchLayout<NS>& lay, const T* piq, const T* piu, const T* pi0,
+                         LayerSol<NS, T>& ls) {
+  const int N = NS, NM = c.NM;
+  T og[2 * NS], kv[NS], Sp[NS * NS];
+  for (int l = 0; l <= NM; ++l) og[l] = (l >= m) ? W[lay.og + l + 2 * NS * (long)n] : (T)0;
+  const T dtau = W[lay.tdtau + n];
+  T uh_dn[NS], uh_up[NS], hm1[NS], hm2[NS], norm[NS];
+  int st = layer_eigen<NS, T>(c, m, dtau, W[lay.om1 + n], og, piq, piu, ls, kv, Sp, norm, uh_dn, uh_up);
   if (st != RT_OK) return st;
-  const double tuser = S[lay.tuser + n];
-  const double smu = c.sec_u;
-  double uh_dn[NS], uh_up[NS], hm1[NS], hm2[NS], norm[NS];
+  const T tuser = W[lay.tuser + n];
+  const T smu = c.sec_u;
   for (int a = 0; a < N; ++a) {
-    // user-angle homogeneous solutions
-    double dn = 0.0, up = 0.0;
-    for (int l = m; l <= NM; ++l) {
-      double sgn = ((l - m) & 1) ? -1.0 : 1.0;
-      double sps = 0.0;
-      for (int j = 0; j < N; ++j) sps += 0.5 * c.qw[j] * piq[l + 2 * NS * j] * (ls.P[j + NS * a] + sgn * ls.Q[j + NS * a]);
-      double h = og[l] * sps;
-      dn += sgn * piu[l] * h;
-      up += piu[l] * h;
-    }
-    uh_dn[a] = laysc ? dn : 0.0;
-    uh_up[a] = laysc ? up : 0.0;
+    if (!laysc) { uh_dn[a] = 0; uh_up[a] = 0; }
     // homogeneous multipliers
-    double zdel = ls.t[a];
-    double rho_p = smu + kv[a], rho_m = smu - kv[a];
-    hm2[a] = smu * (1.0 - zdel * tuser) * (1.0 / rho_p);
-    if (fabs(rho_m) < kTaylorSmall) hm1[a] = taylor1(opt.taylor_order, rho_m, dtau, tuser, smu);
-    else hm1[a] = smu * (zdel - tuser) * (1.0 / rho_m);
-    double nr = 0.0;
-    for (int j = 0; j < N; ++j) nr += c.qx[j] * c.qw[j] * (ls.P[j + NS * a] * ls.P[j + NS * a] - ls.Q[j + NS * a] * ls.Q[j + NS * a]);
-    norm[a] = nr;
+    T zdel = ls.t[a];
+    T rho_p = smu + kv[a], rho_m = smu - kv[a];
+    if constexpr (sizeof(T) == sizeof(float)) {
+      hm2[a] = smu * dtau * e1_fn(rho_p * dtau);
+      hm1[a] = smu * dd1_neg(kv[a], smu, dtau);
+    } else {
+      hm2[a] = smu * (1.0 - zdel * tuser) * (1.0 / rho_p);
+      if (fabs(rho_m) < kTaylorSmall) hm1[a] = taylor1<T>(opt.taylor_order, rho_m, dtau, tuser, smu);
+      else hm1[a] = smu * (zdel - tuser) * (1.0 / rho_m);
+    }
   }
   for (int a = 0; a < N; ++a) {
-    S[lay.a + a + N * (long)n] = uh_dn[a] * hm2[a];
-    S[lay.b + a + N * (long)n] = uh_up[a] * hm1[a];
+    W[lay.a + a + N * (long)n] = uh_dn[a] * hm2[a];
+    W[lay.b + a + N * (long)n] = uh_up[a] * hm1[a];
   }
-  for (int i = 0; i < 2 * N; ++i) { ls.wt[i] = 0.0; ls.wb[i] = 0.0; }
-  double spart = 0.0;
+  for (int i = 0; i < 2 * N; ++i) { ls.wt[i] = 0; ls.wb[i] = 0; }
+  T spart = 0;
   const bool active = (n < c.cutoff) && laysc;
   if (active) {
     // Green's-function particular integral (VLIDORT_GBEAM_SOLUTION)
-    const double F1 = opt.flux_factor / kPI4;
-    const double secbar = S[lay.avsec + n], cnst = S[lay.itrans + n], wdel = S[lay.tmubar + n];
-    double hq[2 * NS], dpi[NS], dmi[NS];
+    const T F1 = (T)(opt.flux_factor / kPI4);
+    const T secbar = W[lay.tavsec + n], cnst = W[lay.titrans + n], wdel = W[lay.tmubar + n];
+    T hq[2 * NS], dpi[NS], dmi[NS];
     for (int l = m; l <= NM; ++l) hq[l] = og[l] * pi0[l];
-    double upar = 0.0;
-    for (int l = m; l <= NM; ++l) upar += (F1 * hq[l]) * ((((l - m) & 1) ? -1.0 : 1.0) * piu[l]);
+    T upar = 0;
+    for (int l = m; l <= NM; ++l) upar += (F1 * hq[l]) * ((((l - m) & 1) ? (T)-1 : (T)1) * piu[l]);
     for (int i = 0; i < N; ++i) {
-      double sp = 0.0, sm = 0.0;
+      T sp = 0, sm = 0;
       for (int l = m; l <= NM; ++l) {
-        double t = piq[l + 2 * NS * i] * hq[l];
+        T t = piq[l + 2 * NS * i] * hq[l];
         sp += t;
         sm += (((l - m) & 1) ? -t : t);
       }
       dpi[i] = F1 * sp; dmi[i] = F1 * sm;
     }
-    const double emult = S[lay.emult + n];
-    const double itw = -cnst * wdel;
-    const double sigp = secbar + smu;
-    double gup[NS], gdn[NS];
+    const T emult = W[lay.emult + n];
+    const T itw = -cnst * wdel;
+    const T sigp = secbar + smu;
+    T gup[NS], gdn[NS];
     for (int a = 0; a < N; ++a) {
-      double zdel = ls.t[a];
-      double gp = secbar + kv[a], gm = secbar - kv[a];
-      double cf = (fabs(gm) < kTaylorSmall) ? taylor1(opt.taylor_order, gm, dtau, wdel, cnst)
-                                            : cnst * (zdel - wdel) / gm;
-      double df = cnst * (1.0 - zdel * wdel) / gp;
-      double s1 = 0.0, s2 = 0.0;
+      T zdel = ls.t[a];
+      T gp = secbar + kv[a], gm = secbar - kv[a];
+      const bool tay = fabs(gm) < (T)kTaylorSmall;
+      T cf, df;
+      if constexpr (sizeof(T) == sizeof(float)) {
+        cf = cnst * dd1_neg(kv[a], secbar, dtau);
+        df = cnst * dtau * e1_fn(gp * dtau);
+      } else {
+        cf = tay ? taylor1<T>(opt.taylor_order, gm, dtau, wdel, cnst) : cnst * (zdel - wdel) / gm;
+        df = cnst * (1.0 - zdel * wdel) / gp;
+      }
+      T s1 = 0, s2 = 0;
       for (int i = 0; i < N; ++i) {
         s1 += c.qw[i] * (dpi[i] * ls.P[i + NS * a] + dmi[i] * ls.Q[i + NS * a]);
         s2 += c.qw[i] * (dmi[i] * ls.P[i + NS * a] + dpi[i] * ls.Q[i + NS * a]);
       }
-      double at = s1 / norm[a], bt = s2 / norm[a];
+      T at = s1 / norm[a], bt = s2 / norm[a];
       gdn[a] = cf * at;
       gup[a] = df * bt;
       // user-angle particular source (WHOLELAYER_STERM_UP, Green's branch)
-      double sd;
-      if (fabs(gm) < kTaylorSmall) {
-        double mult = taylor2(opt.taylor_order, gm, sigp, dtau, 1.0, wdel * tuser, 1.0);
-        sd = (cnst * smu) * mult;
+      T sd, su;
+      if constexpr (sizeof(T) == sizeof(float)) {
+        sd = cnst * smu * dd2(kv[a] + smu, sigp, dtau);
+        su = cnst * smu * dd2(gp, sigp, dtau);
       } else {
-        sd = (cnst * hm2[a] - emult) / gm;
+        if (tay) {
+          T mult = taylor2<T>(opt.taylor_order, gm, sigp, dtau, (T)1, wdel * tuser, (T)1);
+          sd = (cnst * smu) * mult;
+        } else {
+          sd = (cnst * hm2[a] - emult) / gm;
+        }
+        su = (itw * hm1[a] + emult) / gp;
       }
-      double su = (itw * hm1[a] + emult) / gp;
       spart += uh_dn[a] * sd * at + uh_up[a] * su * bt;
     }
     for (int i = 0; i < N; ++i) {
-      double wu1 = 0.0, wu2 = 0.0, wl1 = 0.0, wl2 = 0.0;
+      T wu1 = 0, wu2 = 0, wl1 = 0, wl2 = 0;
       for (int a = 0; a < N; ++a) {
         wu1 += gup[a] * ls.Q[i + NS * a]; wu2 += gup[a] * ls.P[i + NS * a];
         wl1 += gdn[a] * ls.P[i + NS * a]; wl2 += gdn[a] * ls.Q[i + NS * a];
@@ -316,7 +534,7 @@ RT_HD int layer_solution(const SolveCtx<NS>& c, const RtOptions& opt, int m, int
     }
     if (!c.msmode) spart += upar * emult;
   }
-  S[lay.s + n] = laysc ? spart : 0.0;
+  W[lay.s + n] = laysc ? spart : (T)0;
   return RT_OK;
 }
 
@@ -330,35 +548,39 @@ RT_HD int layer_solution(const SolveCtx<NS>& c, const RtOptions& opt, int m, int
 // pivoted solve; the surface condition closes the system and a bottom-up pass
 // recovers all coefficients while accumulating the TOA source recursion
 // (vlidort_intensity.f90:145-643).
-template <int NS>
-RT_HD int fourier_term(SolveCtx<NS>& c, const RtOptions& opt, int m, const Scratch& S, const ScratchLayout<NS>& lay,
-                       double* out) {
+template <int NS, typename T>
+RT_HD int fourier_term(SolveCtx<NS, T>& c, const RtOptions& opt, int m, const ScratchT<T>& W,
+                       const ScratchLayout<NS>& lay, T* out) {
   const int N = NS, NM = c.NM, L = c.L;
-  const bool incl_surface = (m == 0) && (c.albedo != 0.0);
-  const double surface_factor = (m == 0) ? 2.0 : 1.0;
-  const double delta_factor = (m == 0) ? 1.0 : 2.0;
+  const bool incl_surface = (m == 0) && (c.albedo != (T)0);
+  const T surface_factor = (m == 0) ? (T)2 : (T)1;
+  const T delta_factor = (m == 0) ? (T)1 : (T)2;
   const bool localbeam = incl_surface && c.refl_directbeam;
-  double direct_beam = 0.0;
+  T direct_beam = 0;
   if (localbeam) {
-    double x0 = 4.0 * c.cos_sza / delta_factor;
-    x0 = opt.flux_factor * x0 / kPI4;
+    T x0 = (T)4 * c.cos_sza / delta_factor;
+    x0 = (T)opt.flux_factor * x0 / (T)kPI4;
     direct_beam = x0 * c.trans_solar_beam * c.albedo;
   }
-  double piq[2 * NS * NS], piu[2 * NS], pi0[2 * NS];
-  for (int i = 0; i < N; ++i) legendre_m(m, NM, c.qx[i], &c.pimm_q[i], &piq[2 * NS * i]);
-  legendre_m(m, NM, c.mu_u, &c.pimm_u, piu);
-  legendre_m(m, NM, c.cos_sza, &c.pimm_0, pi0);
+  T piq[2 * NS * NS], piu[2 * NS], pi0[2 * NS];
+  {
+    LegendreCoef<NS, T> lc;
+    lc.init(m, NM);
+    for (int i = 0; i < N; ++i) legendre_m<NS, T>(m, NM, lc, c.qx[i], &c.pimm_q[i], &piq[2 * NS * i]);
+    legendre_m<NS, T>(m, NM, lc, c.mu_u, &c.pimm_u, piu);
+    legendre_m<NS, T>(m, NM, lc, c.cos_sza, &c.pimm_0, pi0);
+  }
 
-  LayerSol<NS> A, B;
-  LayerSol<NS>* prev = &A;
-  LayerSol<NS>* cur = &B;
-  double F[NS * NS], f[NS];
-  double K[4 * NS * NS], R[2 * NS * (NS + 1)];
+  LayerSol<NS, T> A, B;
+  LayerSol<NS, T>* prev = &A;
+  LayerSol<NS, T>* cur = &B;
+  T F[NS * NS], f[NS];
+  T K[4 * NS * NS], R[2 * NS * (NS + 1)];
   for (int n = 0; n < L; ++n) {
     // DO_LAYER_SCATTERING(m, n) (vlidort_inputs.f90:4321-4330): false for m >= 3
     // when every input moment l = m..NMOMENTS of the layer is zero
-    const bool lsc = (m < 3) || (m <= (int)S[lay.lnz + n]);
-    int st = layer_solution<NS>(c, opt, m, n, lsc, S, lay, piq, piu, pi0, *cur);
+    const bool lsc = (m < 3) || ((T)m <= W[lay.lnz + n]);
+    int st = layer_solution<NS, T>(c, opt, m, n, lsc, W, lay, piq, piu, pi0, *cur);
     if (st != RT_OK) return st;
     if (n == 0) {
       // TOA: downwelling diffuse intensity vanishes -> L_1 = F_1 M_1 + f_1
@@ -370,18 +592,18 @@ RT_HD int fourier_term(SolveCtx<NS>& c, const RtOptions& opt, int m, const Scrat
       for (int i = 0; i < N; ++i) R[i + 2 * NS * N] = -cur->wt[i];
       if (!lu_solve<2 * NS>(N, K, R, N + 1)) return RT_BVP_SINGULAR;
       for (int j = 0; j < N; ++j)
-        for (int i = 0; i < N; ++i) { F[i + NS * j] = R[i + 2 * NS * j]; S[lay.F + i + NS * j + (long)NS * NS * n] = F[i + NS * j]; }
-      for (int i = 0; i < N; ++i) { f[i] = R[i + 2 * NS * N]; S[lay.f + i + NS * (long)n] = f[i]; }
+        for (int i = 0; i < N; ++i) { F[i + NS * j] = R[i + 2 * NS * j]; W[lay.F + i + NS * j + (long)NS * NS * n] = F[i + NS * j]; }
+      for (int i = 0; i < N; ++i) { f[i] = R[i + 2 * NS * N]; W[lay.f + i + NS * (long)n] = f[i]; }
     } else {
       // interface between layer n-1 (prev) and n (cur):
       // G M_{n-1} + g + Wb_{n-1} = X+_n L_n + X-_n T_n M_n + Wt_n
-      double TF[NS * NS], tf[NS];
+      T TF[NS * NS], tf[NS];
       for (int j = 0; j < N; ++j)
         for (int k = 0; k < N; ++k) TF[k + NS * j] = prev->t[k] * F[k + NS * j];
       for (int k = 0; k < N; ++k) tf[k] = prev->t[k] * f[k];
       for (int j = 0; j < N; ++j)
         for (int i = 0; i < N; ++i) {
-          double gt = prev->Q[i + NS * j], gb = prev->P[i + NS * j];
+          T gt = prev->Q[i + NS * j], gb = prev->P[i + NS * j];
           for (int k = 0; k < N; ++k) {
             gt += prev->P[i + NS * k] * TF[k + NS * j];
             gb += prev->Q[i + NS * k] * TF[k + NS * j];
@@ -394,7 +616,7 @@ RT_HD int fourier_term(SolveCtx<NS>& c, const RtOptions& opt, int m, const Scrat
           R[N + i + 2 * NS * j] = cur->P[i + NS * j] * cur->t[j];
         }
       for (int i = 0; i < N; ++i) {
-        double gt = 0.0, gb = 0.0;
+        T gt = 0, gb = 0;
         for (int k = 0; k < N; ++k) { gt += prev->P[i + NS * k] * tf[k]; gb += prev->Q[i + NS * k] * tf[k]; }
         R[i + 2 * NS * N] = cur->wt[i] - prev->wb[i] - gt;
         R[N + i + 2 * NS * N] = cur->wt[N + i] - prev->wb[N + i] - gb;
@@ -404,25 +626,25 @@ RT_HD int fourier_term(SolveCtx<NS>& c, const RtOptions& opt, int m, const Scrat
       long oF = lay.F + (long)NS * NS * n, of = lay.f + (long)NS * n;
       for (int j = 0; j < N; ++j)
         for (int i = 0; i < N; ++i) {
-          S[oC + i + NS * j] = R[i + 2 * NS * j];
+          W[oC + i + NS * j] = R[i + 2 * NS * j];
           F[i + NS * j] = R[N + i + 2 * NS * j];
-          S[oF + i + NS * j] = F[i + NS * j];
+          W[oF + i + NS * j] = F[i + NS * j];
         }
       for (int i = 0; i < N; ++i) {
-        S[oc + i] = R[i + 2 * NS * N];
+        W[oc + i] = R[i + 2 * NS * N];
         f[i] = R[N + i + 2 * NS * N];
-        S[of + i] = f[i];
+        W[of + i] = f[i];
       }
     }
-    LayerSol<NS>* t = prev; prev = cur; cur = t;
+    LayerSol<NS, T>* t = prev; prev = cur; cur = t;
   }
   // surface: upwelling at the bottom = Lambertian reflection of the downwelling
   // diffuse field + reflected direct beam (bvproblem.f90:439-623, 1625-1739)
-  const LayerSol<NS>& bl = *prev;
-  const double kmult = incl_surface ? surface_factor * c.albedo : 0.0;
-  double r2p[NS], r2m[NS], r2b = 0.0;
+  const LayerSol<NS, T>& bl = *prev;
+  const T kmult = incl_surface ? surface_factor * c.albedo : (T)0;
+  T r2p[NS], r2m[NS], r2b = 0;
   for (int k = 0; k < N; ++k) {
-    double sp = 0.0, sm = 0.0;
+    T sp = 0, sm = 0;
     for (int j = 0; j < N; ++j) { sp += c.qx[j] * c.qw[j] * bl.P[j + NS * k]; sm += c.qx[j] * c.qw[j] * bl.Q[j + NS * k]; }
     r2p[k] = sp * kmult; r2m[k] = sm * kmult;
   }
@@ -431,30 +653,30 @@ RT_HD int fourier_term(SolveCtx<NS>& c, const RtOptions& opt, int m, const Scrat
   {
     for (int j = 0; j < N; ++j)
       for (int i = 0; i < N; ++i) {
-        double s = bl.P[i + NS * j] - r2m[j];
+        T s = bl.P[i + NS * j] - r2m[j];
         for (int k = 0; k < N; ++k) s += (bl.Q[i + NS * k] - r2p[k]) * bl.t[k] * F[k + NS * j];
         K[i + 2 * NS * j] = s;
       }
     for (int i = 0; i < N; ++i) {
-      double s = -bl.wb[N + i] + r2b + (localbeam ? direct_beam : 0.0);
+      T s = -bl.wb[N + i] + r2b + (localbeam ? direct_beam : (T)0);
       for (int k = 0; k < N; ++k) s -= (bl.Q[i + NS * k] - r2p[k]) * bl.t[k] * f[k];
       R[i] = s;
     }
     if (!lu_solve<2 * NS>(N, K, R, 1)) return RT_BVP_SINGULAR;
   }
-  double Mc[NS], Lc[NS], Mn[NS];
+  T Mc[NS], Lc[NS], Mn[NS];
   for (int i = 0; i < N; ++i) Mc[i] = R[i];
   for (int i = 0; i < N; ++i) {
-    double s = f[i];
+    T s = f[i];
     for (int k = 0; k < N; ++k) s += F[i + NS * k] * Mc[k];
     Lc[i] = s;
   }
   // bottom boundary source at the user angle (GET_BOA_SOURCE)
-  double cum = 0.0;
+  T cum = 0;
   if (incl_surface) {
-    double s = 0.0;
+    T s = 0;
     for (int i = 0; i < N; ++i) {
-      double h = bl.wb[i];
+      T h = bl.wb[i];
       for (int k = 0; k < N; ++k) h += Lc[k] * bl.P[i + NS * k] * bl.t[k] + Mc[k] * bl.Q[i + NS * k];
       s += c.qx[i] * c.qw[i] * h;
     }
@@ -467,20 +689,20 @@ RT_HD int fourier_term(SolveCtx<NS>& c, const RtOptions& opt, int m, const Scrat
       long oC = lay.C + (long)NS * NS * n, oc = lay.c + (long)NS * n;
       long oF = lay.F + (long)NS * NS * n, of = lay.f + (long)NS * n;
       for (int i = 0; i < N; ++i) {
-        double s = S[oc + i];
-        for (int k = 0; k < N; ++k) s += S[oC + i + NS * k] * Mc[k];
+        T s = W[oc + i];
+        for (int k = 0; k < N; ++k) s += W[oC + i + NS * k] * Mc[k];
         Mn[i] = s;
       }
       for (int i = 0; i < N; ++i) {
-        double s = S[of + i];
-        for (int k = 0; k < N; ++k) s += S[oF + i + NS * k] * Mn[k];
+        T s = W[of + i];
+        for (int k = 0; k < N; ++k) s += W[oF + i + NS * k] * Mn[k];
         Lc[i] = s;
       }
       for (int i = 0; i < N; ++i) Mc[i] = Mn[i];
     }
-    double src = S[lay.s + n];
-    for (int k = 0; k < N; ++k) src += Lc[k] * S[lay.a + k + N * (long)n] + Mc[k] * S[lay.b + k + N * (long)n];
-    cum = src + S[lay.tuser + n] * cum;
+    T src = W[lay.s + n];
+    for (int k = 0; k < N; ++k) src += Lc[k] * W[lay.a + k + N * (long)n] + Mc[k] * W[lay.b + k + N * (long)n];
+    cum = src + W[lay.tuser + n] * cum;
   }
   *out = delta_factor * cum;
   return RT_OK;
@@ -493,11 +715,24 @@ constexpr double kHeightScale = 0.001000000047497451305389404296875;  // 1.E-3
 constexpr double kSsaCap = 0.999989986419677734375;            // 0.99999
 constexpr double kAccuracySingle = 9.99999974737875163555145263671875e-05;  // 0.0001
 
+// ---------------------------------------------------------------------------------- geometry
+// Spherical-shell geometry without inverse trigonometry.  A straight ray with
+// impact parameter p (distance of closest approach to the Earth's centre)
+// crosses the shell between radii r_lo < r_hi on a chord of length
+//   sqrt(r_hi^2 - p^2) - sqrt(r_lo^2 - p^2) = (r_hi - r_lo)(r_hi + r_lo) / (c_hi + c_lo),
+// c = sqrt((r - p)(r + p)).  The reference evaluates the same chord by the
+// law of sines, r_lo sin(th_lo - th_hi) / sin(th_hi) with th = asin(p / r)
+// (FO_geometry_Generic.f90:169-329, vlidort_geometry.f90:119-317); the form
+// here needs one square root per level and has no cancellation between
+// nearly equal angles.
+RT_HD double shell_c(double r, double p) { return sqrt((r - p) * (r + p)); }
+
 // Sun path through layers 1..nn of a straight ray that leaves radius radstart
-// with local solar zenith th (sine sth), layers ordered from TOA (index 0 of
-// radii) down; returns sum_k ext_k * path_k.  Direct-sun and tangent-ray
-// branches follow FO_geometry_Generic.f90:169-329 (FindSunPaths_D / _T).
-RT_HD double sun_optical_path(bool zero_sun_boa, bool direct, double radstart, double th, double sth, int nn,
+// (inside layer nn) towards the sun, with local solar zenith cosine ct and
+// sine st there; layers ordered from TOA (level 0) down; returns
+// sum_k ext_k * path_k.  Direct-sun and tangent-ray branches follow
+// FO_geometry_Generic.f90:169-329 (FindSunPaths_D / _T).
+RT_HD double sun_optical_path(bool zero_sun_boa, bool direct, double radstart, double ct, double st, int nn,
                               double R0, const Scratch& S, long ohgt, long oext, int L) {
   auto radius = [&](int k) { return R0 + S[ohgt + k]; };
   double tau = 0.0;
@@ -507,19 +742,25 @@ RT_HD double sun_optical_path(bool zero_sun_boa, bool direct, double radstart, d
       for (int k = nn - 1; k >= 1; --k) tau += S[oext + k - 1] * (radius(k - 1) - radius(k));
       return tau;
     }
-    double sth0 = sth, th0 = th;
-    double sth1 = sth0 * radstart / radius(nn - 1), th1 = asin(sth1);
-    tau += S[oext + nn - 1] * (sin(th0 - th1) * radstart / sth1);
-    sth0 = sth1; th0 = th1;
+    const double p = radstart * st;
+    double r_lo = radstart, c_lo = radstart * ct;
+    {
+      const double r_hi = radius(nn - 1), c_hi = shell_c(r_hi, p);
+      tau += S[oext + nn - 1] * ((r_hi - r_lo) * (r_hi + r_lo) / (c_hi + c_lo));
+      r_lo = r_hi; c_lo = c_hi;
+    }
     for (int k = nn - 1; k >= 1; --k) {
-      sth1 = sth0 * radius(k) / radius(k - 1);
-      th1 = asin(sth1);
-      tau += S[oext + k - 1] * (sin(th0 - th1) * radius(k) / sth1);
-      sth0 = sth1; th0 = th1;
+      const double r_hi = radius(k - 1), c_hi = shell_c(r_hi, p);
+      const double dz = S[ohgt + k - 1] - S[ohgt + k];
+      tau += S[oext + k - 1] * (dz * (r_hi + r_lo) / (c_hi + c_lo));
+      r_lo = r_hi; c_lo = c_hi;
     }
     return tau;
   }
-  // tangent ray: passes its lowest point below the start level, then rises to TOA
+  // tangent ray (sun below the local horizon): passes its lowest point below
+  // the start level, then rises to TOA.  Rare at the angles AeroApps uses;
+  // kept in the reference's angle form.
+  const double th = acos(ct), sth = st;
   double tanr = sth * radstart;
   int k = nn - 1;
   bool trawl = true;
@@ -539,7 +780,7 @@ RT_HD double sun_optical_path(bool zero_sun_boa, bool direct, double radstart, d
     }
     tau += S[oext + nt - 1] * (2.0 * sin(0.5 * kPIE - th0) * radius(nt - 1));
   } else if (nt == nn) {
-    pnn = -2.0 * radstart * cos(th);
+    pnn = -2.0 * radstart * ct;
   }
   double th0 = kPIE - th, sth0 = sth;
   double sth1 = sth0 * radstart / radius(nn - 1), th1 = asin(sth1);
@@ -580,7 +821,7 @@ RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double 
         st = 0.0;
         for (int k = 1; k <= n; ++k) st += S[oext + k - 1] * ((S[ohgt + k - 1] - S[ohgt + k]) / cth);
       } else {
-        st = sun_optical_path(overhead, true, radius(n), th_R, sthb, n, R0, S, ohgt, oext, L);
+        st = sun_optical_path(overhead, true, radius(n), cth, sthb, n, R0, S, ohgt, oext, L);
       }
       double att = st < kFoCutoff ? exp(-st) : 0.0;
       double lostrans = 0.0, mult = 0.0;
@@ -599,41 +840,32 @@ RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double 
     return true;
   }
   const bool donadir = (vza == 0.0);
-  double raycon = 0.0, alphaL = 0.0, caL = 1.0;
+  double raycon = 0.0, caL = 1.0, saL = 0.0;
   if (!donadir) {
-    alphaL = vza * kDTR;
-    double sa = (vza == 90.0) ? 1.0 : sin(alphaL);
+    const double alphaL = vza * kDTR;
+    saL = (vza == 90.0) ? 1.0 : sin(alphaL);
     caL = (vza == 90.0) ? 0.0 : cos(alphaL);
-    raycon = sa * radius(L);
+    raycon = saL * radius(L);
   }
   // solar direction at BOA (the y component does not enter: the line of sight lies in the x-z plane)
   double sdir0 = 0.0, sdir2 = 0.0;
   if (!overhead) { sdir0 = -sthb * cos(phi * kDTR); sdir2 = -cth; }
-  auto findsun = [&](double rad, double cumangle, double* th, double* sth, bool* dirsun) {
-    if (donadir) { *dirsun = true; *th = th_R; *sth = sin(th_R); return; }
-    if (overhead) { *dirsun = true; *sth = sin(cumangle); *th = cumangle; return; }
-    double b = (-rad * sin(cumangle)) * sdir0 + (rad * cos(cumangle)) * sdir2;
-    double ct = -b / rad;
-    *dirsun = (ct >= 0.0);
-    *sth = sqrt(1.0 - ct * ct);
-    *th = acos(ct);
-  };
   // direct-sun attenuation at the surface (used by the direct bounce)
   {
-    double st = sun_optical_path(overhead, true, radius(L), th_R, sthb, L, R0, S, ohgt, oext, L);
+    double st = sun_optical_path(overhead, true, radius(L), cth, sthb, L, R0, S, ohgt, oext, L);
     atten_boa = st < kFoCutoff ? exp(-st) : 0.0;
   }
   // top-down accumulation of the line-of-sight source: TOA sees layer n through layers 1..n-1
+  double c_up = donadir ? 0.0 : shell_c(radius(0), raycon);
   for (int n = 1; n <= L; ++n) {
-    double r_up = radius(n - 1), r_lo = radius(n);
-    double losw, cosa_lo;
+    const double r_up = radius(n - 1), r_lo = radius(n);
+    double losw, c_lo;
     if (donadir) {
       losw = r_up - r_lo;
-      cosa_lo = 1.0;
+      c_lo = r_lo;
     } else {
-      double ca_up = cos(asin(raycon / r_up));
-      cosa_lo = (n == L) ? caL : cos(asin(raycon / r_lo));
-      losw = r_up * ca_up - r_lo * cosa_lo;
+      c_lo = (n == L) ? r_lo * caL : shell_c(r_lo, raycon);
+      losw = (S[ohgt + n - 1] - S[ohgt + n]) * (r_up + r_lo) / (c_up + c_lo);
     }
     const double kn = S[oext + n - 1];
     const double lostau = kn * losw;
@@ -642,22 +874,35 @@ RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double 
     double sum = 0.0;
     for (int j = 0; j < opt.nfine; ++j) {
       const double tf = losw * tu[j], wf = losw * wu[j];
-      double rf, af = 0.0;
+      // fine point at distance tf above the layer bottom along the line of
+      // sight: radius rf, and the angle af it subtends at the centre from the
+      // surface point (tan af = raycon / (c_lo + tf))
+      double rf, ct, st;
       if (donadir) {
         rf = r_lo + tf;
+        ct = cth; st = sthb;
       } else {
-        double tanf = raycon / (r_lo * cosa_lo + tf);
-        af = atan(tanf);
-        rf = raycon / sin(af);
+        const double X = c_lo + tf;
+        rf = sqrt(raycon * raycon + X * X);
+        const double caf = X / rf, saf = raycon / rf;
+        // cumulative angle alphaL - af
+        const double scum = saL * caf - caL * saf, ccum = caL * caf + saL * saf;
+        if (overhead) {
+          ct = ccum; st = scum;
+        } else {
+          // FindSun: cosine of the local solar zenith at the fine point
+          ct = scum * sdir0 - ccum * sdir2;
+          st = sqrt(1.0 - ct * ct);
+        }
       }
-      double thf, sthf; bool dsf;
-      findsun(rf, alphaL - af, &thf, &sthf, &dsf);
-      double sd = sun_optical_path(zero_sun_boa, dsf, rf, thf, sthf, n, R0, S, ohgt, oext, L);
+      const bool dsf = donadir || overhead || (ct >= 0.0);
+      double sd = sun_optical_path(zero_sun_boa, dsf, rf, ct, st, n, R0, S, ohgt, oext, L);
       double attf = sd < kFoCutoff ? exp(-sd) : 0.0;
       sum += attf * exp(-kn * (losw - tf)) * wf;
     }
     cum += trans_above * S[oescat + n - 1] * (sum * kn);
     trans_above *= lostrans;
+    c_up = c_lo;
   }
   *ss = flux * cum;
   *db = flux * (4.0 * cth * albedo * atten_boa) * trans_above;
@@ -668,10 +913,13 @@ RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double 
 // reference loop order (VLIDORT_LAMBERT.F90:106-165).  Writes radiance,
 // reflectance, last Fourier index and status.  qx/qw: Gauss-Legendre streams on
 // (0,1); tu/wu: unit fine-layer quadrature for the enhanced-PS line of sight.
-template <int NS>
+// T is the working precision of the Fourier series.
+template <int NS, typename T>
 RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sidx, const double* qx,
-                          const double* qw, const double* tu, const double* wu, const Scratch& S, double* radiance,
-                          double* reflectance, int* nfourier, int* status) {
+                          const double* qw, const double* tu, const double* wu, const SolveScratch<T>& SS,
+                          double* radiance, double* reflectance, int* nfourier, int* status) {
+  const Scratch& S = SS.D;
+  const ScratchT<T>& W = SS.W;
   const int nch = in.nch, j = sidx / nch, i = sidx % nch;
   const long o = (long)j + (long)in.nobs * i;
   const int L = in.nlay ? in.nlay[j] : in.km, ngreek = in.nmom;
@@ -684,16 +932,20 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
     radiance[o] = in.missing; reflectance[o] = in.missing;
     return;
   }
-  SolveCtx<NS> c;
+  SolveCtx<NS, T> c;
   c.L = L;
   c.NM = (2 * NS - 1 < ngreek) ? 2 * NS - 1 : ngreek;
   c.msmode = opt.do_focorr != 0;
-  c.albedo = alb;
-  for (int q = 0; q < NS; ++q) { c.qx[q] = qx[q]; c.qw[q] = qw[q]; c.sqw[q] = sqrt(qw[q]); c.pimm_q[q] = 0.0; }
-  c.pimm_u = 0.0; c.pimm_0 = 0.0;
-  c.mu_u = cos(kDTR * vza);
-  c.sec_u = 1.0 / c.mu_u;
-  c.cos_sza = cos(sza * kDTR);
+  c.albedo = (T)alb;
+  for (int q = 0; q < NS; ++q) {
+    c.qx[q] = (T)qx[q]; c.qw[q] = (T)qw[q]; c.sqw[q] = (T)sqrt(qw[q]); c.pimm_q[q] = 0;
+  }
+  c.pimm_u = 0; c.pimm_0 = 0;
+  const double mu_u = cos(kDTR * vza), cos_sza = cos(sza * kDTR);
+  const double sec_u = 1.0 / mu_u;
+  c.mu_u = (T)mu_u;
+  c.sec_u = (T)sec_u;
+  c.cos_sza = (T)cos_sza;
   const int NM = c.NM;
   const bool nadir_fo = in.nadir_first ? (j >= *in.nadir_first) : false;
   // scattering angle for the exact single-scatter phase function
@@ -764,15 +1016,17 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
         else if (g1 < 0.0 && g1 > -1.0e-9) g1 = -1.0e-9;
         b = 3.0 * g1;
       }
-      S[lay.og + l + 2 * NS * (long)k] = om * b;
+      W[lay.og + l + 2 * NS * (long)k] = (T)(om * b);
     }
-    S[lay.lnz + k] = (double)lnz;
+    W[lay.lnz + k] = (T)lnz;
+    W[lay.om1 + k] = (T)(1.0 - om);
     S[lay.dtau + k] = dtau;
+    W[lay.tdtau + k] = (T)dtau;
     // single-scatter inputs (vlidort_vfo_interface.f90:377-411; FO_VectorSS_RTCalcs_I.f90:340-380)
     const double dz = S[lay.hgt + k] - S[lay.hgt + k + 1];
     const double dts = opt.do_deltam ? dtau : tau_ext;
     S[lay.ext + k] = dts / dz;
-    S[lay.emult + k] = dts;  // temporary: FO regular-PS vertical optical depth
+    S[lay.dts + k] = dts;  // FO regular-PS vertical optical depth
     double tms = opt.do_deltam ? om_in / (1.0 - fdel * om_in) : om_in;
     double p0 = 1.0, p1 = cosscat, fm = beta_in(0) * p0 + (ngreek >= 1 ? beta_in(1) * p1 : 0.0);
     for (int l = 2; l <= ngreek; ++l) {
@@ -789,34 +1043,35 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
     double phi = raa;
     if (phi < 0.0) phi = -phi;
     if (phi > 360.0) phi = 360.0 - phi - 360.0;
-    fo_single_scatter(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.emult, &ss, &db);
+    fo_single_scatter(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts, &ss, &db);
   }
   // ---------------------------------------------------------------- beam attenuation
   // Chapman factors (vlidort_geometry.f90:119-317), QSPREP / PREPTRANS / EMULT
-  // (vlidort_miscsetups.f90:813-1292, 3187-3421)
+  // (vlidort_miscsetups.f90:813-1292, 3187-3421).  The solar zenith is the
+  // input angle at every level n (regular pseudo-spherical): the ray through
+  // level n has impact parameter p = sin(sza) r_n, and its slant optical depth
+  // to TOA is sum_k dtau_k (r_{k-1} + r_k) / (c_{k-1} + c_k).
   {
-    const double mu_toa = c.cos_sza;
+    const double mu_toa = cos_sza;
     const double sn_toa = sqrt(1.0 - mu_toa * mu_toa);
     const double R0 = opt.earth_radius;
     int cutoff = L;
     double tslant_prev = 0.0, s_t_0 = 1.0, s_t_1 = 0.0;
+    bool refl_directbeam = false;
+    double trans_solar_beam = 0.0;
     for (int n = 1; n <= L; ++n) {
       double ts = 0.0;
       if (opt.do_plane_parallel || sn_toa == 0.0) {
         double cf = opt.do_plane_parallel ? 1.0 / mu_toa : 1.0;
         for (int k = 1; k <= n; ++k) ts += S[lay.dtau + k - 1] * cf;
       } else {
-        const double r0 = S[lay.hgt + 0] + R0;
-        double sinth1 = sn_toa * (S[lay.hgt + n] + R0) / r0;
-        double sth1 = asin(sinth1), re_upper = r0;
-        for (int k = 1; k <= n; ++k) {
-          double delz = S[lay.hgt + k - 1] - S[lay.hgt + k];
-          double re_lower = re_upper - delz;
-          double sinth2 = re_upper * sinth1 / re_lower;
-          double sth2 = asin(sinth2);
-          double dist = re_upper * sin(sth2 - sth1) / sinth2;
-          ts += S[lay.dtau + k - 1] * (dist / delz);
-          re_upper = re_lower; sinth1 = sinth2; sth1 = sth2;
+        const double rn = S[lay.hgt + n] + R0;
+        const double p = sn_toa * rn;
+        double r_lo = rn, c_lo = rn * mu_toa;
+        for (int k = n; k >= 1; --k) {
+          const double r_hi = S[lay.hgt + k - 1] + R0, c_hi = shell_c(r_hi, p);
+          ts += S[lay.dtau + k - 1] * ((r_hi + r_lo) / (c_hi + c_lo));
+          r_lo = r_hi; c_lo = c_hi;
         }
       }
       const double dtn = S[lay.dtau + n - 1];
@@ -832,25 +1087,32 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
       S[lay.itrans + n - 1] = itr;
       tslant_prev = ts;
       if (n == L) {
-        c.trans_solar_beam = ts < kMaxTau ? exp(-ts) : 0.0;
-        c.refl_directbeam = ts < kMaxTau;
+        trans_solar_beam = ts < kMaxTau ? exp(-ts) : 0.0;
+        refl_directbeam = ts < kMaxTau;
       }
     }
     c.cutoff = cutoff;
+    c.trans_solar_beam = (T)trans_solar_beam;
+    c.refl_directbeam = refl_directbeam;
     for (int n = 0; n < L; ++n) {
       const double dtn = S[lay.dtau + n];
       double tmu = 0.0, em = 0.0;
-      double sp = dtn * c.sec_u;
+      double sp = dtn * sec_u;
       double tus = sp > kMaxTau ? 0.0 : exp(-sp);
+      const double avs = S[lay.avsec + n], itr = S[lay.itrans + n];
       if (n < cutoff) {
-        double spb = dtn * S[lay.avsec + n];
+        double spb = dtn * avs;
         tmu = spb > kMaxTau ? 0.0 : exp(-spb);
-        double su = (1.0 - tmu * tus) / (S[lay.avsec + n] + c.sec_u);
-        em = (S[lay.itrans + n] * c.sec_u) * su;
+        double su;
+        if constexpr (sizeof(T) == sizeof(float)) su = -expm1(-(avs + sec_u) * dtn) / (avs + sec_u);
+        else su = (1.0 - tmu * tus) / (avs + sec_u);
+        em = (itr * sec_u) * su;
       }
-      S[lay.tmubar + n] = tmu;
-      S[lay.tuser + n] = tus;
-      S[lay.emult + n] = em;
+      W[lay.tavsec + n] = (T)avs;
+      W[lay.titrans + n] = (T)itr;
+      W[lay.tmubar + n] = (T)tmu;
+      W[lay.tuser + n] = (T)tus;
+      W[lay.emult + n] = (T)em;
     }
   }
   // ---------------------------------------------------------------- Fourier series
@@ -859,8 +1121,9 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
   double stokes = 0.0;
   int testconv = 0, m = 0;
   for (m = 0; m <= n_fouriers; ++m) {
-    double sf = 0.0;
-    int st = fourier_term<NS>(c, opt, m, S, lay, &sf);
+    T sf_t = 0;
+    int st = fourier_term<NS, T>(c, opt, m, W, lay, &sf_t);
+    const double sf = (double)sf_t;
     if (st != RT_OK) {
       radiance[o] = in.missing; reflectance[o] = in.missing;
       if (status) status[o] = st;

@@ -63,11 +63,15 @@ def vlidort_scalar_lambert_dev(km, nch, nobs, nstreams, nMom, ROT, depol, tau, s
 
 
 def vlidort_scalar_lambert_batch(km, nch, nobs, nstreams, nMom, nlay, ROT, depol, tau, ssa, pmom, he, albedo,
-                                 solar_zenith, relat_azymuth, sensor_zenith, MISSING=MISSING, plane_parallel=False):
+                                 solar_zenith, relat_azymuth, sensor_zenith, MISSING=MISSING, plane_parallel=False,
+                                 precision="fp64"):
     """Batched host call for columns of different layer counts (nlay(nobs), each <= km).
 
     Same arrays as vlidort_scalar_lambert (pmom: the P11 moments, (km,nch,nobs,nMom));
+    precision "fp64" (plain method) or "mixed" (FP32 Fourier series);
     returns (radiance, reflectance, rc, nfourier, status)."""
+    if precision not in ("fp64", "mixed"):
+        raise ValueError("precision must be 'fp64' or 'mixed'")
     ROT, depol, tau, ssa, pmom, he, albedo, sza, raa, vza = [_f64(a) for a in (ROT, depol, tau, ssa, pmom, he, albedo,
                                                                                solar_zenith, relat_azymuth,
                                                                                sensor_zenith)]
@@ -77,7 +81,9 @@ def vlidort_scalar_lambert_batch(km, nch, nobs, nstreams, nMom, nlay, ROT, depol
     nf = np.zeros((nobs, nch), np.int32, order="F")
     st = np.zeros_like(nf)
     P = lambda a: _lib.ptr(a, _lib.P_d)
-    rc = _lib.lib().aerort_vlidort_scalar_lambert_batch(
+    fn = (_lib.lib().aerort_vlidort_scalar_lambert_batch if precision == "fp64"
+          else _lib.lib().aerort_vlidort_scalar_lambert_mixed_batch)
+    rc = fn(
         km, nch, nobs, nstreams, int(bool(plane_parallel)), nMom, _lib.ptr(nl, _lib.P_i), P(ROT), P(depol), P(tau),
         P(ssa), P(pmom), P(he), P(albedo), P(sza), P(raa), P(vza), float(MISSING), P(rad), P(refl),
         _lib.ptr(nf, _lib.P_i), _lib.ptr(st, _lib.P_i))

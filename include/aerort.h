@@ -30,6 +30,10 @@ extern "C" {
 #define AERORT_RC_ARG 1002         /* invalid argument (null pointer, non-positive size) */
 #define AERORT_RC_UNSUPPORTED 1003 /* configuration not built (e.g. nstreams not in {4,6,8,12,16}) */
 
+/* working precision of the RT solve */
+#define AERORT_PREC_FP64 0         /* plain method: FP64 throughout (parity 1e-9 with the reference)            */
+#define AERORT_PREC_MIXED 1        /* mixed method: FP64 set-up and single scatter, FP32 Fourier series (1e-4)  */
+
 /* per-pixel status written by the *_ex / *_dev RT entry points */
 #define AERORT_ST_OK 0
 #define AERORT_ST_EIGEN 1          /* layer eigenproblem failed (reference: ASYMTX error, rc 4)   */
@@ -134,6 +138,38 @@ int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstre
                                             const double* relat_azymuth, const double* sensor_zenith, double MISSING,
                                             double* radiance_VL, double* reflectance_VL, int* nfourier, int* status,
                                             void* stream);
+
+/* Mixed-precision forms of the two batched calls (same arguments).  No
+ * counterpart in the reference.  The per-column set-up (layer mixing, delta-M,
+ * Chapman factors, first-order single scatter) stays FP64; the Fourier series
+ * runs in FP32 with formulations chosen for FP32: the layer eigenproblem by
+ * one-sided Jacobi on a graded factor (k to relative accuracy), the
+ * conservative mode of Fourier term 0 split off exactly, and the
+ * Green's-function multipliers as divided differences of exp(-x tau).
+ * Radiance error against the FP64 method: <= 1e-5 on the synthetic configs,
+ * <= 1e-4 with layer SSA in [0.999, 1). */
+int aerort_vlidort_scalar_lambert_mixed_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel,
+                                                  int nMom, const int* nlay, const double* ROT, const double* depol,
+                                                  const double* tau, const double* ssa, const double* pmom,
+                                                  const float* tau_f, const float* ssa_f, const float* pmom_f,
+                                                  const double* he, const double* albedo, const double* solar_zenith,
+                                                  const double* relat_azymuth, const double* sensor_zenith,
+                                                  double MISSING, double* radiance_VL, double* reflectance_VL,
+                                                  int* nfourier, int* status, void* stream);
+int aerort_vlidort_scalar_lambert_mixed_batch(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                              const int* nlay, const double* ROT, const double* depol,
+                                              const double* tau, const double* ssa, const double* pmom,
+                                              const double* he, const double* albedo, const double* solar_zenith,
+                                              const double* relat_azymuth, const double* sensor_zenith,
+                                              double MISSING, double* radiance_VL, double* reflectance_VL,
+                                              int* nfourier, int* status);
+
+/* Launch schedule of the RT kernel per (stream count, precision): threads per
+ * block (32, 64, 96 or 128) and resident blocks per SM (0 = occupancy limit).
+ * Set by the autotuner (aeroapps_gb300/autotune.py); no counterpart in the
+ * reference. */
+int aerort_set_schedule(int nstreams, int precision, int threads_per_block, int blocks_per_sm);
+int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int* blocks_per_sm);
 
 /* Allocation-free form of aerort_vlidort_scalar_lambert_batch_dev (same
  * arguments, same results).  No counterpart in the reference: it exists for

@@ -17,29 +17,46 @@ static void gl(int n, double* x, double* w) {  // own Gauss-Legendre on (0,1) by
     x[n-1-i] = 0.5 - 0.5*z; w[n-1-i] = 1.0/((1-z*z)*pp*pp);
   }
 }
-template <int NS>
+template <int NS, typename T>
 static int run(const RtOptions& opt, const LambertInputs& in, double* rad, double* refl, int* nf, int* st) {
   double qx[NS], qw[NS], tu[4], wu[4];
   gl(NS, qx, qw);
   gl(opt.nfine > 0 ? opt.nfine : 1, tu, wu);
   ScratchLayout<NS> lay(in.km);
-  std::vector<double> scr(lay.total);
-  Scratch S{scr.data(), 1};
-  for (int s = 0; s < in.nobs * in.nch; ++s) solve_lambert<NS>(opt, in, s, qx, qw, tu, wu, S, rad, refl, nf, st);
+  std::vector<double> scr((lay.template bytes<T>() + 7) / 8);
+  const SolveScratch<T> S = make_scratch<NS, T>(scr.data(), 0, 1, in.km);
+  for (int s = 0; s < in.nobs * in.nch; ++s) solve_lambert<NS, T>(opt, in, s, qx, qw, tu, wu, S, rad, refl, nf, st);
   return 0;
 }
-extern "C" int host_scalar_lambert(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
+template <typename T>
+static int dispatch(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
     const double* tau, const double* ssa, const double* pmom, const double* he, const double* albedo, const double* sza,
     const double* raa, const double* vza, const int* nadir, double missing, int max_fourier,
     double* rad, double* refl, int* nf, int* st) {
   RtOptions opt{1, 1, 0, 1, 3, 3, kAccuracySingle, 6371.0, 1.0, max_fourier};
   LambertInputs in{km, nch, nobs, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nullptr, nullptr, nullptr, nullptr, nadir, missing};
   switch (nstreams) {
-    case 4: return run<4>(opt, in, rad, refl, nf, st);
-    case 6: return run<6>(opt, in, rad, refl, nf, st);
-    case 8: return run<8>(opt, in, rad, refl, nf, st);
-    case 12: return run<12>(opt, in, rad, refl, nf, st);
-    case 16: return run<16>(opt, in, rad, refl, nf, st);
+    case 4: return run<4, T>(opt, in, rad, refl, nf, st);
+    case 6: return run<6, T>(opt, in, rad, refl, nf, st);
+    case 8: return run<8, T>(opt, in, rad, refl, nf, st);
+    case 12: return run<12, T>(opt, in, rad, refl, nf, st);
+    case 16: return run<16, T>(opt, in, rad, refl, nf, st);
   }
   return -1;
+}
+// FP64 (plain method) solver
+extern "C" int host_scalar_lambert(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
+    const double* tau, const double* ssa, const double* pmom, const double* he, const double* albedo, const double* sza,
+    const double* raa, const double* vza, const int* nadir, double missing, int max_fourier,
+    double* rad, double* refl, int* nf, int* st) {
+  return dispatch<double>(km, nch, nobs, nstreams, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nadir,
+                          missing, max_fourier, rad, refl, nf, st);
+}
+// mixed method: FP32 Fourier series
+extern "C" int host_scalar_lambert_mixed(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
+    const double* tau, const double* ssa, const double* pmom, const double* he, const double* albedo, const double* sza,
+    const double* raa, const double* vza, const int* nadir, double missing, int max_fourier,
+    double* rad, double* refl, int* nf, int* st) {
+  return dispatch<float>(km, nch, nobs, nstreams, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nadir,
+                         missing, max_fourier, rad, refl, nf, st);
 }
