@@ -48,8 +48,14 @@ _SIGNATURES = {
     "aerort_vlidort_scalar_lambert_mixed_batch": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, P_i] + [P_d] * 10 +
                                                   [c_double, P_d, P_d, P_i, P_i]),
     "aerort_set_schedule": (c_int, [c_int, c_int, c_int, c_int]),
+    "aerort_workspace_create": (c_int, [ctypes.c_size_t, ctypes.POINTER(c_void_p)]),
+    "aerort_workspace_destroy": (c_int, [c_void_p]),
+    "aerort_workspace_bytes_per_thread": (ctypes.c_long, [c_int, c_int, c_int]),
+    "aerort_vlidort_scalar_lambert_ws_dev": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int] +
+                                             [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
     "aerort_get_schedule": (c_int, [c_int, c_int, P_i, P_i]),
     "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
+    "aerort_probe_ffma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_last_error": (ctypes.c_char_p, []),
     "aerort_version": (c_int, []),
     "aerort_release": (c_int, []),

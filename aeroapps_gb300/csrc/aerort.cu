@@ -542,6 +542,102 @@ extern "C" int aerort_get_schedule(int nstreams, int precision, int* threads_per
   return AERORT_OK;
 }
 
+namespace {
+template <typename T>
+int dispatch_fixed_t(int nstreams, const RtOptions& opt, const LambertInputs& in, void* arena, size_t bytes, int* sched,
+                     int num_sms, const Schedule& sc, double* r, double* f, int* nf, int* st, cudaStream_t s) {
+  switch (nstreams) {
+    case 4: return launch_scalar_lambert_fixed<4, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+    case 6: return launch_scalar_lambert_fixed<6, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+    case 8: return launch_scalar_lambert_fixed<8, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+    case 12: return launch_scalar_lambert_fixed<12, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+    case 16: return launch_scalar_lambert_fixed<16, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+  }
+  return set_error(AERORT_RC_UNSUPPORTED, "nstreams must be one of 4, 6, 8, 12, 16");
+}
+int dispatch_fixed(int precision, int nstreams, const RtOptions& opt, const LambertInputs& in, void* arena,
+                   size_t bytes, int* sched, int num_sms, const Schedule& sc, double* r, double* f, int* nf, int* st,
+                   cudaStream_t s) {
+  if (precision == AERORT_PREC_MIXED)
+    return dispatch_fixed_t<float>(nstreams, opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+  if (precision == AERORT_PREC_FP64)
+    return dispatch_fixed_t<double>(nstreams, opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+  return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
+}
+}  // namespace
+
+// Caller-owned RT workspace: device scratch plus the two scheduling ints of
+// one launch at a time.  Launches on different workspaces may run
+// concurrently on different streams.
+struct aerort_workspace {
+  int device = -1, num_sms = 0;
+  void* arena = nullptr;
+  size_t bytes = 0;
+  int* sched = nullptr;
+};
+
+extern "C" int aerort_workspace_create(size_t bytes, aerort_workspace** out) {
+  if (!out || bytes < 4096) return set_error(AERORT_RC_ARG, "workspace_create: bytes must be >= 4096");
+  *out = nullptr;
+  auto* ws = new aerort_workspace;
+  cudaError_t e = cudaGetDevice(&ws->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ws->num_sms, cudaDevAttrMultiProcessorCount, ws->device);
+  if (e == cudaSuccess) e = cudaMalloc(&ws->arena, bytes);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&ws->sched, 256);
+  if (e != cudaSuccess) {
+    if (ws->arena) cudaFree(ws->arena);
+    delete ws;
+    return set_error(AERORT_RC_CUDA, std::string("workspace_create: ") + cudaGetErrorString(e));
+  }
+  ws->bytes = bytes;
+  *out = ws;
+  return AERORT_OK;
+}
+
+extern "C" int aerort_workspace_destroy(aerort_workspace* ws) {
+  if (!ws) return AERORT_OK;
+  cudaFree(ws->arena);
+  cudaFree(ws->sched);
+  delete ws;
+  return AERORT_OK;
+}
+
+extern "C" long aerort_workspace_bytes_per_thread(int km, int nstreams, int precision) {
+  const bool f = (precision == AERORT_PREC_MIXED);
+  switch (nstreams) {
+    case 4: return f ? ScratchLayout<4>(km).bytes<float>() : ScratchLayout<4>(km).bytes<double>();
+    case 6: return f ? ScratchLayout<6>(km).bytes<float>() : ScratchLayout<6>(km).bytes<double>();
+    case 8: return f ? ScratchLayout<8>(km).bytes<float>() : ScratchLayout<8>(km).bytes<double>();
+    case 12: return f ? ScratchLayout<12>(km).bytes<float>() : ScratchLayout<12>(km).bytes<double>();
+    case 16: return f ? ScratchLayout<16>(km).bytes<float>() : ScratchLayout<16>(km).bytes<double>();
+  }
+  return -1;
+}
+
+extern "C" int aerort_vlidort_scalar_lambert_ws_dev(
+    aerort_workspace* ws, int precision, int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+    const int* nlay, const double* ROT, const double* depol, const double* tau, const double* ssa,
+    const double* pmom, const float* tau_f, const float* ssa_f, const float* pmom_f, const double* he,
+    const double* albedo, const double* solar_zenith, const double* relat_azymuth, const double* sensor_zenith,
+    double MISSING, double* radiance_VL, double* reflectance_VL, int* nfourier, int* status, void* stream) {
+  if (!ws) return set_error(AERORT_RC_ARG, "scalar_lambert_ws_dev: null workspace");
+  if (int rc = lambert_checks(km, nch, nobs, nstreams, nMom)) return rc;
+  if ((!tau_f && (!tau || !ssa || !pmom)) || (tau_f && (!ssa_f || !pmom_f)))
+    return set_error(AERORT_RC_ARG, "scalar_lambert_ws_dev: optics missing");
+  if ((long)nobs * nch > 0x7fffff00L) return set_error(AERORT_RC_ARG, "scalar_lambert_ws_dev: nobs * nch too large");
+  Schedule sc;
+  {
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    const int si = stream_index(nstreams);
+    if (si >= 0 && (precision == AERORT_PREC_FP64 || precision == AERORT_PREC_MIXED)) sc = c.sched[precision][si];
+  }
+  LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
+                   sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
+  return dispatch_fixed(precision, nstreams, lambert_options(plane_parallel), in, ws->arena, ws->bytes, ws->sched,
+                        ws->num_sms, sc, radiance_VL, reflectance_VL, nfourier, status, (cudaStream_t)stream);
+}
+
 extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
     int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom, const int* nlay, const double* ROT,
     const double* depol, const double* tau, const double* ssa, const double* pmom, const float* tau_f,
@@ -559,18 +655,10 @@ extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
   if (int rc = static_arena(&arena, &arena_doubles, &sched, &num_sms)) return rc;
   LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
                    sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
-  const RtOptions opt = lambert_options(plane_parallel);
-  cudaStream_t s = (cudaStream_t)stream;
-  double* r = radiance_VL;
-  double* f = reflectance_VL;
-  switch (nstreams) {
-    case 4: return launch_scalar_lambert_fixed<4>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
-    case 6: return launch_scalar_lambert_fixed<6>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
-    case 8: return launch_scalar_lambert_fixed<8>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
-    case 12: return launch_scalar_lambert_fixed<12>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
-    case 16: return launch_scalar_lambert_fixed<16>(opt, in, arena, arena_doubles, sched, num_sms, r, f, nfourier, status, s);
-  }
-  return set_error(AERORT_RC_UNSUPPORTED, "nstreams must be one of 4, 6, 8, 12, 16");
+  const Schedule sc;  // 64 threads per block, occupancy-limited
+  return dispatch_fixed(AERORT_PREC_FP64, nstreams, lambert_options(plane_parallel), in, arena,
+                        arena_doubles * sizeof(double), sched, num_sms, sc, radiance_VL, reflectance_VL, nfourier,
+                        status, (cudaStream_t)stream);
 }
 
 extern "C" int aerort_vlidort_scalar_lambert_ex(int km, int nch, int nobs, const double* channels, int nstreams,
@@ -731,7 +819,25 @@ __global__ void k_dfma_probe(int iters, double* out) {
   double r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
   if (r == 1234.5) out[0] = r;  // keeps the chains live
 }
+__global__ void k_ffma_probe(int iters, float* out) {
+  float a0 = threadIdx.x * 1e-9f, a1 = a0 + 1e-9f, a2 = a0 + 2e-9f, a3 = a0 + 3e-9f;
+  float a4 = a0 + 4e-9f, a5 = a0 + 5e-9f, a6 = a0 + 6e-9f, a7 = a0 + 7e-9f;
+  const float b = 0.9999f, c = 1e-7f;
+  for (int i = 0; i < iters; ++i) {
+    a0 = fmaf(a0, b, c); a1 = fmaf(a1, b, c); a2 = fmaf(a2, b, c); a3 = fmaf(a3, b, c);
+    a4 = fmaf(a4, b, c); a5 = fmaf(a5, b, c); a6 = fmaf(a6, b, c); a7 = fmaf(a7, b, c);
+  }
+  float r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (r == 1234.5f) out[0] = r;
+}
 }  // namespace
+
+extern "C" int aerort_probe_ffma(int blocks, int threads, int iters, float* out_dev, void* stream) {
+  if (blocks <= 0 || threads <= 0 || iters <= 0 || !out_dev) return set_error(AERORT_RC_ARG, "probe_ffma: bad arguments");
+  k_ffma_probe<<<blocks, threads, 0, (cudaStream_t)stream>>>(iters, out_dev);
+  CUDA_TRY(cudaGetLastError());
+  return AERORT_OK;
+}
 
 extern "C" int aerort_probe_dfma(int blocks, int threads, int iters, double* out_dev, void* stream) {
   if (blocks <= 0 || threads <= 0 || iters <= 0 || !out_dev) return set_error(AERORT_RC_ARG, "probe_dfma: bad arguments");

@@ -64,10 +64,10 @@ template <int NS, typename T>
 int launch_scalar_lambert(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
                           double* refl, int* nf, int* st, cudaStream_t s);
 
-template <int NS>
-int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* arena,
-                                size_t arena_doubles, int* sched, int num_sms, double* rad, double* refl, int* nf,
-                                int* st, cudaStream_t s);
+template <int NS, typename T>
+int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::LambertInputs& in, void* arena,
+                                size_t arena_bytes, int* sched, int num_sms, const Schedule& sc, double* rad,
+                                double* refl, int* nf, int* st, cudaStream_t s);
 
 // Static device arena of the allocation-free entry point (rt_static.cu):
 // address of the calling thread's current device's copy, set up on first use.

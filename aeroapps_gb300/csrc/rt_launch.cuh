@@ -67,30 +67,30 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   return 0;
 }
 
-// Same launch on caller-independent fixed storage: the per-thread scratch
-// comes from a static arena of arena_doubles doubles and the two scheduling
-// ints from sched (both reset or fully rewritten here, so neither needs to
-// start at zero).  The persistent grid is capped so that its threads' scratch
-// fits the arena; any nobs is then covered by the work queue.
-template <int NS>
-int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, double* arena, size_t arena_doubles,
-                                int* sched, int num_sms, double* rad, double* refl, int* nf, int* st,
-                                cudaStream_t s) {
+// Same launch on fixed storage owned by the caller: the per-thread scratch
+// comes from an arena of arena_bytes and the two scheduling ints from sched
+// (both reset or fully rewritten here, so neither needs to start at zero).
+// The persistent grid is capped so that its threads' scratch fits the arena;
+// any nobs is then covered by the work queue.
+template <int NS, typename T>
+int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, void* arena, size_t arena_bytes,
+                                int* sched, int num_sms, const Schedule& sc, double* rad, double* refl, int* nf,
+                                int* st, cudaStream_t s) {
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
-  const int bs = 64;
+  const int bs = sc.threads;
   const ScratchLayout<NS> lay(in.km);
-  const long fit_blocks = (long)(arena_doubles * sizeof(double) / ((size_t)lay.template bytes<double>() * bs));
+  const long fit_blocks = (long)(arena_bytes / ((size_t)lay.template bytes<T>() * bs));
   if (fit_blocks < 1)
-    return set_error(AERORT_RC_ARG, "scalar_lambert_noalloc: one 64-thread block needs more scratch than the "
-                                    "static arena holds");
+    return set_error(AERORT_RC_ARG, "scalar_lambert: one block needs more scratch than the workspace holds");
   Quad q;
   std::memset(&q, 0, sizeof(q));
   gauss_legendre01(NS, q.qx, q.qw);
   if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
   int per_sm = 0;
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS, double>, bs, 0));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert<NS, T>, bs, 0));
   if (per_sm < 1) per_sm = 1;
+  if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
   long nblocks = (nsolve + bs - 1) / bs;
   if (nblocks > (long)per_sm * num_sms) nblocks = (long)per_sm * num_sms;
   if (nblocks > fit_blocks) nblocks = fit_blocks;
@@ -103,8 +103,8 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, d
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
-  k_scalar_lambert<NS, double><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, arena, nthreads, nsolve, counter, rad,
-                                                                refl, nf, st);
+  k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, arena, nthreads, nsolve, counter, rad, refl,
+                                                           nf, st);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -118,6 +118,9 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, d
   template int aerort_internal::launch_scalar_lambert<NS, float>(                                              \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
       int*, cudaStream_t);                                                                                      \
-  template int aerort_internal::launch_scalar_lambert_fixed<NS>(                                               \
-      const aerort::RtOptions&, const aerort::LambertInputs&, double*, size_t, int*, int, double*, double*, int*, \
-      int*, cudaStream_t);
+  template int aerort_internal::launch_scalar_lambert_fixed<NS, double>(                                       \
+      const aerort::RtOptions&, const aerort::LambertInputs&, void*, size_t, int*, int,                         \
+      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t);                            \
+  template int aerort_internal::launch_scalar_lambert_fixed<NS, float>(                                        \
+      const aerort::RtOptions&, const aerort::LambertInputs&, void*, size_t, int*, int,                         \
+      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t);

@@ -23,8 +23,8 @@
 //   .../vlidort_main/regular/vlidort_converge.f90:825-1236             (Fourier convergence)
 //   .../vlidort_focode/*.f90                                           (first-order single scatter)
 // The numerical methods differ where GB300 favours another formulation (see
-// sym_eigen_layer and the block sweep in fourier_term); results agree with the
-// reference algorithm to round-off.
+// layer_eigen and the block sweep in fourier_term in rt_solve.cuh); results
+// agree with the reference algorithm to round-off.
 #pragma once
 
 #ifdef __CUDACC__
@@ -150,99 +150,10 @@ RT_HD bool cholesky(int n, T* A) {
   return true;
 }
 
-// Symmetric eigendecomposition H = V diag(lam) V^T of an n x n matrix stored
-// column-major with leading dimension NS: Householder reduction to
-// tridiagonal form with the transformations accumulated in V, then implicit
-// QR sweeps with Wilkinson shifts applied as Givens rotations.  H is
-// destroyed.  Returns false if the iteration budget is exhausted.
+// Unit roundoff of the working precision.
 template <typename T> struct Eps;
 template <> struct Eps<double> { static constexpr double v = 2.220446049250313e-16; };
 template <> struct Eps<float> { static constexpr float v = 1.1920929e-07f; };
-
-template <int NS, typename T>
-RT_HD bool sym_eigen(int n, T* H, T* V, T* lam) {
-  for (int j = 0; j < n; ++j)
-    for (int i = 0; i < n; ++i) V[i + NS * j] = (i == j) ? 1.0 : 0.0;
-  T v[NS], p[NS];
-  for (int k = 0; k + 2 < n; ++k) {
-    // Householder vector for column k below the subdiagonal
-    T alpha2 = 0.0;
-    for (int i = k + 1; i < n; ++i) alpha2 += H[i + NS * k] * H[i + NS * k];
-    if (alpha2 == 0.0) continue;
-    T x0 = H[(k + 1) + NS * k];
-    T alpha = -copysign(sqrt(alpha2), x0);
-    for (int i = k + 1; i < n; ++i) v[i] = H[i + NS * k];
-    v[k + 1] = x0 - alpha;
-    T vtv = alpha2 - x0 * x0 + v[k + 1] * v[k + 1];
-    if (vtv == 0.0) continue;
-    T beta = (T)2 / vtv;
-    // p = beta * H22 v ; w = p - (beta/2)(p.v) v ; H22 -= v w^T + w v^T
-    T pv = 0.0;
-    for (int i = k + 1; i < n; ++i) {
-      T s = 0.0;
-      for (int j = k + 1; j < n; ++j) s += H[i + NS * j] * v[j];
-      p[i] = beta * s;
-      pv += p[i] * v[i];
-    }
-    T half = (T)0.5 * beta * pv;
-    for (int i = k + 1; i < n; ++i) p[i] -= half * v[i];
-    for (int j = k + 1; j < n; ++j)
-      for (int i = k + 1; i < n; ++i) H[i + NS * j] -= v[i] * p[j] + p[i] * v[j];
-    H[(k + 1) + NS * k] = alpha;
-    H[k + NS * (k + 1)] = alpha;
-    for (int i = k + 2; i < n; ++i) { H[i + NS * k] = 0.0; H[k + NS * i] = 0.0; }
-    // V <- V (I - beta v v^T)
-    for (int i = 0; i < n; ++i) {
-      T s = 0.0;
-      for (int j = k + 1; j < n; ++j) s += V[i + NS * j] * v[j];
-      s *= beta;
-      for (int j = k + 1; j < n; ++j) V[i + NS * j] -= s * v[j];
-    }
-  }
-  T d[NS], e[NS];  // e[i] couples i and i+1
-  for (int i = 0; i < n; ++i) d[i] = H[i + NS * i];
-  for (int i = 0; i + 1 < n; ++i) e[i] = H[(i + 1) + NS * i];
-  const T eps = Eps<T>::v;
-  int q = n - 1, sweeps = 0;
-  while (q > 0) {
-    // deflate negligible couplings at the bottom of the active block
-    if (fabs(e[q - 1]) <= eps * (fabs(d[q - 1]) + fabs(d[q]))) { e[q - 1] = 0.0; --q; continue; }
-    int p0 = q - 1;
-    while (p0 > 0 && fabs(e[p0 - 1]) > eps * (fabs(d[p0 - 1]) + fabs(d[p0]))) --p0;
-    if (p0 > 0) e[p0 - 1] = 0.0;
-    if (++sweeps > 40 * n) return false;
-    // Wilkinson shift from the trailing 2x2 block
-    T dd = (T)0.5 * (d[q - 1] - d[q]);
-    T eq = e[q - 1];
-    T den = dd + copysign(sqrt(dd * dd + eq * eq), dd);
-    T mu = d[q] - (den != (T)0 ? eq * eq / den : (T)0);
-    T x = d[p0] - mu, z = e[p0];
-    T bulge = 0.0;
-    for (int k = p0; k < q; ++k) {
-      T r = sqrt(x * x + z * z);
-      T c = (r == (T)0) ? (T)1 : x / r, s = (r == (T)0) ? (T)0 : z / r;
-      // rotate rows/columns k, k+1 of the tridiagonal (with bulge below it)
-      if (k > p0) e[k - 1] = r;
-      T dk = d[k], dk1 = d[k + 1], ek = e[k];
-      d[k] = c * c * dk + (T)2 * c * s * ek + s * s * dk1;
-      d[k + 1] = s * s * dk - (T)2 * c * s * ek + c * c * dk1;
-      e[k] = c * s * (dk1 - dk) + (c * c - s * s) * ek;
-      if (k + 1 < q) {
-        bulge = s * e[k + 1];
-        e[k + 1] = c * e[k + 1];
-        x = e[k];
-        z = bulge;
-      }
-      for (int i = 0; i < n; ++i) {
-        T a = V[i + NS * k], b = V[i + NS * (k + 1)];
-        V[i + NS * k] = c * a + s * b;
-        V[i + NS * (k + 1)] = -s * a + c * b;
-      }
-    }
-  }
-  for (int i = 0; i < n; ++i) lam[i] = d[i];
-  return true;
-}
 
 // A <- Q A Q for the reflector Q = I - beta v v^T (A symmetric, full storage,
 // column-major with leading dimension NS).

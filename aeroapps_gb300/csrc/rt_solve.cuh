@@ -229,7 +229,6 @@ RT_HD int layer_eigen(const SolveCtx<NS, T>& c, int m, T dtau, T om1, const T* o
                       LayerSol<NS, T>& ls, T* kv, T* Sp, T* norm, T* uh_dn, T* uh_up) {
   const int N = NS, NM = c.NM;
   T Bs[NS * NS], H[NS * NS], V[NS * NS];
-  [[maybe_unused]] T lam[NS];
   // Sp (even l-m) and Sm (odd l-m) contractions of omega*beta_l P_l(mu_i) P_l(mu_j)
   for (int j = 0; j < N; ++j)
     for (int i = 0; i <= j; ++i) {
@@ -248,113 +247,59 @@ RT_HD int layer_eigen(const SolveCtx<NS, T>& c, int m, T dtau, T om1, const T* o
   for (int j = 0; j < N; ++j)
     for (int i = j; i < N; ++i) Bs[i + NS * j] /= c.qx[i];
   T kq[NS];  // k of each eigenvector column of V
-  [[maybe_unused]] T G[NS * NS];  // FP32 path: La u_a per eigenvector
-  if constexpr (sizeof(T) == sizeof(float)) {
-    // FP32: H = G^T G with G = La^T R (As = La La^T).  One-sided Jacobi
-    // (Hestenes) orthogonalises the columns of G by plane rotations V, so that
-    // the singular values k = |G V e_a| come with relative accuracy even
-    // though the k span four decades; the eigenvectors of H are the columns of V.
-    T rv[NS], rbeta = 0;
-    if (m == 0) {
-      // Fourier term 0: As has the exact eigenvector s = W^1/2 1 with
-      // eigenvalue 1 - omega (the half-range Gauss rule integrates every even
-      // moment l >= 2 to zero).  The reflector Q (Q s = -e_1 |s|) splits it
-      // off exactly; 1 - omega comes from FP64, so nearly conservative layers
-      // keep their small eigenvalue, and only the well-conditioned complement
-      // B = (Q As Q)[1:, 1:] is factorised in FP32.  La = Q diag(sqrt(1-omega), Lb_B).
-      T v[NS], vv = 0;
-      {
-        T ns = 0;
-        for (int i = 0; i < N; ++i) { v[i] = c.sqw[i]; ns += v[i] * v[i]; }
-        ns = sqrt(ns);
-        v[0] += ns;  // s has positive entries
-        for (int i = 0; i < N; ++i) vv += v[i] * v[i];
-      }
-      const T beta = (T)2 / vv;
-      rbeta = beta;
-      for (int i = 0; i < N; ++i) rv[i] = v[i];
-      // As (full) in H, then C = Q As Q
-      for (int j = 0; j < N; ++j)
-        for (int i = 0; i < N; ++i) {
-          T a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
-          if (i == j) a += (T)1;
-          H[i + NS * j] = a;
-        }
-      apply_reflector_sym<NS>(N, H, v, beta);
-      H[0] = om1;
-      for (int i = 1; i < N; ++i) { H[i] = 0; H[NS * i] = 0; }
-      if (!(om1 > (T)0) || !cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
-      // G = La^T R = diag-block(L~)^T (Q R)
-      T QR[NS * NS];
-      for (int j = 0; j < N; ++j) {
-        T d = 0;
-        for (int k = j; k < N; ++k) d += v[k] * Bs[k + NS * j];
-        d *= beta;
-        for (int i = 0; i < N; ++i) QR[i + NS * j] = ((i >= j) ? Bs[i + NS * j] : (T)0) - d * v[i];
-      }
-      for (int j = 0; j < N; ++j)
-        for (int i = 0; i < N; ++i) {
-          T s = 0;
-          for (int k = i; k < N; ++k) s += H[k + NS * i] * QR[k + NS * j];
-          G[i + NS * j] = s;
-        }
-    } else {
-      for (int j = 0; j < N; ++j)
-        for (int i = j; i < N; ++i) {
-          T a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
-          if (i == j) a += (T)1;
-          H[i + NS * j] = a;
-        }
-      if (!cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
-      for (int j = 0; j < N; ++j)
-        for (int i = 0; i < N; ++i) {
-          T s = 0;
-          for (int k = (i > j ? i : j); k < N; ++k) s += H[k + NS * i] * Bs[k + NS * j];
-          G[i + NS * j] = s;
-        }
+  T G[NS * NS];
+  // H = G^T G with G = La^T R (As = La La^T).  One-sided Jacobi (Hestenes)
+  // orthogonalises the columns of G by plane rotations V, so that the
+  // singular values k = |G V e_a| and the eigenvectors (columns of V) come with
+  // relative accuracy although k^2 spans four to five decades (1/mu^2 of the
+  // shallowest stream); a QR eigensolver on H itself leaves the small-k
+  // eigenvectors an error of order eps |H| / gap.
+  T rv[NS], rbeta = 0;
+  if (m == 0) {
+    // Fourier term 0: As has the exact eigenvector s = W^1/2 1 with
+    // eigenvalue 1 - omega (the half-range Gauss rule integrates every even
+    // moment l >= 2 to zero).  The reflector Q (Q s = -e_1 |s|) splits it
+    // off exactly; 1 - omega comes from the FP64 set-up, so nearly
+    // conservative layers keep their small eigenvalue in either precision,
+    // and only the well-conditioned complement B = (Q As Q)[1:, 1:] is
+    // factorised.  La = Q diag(sqrt(1-omega), Lb_B).
+    T v[NS], vv = 0;
+    {
+      T ns = 0;
+      for (int i = 0; i < N; ++i) { v[i] = c.sqw[i]; ns += v[i] * v[i]; }
+      ns = sqrt(ns);
+      v[0] += ns;  // s has positive entries
+      for (int i = 0; i < N; ++i) vv += v[i] * v[i];
     }
-    if (!jacobi_svd<NS>(N, G, V, kq)) return RT_EIGEN_FAIL;
-    // G now holds G V = U diag(k).  As v_a = La La^T R q_a = La (G V)e_a, so
-    // SAB x / k needs La u_a only (u_a = unit left singular vector): no
-    // cancellation for the small-k modes.  Overwrite G[:, a] with La u_a.
-    for (int a = 0; a < N; ++a) {
-      if (!(kq[a] > (T)0)) return RT_EIGEN_FAIL;
-      const T inv = (T)1 / kq[a];
-      T u[NS], y[NS];
-      for (int i = 0; i < N; ++i) u[i] = G[i + NS * a] * inv;
+    const T beta = (T)2 / vv;
+    rbeta = beta;
+    for (int i = 0; i < N; ++i) rv[i] = v[i];
+    // As (full) in H, then C = Q As Q
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        T a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
+        if (i == j) a += (T)1;
+        H[i + NS * j] = a;
+      }
+    apply_reflector_sym<NS>(N, H, v, beta);
+    H[0] = om1;
+    for (int i = 1; i < N; ++i) { H[i] = 0; H[NS * i] = 0; }
+    if (!(om1 > (T)0) || !cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
+    // G = La^T R = diag-block(L~)^T (Q R)
+    T QR[NS * NS];
+    for (int j = 0; j < N; ++j) {
+      T d = 0;
+      for (int k = j; k < N; ++k) d += v[k] * Bs[k + NS * j];
+      d *= beta;
+      for (int i = 0; i < N; ++i) QR[i + NS * j] = ((i >= j) ? Bs[i + NS * j] : (T)0) - d * v[i];
+    }
+    for (int j = 0; j < N; ++j)
       for (int i = 0; i < N; ++i) {
         T s = 0;
-        for (int k = 0; k <= i; ++k) s += H[i + NS * k] * u[k];
-        y[i] = s;
+        for (int k = i; k < N; ++k) s += H[k + NS * i] * QR[k + NS * j];
+        G[i + NS * j] = s;
       }
-      if (m == 0) {
-        T d = 0;
-        for (int i = 0; i < N; ++i) d += rv[i] * y[i];
-        d *= rbeta;
-        for (int i = 0; i < N; ++i) y[i] -= d * rv[i];
-      }
-      for (int i = 0; i < N; ++i) G[i + NS * a] = y[i];
-    }
   } else {
-    // Y = As R with As = I - W^1/2 Sp W^1/2 ; H = R^T Y
-    for (int j = 0; j < N; ++j)
-      for (int i = 0; i < N; ++i) {
-        T y = (i >= j) ? Bs[i + NS * j] : (T)0;
-        T s = 0;
-        for (int k = j; k < N; ++k) s += c.sqw[i] * Sp[i + NS * k] * c.sqw[k] * Bs[k + NS * j];
-        V[i + NS * j] = y - s;  // V used as temporary for Y
-      }
-    for (int j = 0; j < N; ++j)
-      for (int i = 0; i <= j; ++i) {
-        T s = 0;
-        for (int k = i; k < N; ++k) s += Bs[k + NS * i] * V[k + NS * j];
-        H[i + NS * j] = s; H[j + NS * i] = s;
-      }
-    if (!sym_eigen<NS>(N, H, V, lam)) return RT_EIGEN_FAIL;
-    // As = La La^T: the eigenvalues are recomputed as Rayleigh quotients
-    // lam = q^T R^T As R q = |La^T (R q)|^2, which keeps full relative accuracy
-    // for the small eigenvalues of nearly conservative layers (forming H
-    // explicitly leaves them an absolute error of order eps*|H|).
     for (int j = 0; j < N; ++j)
       for (int i = j; i < N; ++i) {
         T a = -c.sqw[i] * Sp[i + NS * j] * c.sqw[j];
@@ -362,24 +307,34 @@ RT_HD int layer_eigen(const SolveCtx<NS, T>& c, int m, T dtau, T om1, const T* o
         H[i + NS * j] = a;
       }
     if (!cholesky<NS>(N, H)) return RT_EIGEN_FAIL;
-    for (int a = 0; a < N; ++a) {
-      T v[NS];
+    for (int j = 0; j < N; ++j)
       for (int i = 0; i < N; ++i) {
         T s = 0;
-        for (int j = 0; j <= i; ++j) s += Bs[i + NS * j] * V[j + NS * a];
-        v[i] = s;
+        for (int k = (i > j ? i : j); k < N; ++k) s += H[k + NS * i] * Bs[k + NS * j];
+        G[i + NS * j] = s;
       }
-      T qq = 0, lr = 0;
-      for (int i = 0; i < N; ++i) {
-        qq += V[i + NS * a] * V[i + NS * a];
-        T w = 0;
-        for (int j = i; j < N; ++j) w += H[j + NS * i] * v[j];
-        lr += w * w;
-      }
-      lr /= qq;
-      if (!(lr > (T)0)) return RT_EIGEN_FAIL;
-      kq[a] = sqrt(lr);
+  }
+  if (!jacobi_svd<NS>(N, G, V, kq)) return RT_EIGEN_FAIL;
+  // G now holds G V = U diag(k).  As v_a = La La^T R q_a = La (G V)e_a, so
+  // SAB x / k needs La u_a only (u_a = unit left singular vector): no
+  // cancellation for the small-k modes.  Overwrite G[:, a] with La u_a.
+  for (int a = 0; a < N; ++a) {
+    if (!(kq[a] > (T)0)) return RT_EIGEN_FAIL;
+    const T inv = (T)1 / kq[a];
+    T u[NS], y[NS];
+    for (int i = 0; i < N; ++i) u[i] = G[i + NS * a] * inv;
+    for (int i = 0; i < N; ++i) {
+      T s = 0;
+      for (int k = 0; k <= i; ++k) s += H[i + NS * k] * u[k];
+      y[i] = s;
     }
+    if (m == 0) {
+      T d = 0;
+      for (int i = 0; i < N; ++i) d += rv[i] * y[i];
+      d *= rbeta;
+      for (int i = 0; i < N; ++i) y[i] -= d * rv[i];
+    }
+    for (int i = 0; i < N; ++i) G[i + NS * a] = y[i];
   }
   for (int a = 0; a < N; ++a) {
     // v = R q ; sum vector x = W^-1/2 v, unit 2-norm
@@ -395,16 +350,11 @@ RT_HD int layer_eigen(const SolveCtx<NS, T>& c, int m, T dtau, T om1, const T* o
     kv[a] = k;
     nrm = (T)1 / sqrt(nrm);
     for (int i = 0; i < N; ++i) x[i] *= nrm;
-    // difference vector SAB x / k ; SAB(i,j) = (delta_ij - w_j Sp(i,j)) / mu_i
-    T invk = (T)1 / k, dif[NS], nr = 0;
+    // difference vector SAB x / k = M^-1 W^-1/2 As v / (k |W^-1/2 v|)
+    //                             = M^-1 W^-1/2 La u_a / |W^-1/2 v|
+    T dif[NS], nr = 0;
     for (int i = 0; i < N; ++i) {
-      if constexpr (sizeof(T) == sizeof(float)) {
-        dif[i] = G[i + NS * a] / (c.qx[i] * c.sqw[i]) * nrm;
-      } else {
-        T s = 0;
-        for (int j = 0; j < N; ++j) s += c.qw[j] * Sp[i + NS * j] * x[j];
-        dif[i] = (x[i] - s) / c.qx[i] * invk;
-      }
+      dif[i] = G[i + NS * a] / (c.qx[i] * c.sqw[i]) * nrm;
       ls.P[i + NS * a] = (T)0.5 * (x[i] + dif[i]);
       ls.Q[i + NS * a] = (T)0.5 * (x[i] - dif[i]);
       nr += c.qx[i] * c.qw[i] * x[i] * dif[i];
@@ -716,6 +666,180 @@ constexpr double kSsaCap = 0.999989986419677734375;            // 0.99999
 constexpr double kAccuracySingle = 9.99999974737875163555145263671875e-05;  // 0.0001
 
 // ---------------------------------------------------------------------------------- geometry
+// Two forms of the spherical-shell geometry.  The plain FP64 method keeps the
+// reference's law-of-sines form (asin of the local zenith sines, sin of their
+// differences), whose rounding at small solar zenith angles is part of the
+// result the plain method must reproduce to 1e-9.  The mixed method uses the
+// chord form below (square roots only).
+
+// Sun path through layers 1..nn of a straight ray that leaves radius radstart
+// with local solar zenith th (sine sth), layers ordered from TOA (index 0 of
+// radii) down; returns sum_k ext_k * path_k.  Direct-sun and tangent-ray
+// branches follow FO_geometry_Generic.f90:169-329 (FindSunPaths_D / _T).
+RT_HD double sun_optical_path_ref(bool zero_sun_boa, bool direct, double radstart, double th, double sth, int nn,
+                              double R0, const Scratch& S, long ohgt, long oext, int L) {
+  auto radius = [&](int k) { return R0 + S[ohgt + k]; };
+  double tau = 0.0;
+  if (direct) {
+    if (zero_sun_boa) {
+      tau += S[oext + nn - 1] * (radius(nn - 1) - radstart);
+      for (int k = nn - 1; k >= 1; --k) tau += S[oext + k - 1] * (radius(k - 1) - radius(k));
+      return tau;
+    }
+    double sth0 = sth, th0 = th;
+    double sth1 = sth0 * radstart / radius(nn - 1), th1 = asin(sth1);
+    tau += S[oext + nn - 1] * (sin(th0 - th1) * radstart / sth1);
+    sth0 = sth1; th0 = th1;
+    for (int k = nn - 1; k >= 1; --k) {
+      sth1 = sth0 * radius(k) / radius(k - 1);
+      th1 = asin(sth1);
+      tau += S[oext + k - 1] * (sin(th0 - th1) * radius(k) / sth1);
+      sth0 = sth1; th0 = th1;
+    }
+    return tau;
+  }
+  // tangent ray: passes its lowest point below the start level, then rises to TOA
+  double tanr = sth * radstart;
+  int k = nn - 1;
+  bool trawl = true;
+  while (k >= nn - 1 && trawl && k <= L) { trawl = (radius(k) > tanr); k = k + 1; }
+  int nt = k - 1;
+  double pnn = 0.0;
+  if (nt > nn) {
+    double th0 = kPIE - th, sth0 = sth;
+    double sth1 = sth0 * radstart / radius(nn), th1 = asin(sth1);
+    pnn = 2.0 * sin(th0 - th1) * radstart / sth1;
+    sth0 = sth1; th0 = th1;
+    for (int kk = nn + 1; kk <= nt - 1; ++kk) {
+      sth1 = sth0 * radius(kk - 1) / radius(kk);
+      th1 = asin(sth1);
+      tau += S[oext + kk - 1] * (2.0 * sin(th0 - th1) * radius(kk) / sth0);
+      sth0 = sth1; th0 = th1;
+    }
+    tau += S[oext + nt - 1] * (2.0 * sin(0.5 * kPIE - th0) * radius(nt - 1));
+  } else if (nt == nn) {
+    pnn = -2.0 * radstart * cos(th);
+  }
+  double th0 = kPIE - th, sth0 = sth;
+  double sth1 = sth0 * radstart / radius(nn - 1), th1 = asin(sth1);
+  tau += S[oext + nn - 1] * (pnn + sin(th0 - th1) * radstart / sth1);
+  sth0 = sth1; th0 = th1;
+  for (int kk = nn - 1; kk >= 1; --kk) {
+    sth1 = sth0 * radius(kk) / radius(kk - 1);
+    th1 = asin(sth1);
+    tau += S[oext + kk - 1] * (sin(th0 - th1) * radius(kk) / sth1);
+    sth0 = sth1; th0 = th1;
+  }
+  return tau;
+}
+
+// First-order single scatter, law-of-sines geometry (plain method); see
+// fo_single_scatter_chord for the references.
+RT_HD bool fo_single_scatter_ref(const RtOptions& opt, bool enhanced, int L, double sza, double vza, double phi,
+                             double albedo, const double* tu, const double* wu, const Scratch& S, long ohgt, long oext,
+                             long oescat, long odts, double* ss, double* db) {
+  const double R0 = opt.earth_radius;
+  auto radius = [&](int k) { return R0 + S[ohgt + k]; };
+  const double flux = opt.flux_factor / kPI4;
+  const bool overhead = (sza == 0.0);
+  const double th_R = sza * kDTR;
+  double cth, sthb;
+  if (sza == 90.0) { cth = 0.0; sthb = 1.0; } else { sthb = sin(th_R); cth = cos(th_R); }
+  double cum = 0.0, trans_above = 1.0, atten_boa = 0.0;
+  if (!enhanced) {
+    double ca = (vza == 90.0) ? 0.0 : cos(vza * kDTR);
+    double tau_prev = 0.0, att_prev = 1.0;
+    for (int n = 1; n <= L; ++n) {
+      double st;
+      if (opt.do_plane_parallel) {
+        st = 0.0;
+        for (int k = 1; k <= n; ++k) st += S[oext + k - 1] * ((S[ohgt + k - 1] - S[ohgt + k]) / cth);
+      } else {
+        st = sun_optical_path_ref(overhead, true, radius(n), th_R, sthb, n, R0, S, ohgt, oext, L);
+      }
+      double att = st < kFoCutoff ? exp(-st) : 0.0;
+      double lostrans = 0.0, mult = 0.0;
+      if (ca > 0.0) {
+        double lostau = S[odts + n - 1] / ca;
+        if (lostau < kFoCutoff) lostrans = exp(-lostau);
+        mult = (att_prev - att * lostrans) / (1.0 + (st - tau_prev) / lostau);
+      }
+      cum += trans_above * S[oescat + n - 1] * mult;
+      trans_above *= lostrans;
+      tau_prev = st; att_prev = att;
+      if (n == L) atten_boa = att;
+    }
+    *ss = flux * cum;
+    *db = flux * (4.0 * cth * albedo * atten_boa) * trans_above;
+    return true;
+  }
+  const bool donadir = (vza == 0.0);
+  double raycon = 0.0, alphaL = 0.0, caL = 1.0;
+  if (!donadir) {
+    alphaL = vza * kDTR;
+    double sa = (vza == 90.0) ? 1.0 : sin(alphaL);
+    caL = (vza == 90.0) ? 0.0 : cos(alphaL);
+    raycon = sa * radius(L);
+  }
+  // solar direction at BOA (the y component does not enter: the line of sight lies in the x-z plane)
+  double sdir0 = 0.0, sdir2 = 0.0;
+  if (!overhead) { sdir0 = -sthb * cos(phi * kDTR); sdir2 = -cth; }
+  auto findsun = [&](double rad, double cumangle, double* th, double* sth, bool* dirsun) {
+    if (donadir) { *dirsun = true; *th = th_R; *sth = sin(th_R); return; }
+    if (overhead) { *dirsun = true; *sth = sin(cumangle); *th = cumangle; return; }
+    double b = (-rad * sin(cumangle)) * sdir0 + (rad * cos(cumangle)) * sdir2;
+    double ct = -b / rad;
+    *dirsun = (ct >= 0.0);
+    *sth = sqrt(1.0 - ct * ct);
+    *th = acos(ct);
+  };
+  // direct-sun attenuation at the surface (used by the direct bounce)
+  {
+    double st = sun_optical_path_ref(overhead, true, radius(L), th_R, sthb, L, R0, S, ohgt, oext, L);
+    atten_boa = st < kFoCutoff ? exp(-st) : 0.0;
+  }
+  // top-down accumulation of the line-of-sight source: TOA sees layer n through layers 1..n-1
+  for (int n = 1; n <= L; ++n) {
+    double r_up = radius(n - 1), r_lo = radius(n);
+    double losw, cosa_lo;
+    if (donadir) {
+      losw = r_up - r_lo;
+      cosa_lo = 1.0;
+    } else {
+      double ca_up = cos(asin(raycon / r_up));
+      cosa_lo = (n == L) ? caL : cos(asin(raycon / r_lo));
+      losw = r_up * ca_up - r_lo * cosa_lo;
+    }
+    const double kn = S[oext + n - 1];
+    const double lostau = kn * losw;
+    const double lostrans = lostau < kFoCutoff ? exp(-lostau) : 0.0;
+    const bool zero_sun_boa = overhead && (n == L || donadir);
+    double sum = 0.0;
+    for (int j = 0; j < opt.nfine; ++j) {
+      const double tf = losw * tu[j], wf = losw * wu[j];
+      double rf, af = 0.0;
+      if (donadir) {
+        rf = r_lo + tf;
+      } else {
+        double tanf = raycon / (r_lo * cosa_lo + tf);
+        af = atan(tanf);
+        rf = raycon / sin(af);
+      }
+      double thf, sthf; bool dsf;
+      findsun(rf, alphaL - af, &thf, &sthf, &dsf);
+      double sd = sun_optical_path_ref(zero_sun_boa, dsf, rf, thf, sthf, n, R0, S, ohgt, oext, L);
+      double attf = sd < kFoCutoff ? exp(-sd) : 0.0;
+      sum += attf * exp(-kn * (losw - tf)) * wf;
+    }
+    cum += trans_above * S[oescat + n - 1] * (sum * kn);
+    trans_above *= lostrans;
+  }
+  *ss = flux * cum;
+  *db = flux * (4.0 * cth * albedo * atten_boa) * trans_above;
+  return true;
+}
+
+
 // Spherical-shell geometry without inverse trigonometry.  A straight ray with
 // impact parameter p (distance of closest approach to the Earth's centre)
 // crosses the shell between radii r_lo < r_hi on a chord of length
@@ -732,7 +856,7 @@ RT_HD double shell_c(double r, double p) { return sqrt((r - p) * (r + p)); }
 // sine st there; layers ordered from TOA (level 0) down; returns
 // sum_k ext_k * path_k.  Direct-sun and tangent-ray branches follow
 // FO_geometry_Generic.f90:169-329 (FindSunPaths_D / _T).
-RT_HD double sun_optical_path(bool zero_sun_boa, bool direct, double radstart, double ct, double st, int nn,
+RT_HD double sun_optical_path_chord(bool zero_sun_boa, bool direct, double radstart, double ct, double st, int nn,
                               double R0, const Scratch& S, long ohgt, long oext, int L) {
   auto radius = [&](int k) { return R0 + S[ohgt + k]; };
   double tau = 0.0;
@@ -801,7 +925,7 @@ RT_HD double sun_optical_path(bool zero_sun_boa, bool direct, double radstart, d
 // enhanced PS with NFINE quadrature points per layer along the line of sight,
 // FO_VectorSS_RTCalcs_I.f90:116-787).  Layer phase sums (escat) and
 // extinctions (ext, per km) are in scratch.  Returns false on a degenerate path.
-RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double sza, double vza, double phi,
+RT_HD bool fo_single_scatter_chord(const RtOptions& opt, bool enhanced, int L, double sza, double vza, double phi,
                              double albedo, const double* tu, const double* wu, const Scratch& S, long ohgt, long oext,
                              long oescat, long odts, double* ss, double* db) {
   const double R0 = opt.earth_radius;
@@ -821,7 +945,7 @@ RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double 
         st = 0.0;
         for (int k = 1; k <= n; ++k) st += S[oext + k - 1] * ((S[ohgt + k - 1] - S[ohgt + k]) / cth);
       } else {
-        st = sun_optical_path(overhead, true, radius(n), cth, sthb, n, R0, S, ohgt, oext, L);
+        st = sun_optical_path_chord(overhead, true, radius(n), cth, sthb, n, R0, S, ohgt, oext, L);
       }
       double att = st < kFoCutoff ? exp(-st) : 0.0;
       double lostrans = 0.0, mult = 0.0;
@@ -852,7 +976,7 @@ RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double 
   if (!overhead) { sdir0 = -sthb * cos(phi * kDTR); sdir2 = -cth; }
   // direct-sun attenuation at the surface (used by the direct bounce)
   {
-    double st = sun_optical_path(overhead, true, radius(L), cth, sthb, L, R0, S, ohgt, oext, L);
+    double st = sun_optical_path_chord(overhead, true, radius(L), cth, sthb, L, R0, S, ohgt, oext, L);
     atten_boa = st < kFoCutoff ? exp(-st) : 0.0;
   }
   // top-down accumulation of the line-of-sight source: TOA sees layer n through layers 1..n-1
@@ -896,7 +1020,7 @@ RT_HD bool fo_single_scatter(const RtOptions& opt, bool enhanced, int L, double 
         }
       }
       const bool dsf = donadir || overhead || (ct >= 0.0);
-      double sd = sun_optical_path(zero_sun_boa, dsf, rf, ct, st, n, R0, S, ohgt, oext, L);
+      double sd = sun_optical_path_chord(zero_sun_boa, dsf, rf, ct, st, n, R0, S, ohgt, oext, L);
       double attf = sd < kFoCutoff ? exp(-sd) : 0.0;
       sum += attf * exp(-kn * (losw - tf)) * wf;
     }
@@ -1043,7 +1167,12 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
     double phi = raa;
     if (phi < 0.0) phi = -phi;
     if (phi > 360.0) phi = 360.0 - phi - 360.0;
-    fo_single_scatter(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts, &ss, &db);
+    if constexpr (sizeof(T) == sizeof(float))
+      fo_single_scatter_chord(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts,
+                              &ss, &db);
+    else
+      fo_single_scatter_ref(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts,
+                            &ss, &db);
   }
   // ---------------------------------------------------------------- beam attenuation
   // Chapman factors (vlidort_geometry.f90:119-317), QSPREP / PREPTRANS / EMULT
@@ -1064,7 +1193,7 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
       if (opt.do_plane_parallel || sn_toa == 0.0) {
         double cf = opt.do_plane_parallel ? 1.0 / mu_toa : 1.0;
         for (int k = 1; k <= n; ++k) ts += S[lay.dtau + k - 1] * cf;
-      } else {
+      } else if constexpr (sizeof(T) == sizeof(float)) {
         const double rn = S[lay.hgt + n] + R0;
         const double p = sn_toa * rn;
         double r_lo = rn, c_lo = rn * mu_toa;
@@ -1072,6 +1201,19 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
           const double r_hi = S[lay.hgt + k - 1] + R0, c_hi = shell_c(r_hi, p);
           ts += S[lay.dtau + k - 1] * ((r_hi + r_lo) / (c_hi + c_lo));
           r_lo = r_hi; c_lo = c_hi;
+        }
+      } else {
+        const double r0 = S[lay.hgt + 0] + R0;
+        double sinth1 = sn_toa * (S[lay.hgt + n] + R0) / r0;
+        double sth1 = asin(sinth1), re_upper = r0;
+        for (int k = 1; k <= n; ++k) {
+          double delz = S[lay.hgt + k - 1] - S[lay.hgt + k];
+          double re_lower = re_upper - delz;
+          double sinth2 = re_upper * sinth1 / re_lower;
+          double sth2 = asin(sinth2);
+          double dist = re_upper * sin(sth2 - sth1) / sinth2;
+          ts += S[lay.dtau + k - 1] * (dist / delz);
+          re_upper = re_lower; sinth1 = sinth2; sth1 = sth2;
         }
       }
       const double dtn = S[lay.dtau + n - 1];

@@ -1,12 +1,16 @@
 """Benchmark: TOA radiances/s of the aerosol-optics + VLIDORT path on GB300.
 
+Metric: TOA radiances per second of the mixed-precision GPU solve, whose
+error against the FP64 solve is measured on every radiance of the batch and
+must stay <= 1e-4, reported beside the plain FP64 GPU solve of the same
+batch, with serving p50/p95/p99 latency.
+
 Workload (one step): one batch of synthetic columns of the 262,144-column
 batching configuration -- 4 wavelengths (470, 550, 670, 865 nm), per-column
 layer count uniform in 20..72, half-space streams drawn from {4,6,8,12,16},
-2 x streams Legendre moments, plain FP64 solve.  A step runs, for every
-stream-count group, the Mie-table AOP kernel (FP32) and the FP64 RT kernel on
-device-resident inputs.  The columns of every step are the same batch; the
-working set (hundreds of MB) exceeds the 129 MB L2.
+2 x streams Legendre moments.  A step runs, for every stream-count group, the
+Mie-table AOP kernel (FP32) and the RT kernel on device-resident inputs.  The
+optics and scratch of a step are hundreds of MB, more than the 129 MB L2.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -25,20 +29,28 @@ sys.path.insert(0, ROOT)
 
 STREAMS = (4, 6, 8, 12, 16)
 CHANNELS = (470.0, 550.0, 670.0, 865.0)
-METRIC = "TOA radiances/sec (plain FP64 GPU solve, 262,144-column batching config)"
-CONFIG_COLUMNS = 262144
+METRIC = ("TOA radiances/sec at <=1e-4 rel err vs FP64 (mixed-precision GPU solve; plain FP64 GPU solve and "
+          "serving p50/p99 latency reported beside it)")
+WORKLOAD = ("batching config: columns of the 262,144-column configuration, 20-72 layers, streams {4,6,8,12,16} "
+            "(moments 2x streams), 4 wavelengths; Mie AOP (FP32) + scalar Lambertian RT per stream group")
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cols", type=int, default=16384, help="columns per step (x4 wavelengths = solves)")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cols", type=int, default=8192, help="columns per step per GPU (x4 wavelengths = solves)")
+    ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 solve")
+    ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-cols", type=int, default=0, help="CPU-baseline sample columns (0 = auto)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate [requests/s]")
+    ap.add_argument("--serve-max-cols", type=int, default=4096, help="largest swath of the serving run")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--tune", action="store_true", help="autotune the RT schedules before timing")
     return ap.parse_args()
 
 
@@ -58,11 +70,12 @@ def make_batch(ncol, seed):
 
 
 def subset(cols, idx):
-    """Columns idx of a make_columns dict (keeps km)."""
+    """Columns idx of a make_columns dict (km trimmed to the deepest column)."""
     out = dict(cols)
     out["ncol"] = len(idx)
-    for k in ("pe", "he", "te", "rh", "albedo"):
-        out[k] = np.asfortranarray(cols[k][..., idx]) if k != "albedo" else np.asfortranarray(cols[k][idx, :])
+    for k in ("pe", "he", "te", "rh"):
+        out[k] = np.asfortranarray(cols[k][..., idx])
+    out["albedo"] = np.asfortranarray(cols["albedo"][idx, :])
     out["qm"] = np.asfortranarray(cols["qm"][:, :, idx])
     out["ROT"] = np.asfortranarray(cols["ROT"][:, idx, :])
     for k in ("sza", "vza", "raa", "nlayers", "nstreams"):
@@ -77,10 +90,9 @@ def subset(cols, idx):
 
 
 def alg_flops(N, L, nfourier, K=None):
-    """Reference-algorithm FP64 flops of one (column, wavelength) solve
-    (banded-LU formulation of the reference), summed over the Fourier terms
-    the solve executed: for m = 0..M, with n = 2NL, kl = ku = 3N - 1,
-    K_m = NMOMENTS - m + 1:
+    """Reference-algorithm flops of one (column, wavelength) solve (banded-LU
+    formulation of the reference), summed over the Fourier terms the solve
+    executed: for m = 0..M, with n = 2NL, kl = ku = 3N - 1, K_m = NMOMENTS - m + 1:
       L(4N^2 K_m + 2N K_m + 2N^3) + 10 L N^3 + L(6N^2 + 20N)
       + 2n kl (kl+ku) + 2n (2kl+ku) + 10 L N,  plus FO: L(2K + 60)."""
     NM = 2 * N - 1
@@ -147,19 +159,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def fp64_peak(torch, lib, stream):
-    """Measured FP64 rates: the DFMA pipe (probe kernel) and cuBLAS DGEMM."""
-    out = torch.zeros(1, dtype=torch.float64, device="cuda")
-    blocks, threads, iters = 152 * 16, 256, 4096
-    lib.aerort_probe_dfma(blocks, threads, 64, out.data_ptr(), stream)
+def pipe_peaks(torch, lib, stream):
+    """Measured FP64 and FP32 FMA pipe rates (probe kernels, TFLOP/s) and cuBLAS DGEMM."""
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = 0.0
-    for _ in range(3):
-        s.record()
-        lib.aerort_probe_dfma(blocks, threads, iters, out.data_ptr(), stream)
-        e.record()
-        torch.cuda.synchronize()
-        best = max(best, blocks * threads * iters * 16.0 / (s.elapsed_time(e) * 1e-3))
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    blocks, threads = 152 * 16, 256
+
+    def rate(fn, iters):
+        fn(blocks, threads, 64, out.data_ptr(), stream)
+        best = 0.0
+        for _ in range(3):
+            s.record()
+            fn(blocks, threads, iters, out.data_ptr(), stream)
+            e.record()
+            torch.cuda.synchronize()
+            best = max(best, blocks * threads * iters * 16.0 / (s.elapsed_time(e) * 1e-3))
+        return best / 1e12
+    fp64 = rate(lib.aerort_probe_dfma, 4096)
+    fp32 = rate(lib.aerort_probe_ffma, 65536)
     a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
     b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
     torch.matmul(a, b)
@@ -170,23 +187,26 @@ def fp64_peak(torch, lib, stream):
         e.record()
         torch.cuda.synchronize()
         dg = max(dg, 2.0 * 4096 ** 3 / (s.elapsed_time(e) * 1e-3))
-    return best / 1e12, dg / 1e12
+    return fp64, fp32, dg / 1e12
 
 
-def cpu_baseline(batch, ncols_sample):
-    """The oracle (C++ restatement, OpenMP over all host cores) on the first columns of the batch."""
-    from oracle import oracle
-    import numpy as np
-    sub = subset(batch, np.arange(ncols_sample))
-    cores = os.cpu_count() or 1
-    from aeroapps_gb300 import mie
-    tabs = mie.generate_tables(list(CHANNELS), nmom=32)
-    names = __import__("aeroapps_gb300.synth", fromlist=["x"]).tracer_names()
+def table_index(tabs):
     qidx = {}
     for ti, t in enumerate(tabs.tables):
         for b in range(t.bext.shape[2]):
             qidx["%s%03d" % (t.name, b + 1)] = (ti, b)
-    qt, qb = zip(*[qidx[n] for n in names])
+    return qidx
+
+
+def cpu_baseline(batch, ncols_sample):
+    """The oracle (C++ restatement of the reference path, OpenMP over all host cores) on the first columns."""
+    from oracle import oracle
+    from aeroapps_gb300 import mie, synth
+    sub = subset(batch, np.arange(ncols_sample))
+    cores = os.cpu_count() or 1
+    tabs = mie.generate_tables(list(CHANNELS), nmom=32)
+    qidx = table_index(tabs)
+    qt, qb = zip(*[qidx[n] for n in synth.tracer_names()])
     t0 = time.perf_counter()
     nsolve = 0
     for N in STREAMS:
@@ -197,24 +217,24 @@ def cpu_baseline(batch, ncols_sample):
         km, n, nch = g["km"], g["ncol"], len(CHANNELS)
         tau, ssa, gg, pm, rc = oracle.get_aop_vector(tabs, km, n, nch, 20, np.float32(CHANNELS), qt, qb, g["qm"],
                                                      g["rh"], 2 * N, 1)
-        rad, refl, rc2, nf, st = oracle.scalar_lambert(km, nch, n, np.array(CHANNELS), N, 0, 2 * N, 1, g["ROT"],
-                                                       g["depol"], tau, ssa, gg, pm, g["pe"], g["he"], g["te"],
-                                                       g["albedo"], g["sza"], g["raa"], g["vza"], -1.0e15,
-                                                       nlay=g["nlayers"])
+        oracle.scalar_lambert(km, nch, n, np.array(CHANNELS), N, 0, 2 * N, 1, g["ROT"], g["depol"], tau, ssa, gg, pm,
+                              g["pe"], g["he"], g["te"], g["albedo"], g["sza"], g["raa"], g["vza"], -1.0e15,
+                              nlay=g["nlayers"])
         nsolve += n * nch
     dt = time.perf_counter() - t0
     return {"value": nsolve / dt, "unit": "radiances/s", "cores": cores, "kind": "port",
-            "sample": "%d columns x %d wavelengths of the same batch (mixed 4-16 streams, 20-72 layers), C++ oracle "
-                      "restating VLIDORT 2.8.3 + Chem_MieQuery, OpenMP over pixels; %.1f s" % (ncols_sample, len(CHANNELS), dt)}
+            "sample": "%d columns x %d wavelengths of the same batch (4-16 streams, 20-72 layers): C++ oracle restating "
+                      "VLIDORT 2.8.3 + Chem_MieQuery (FP64), OpenMP over pixels, %d host threads; %.1f s"
+                      % (ncols_sample, len(CHANNELS), cores, dt)}
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    batch = make_batch(max(args.cpu_cols or 96, 8), seed=20261204)
-    times = []
+    batch = make_batch(max(args.cpu_cols or 64, 8), seed=20261204)
     ncols = batch["ncol"]
+    times = []
     for i in range(args.warmup + args.steps):
         r = cpu_baseline(batch, ncols)
         if i >= args.warmup:
@@ -223,11 +243,11 @@ def run_reference(args):
     line = {"metric": METRIC, "value": v, "unit": "radiances/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": "batching FP64: 262,144 columns, 20-72 layers, streams {4,6,8,12,16}, 4 wavelengths",
-                       "columns_per_step": ncols, "wavelengths": list(CHANNELS)},
+            "config": {"workload": WORKLOAD, "columns_per_step": ncols, "wavelengths": list(CHANNELS)},
             "cpu_baseline": {"value": v, "unit": "radiances/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": "%d columns x 4 wavelengths per step; the reference (Fortran) cannot be built "
-                                       "here (no Fortran compiler), so its C++ restatement runs" % ncols},
+                             "sample": "%d columns x 4 wavelengths per step; the reference Fortran cannot be built "
+                                       "here or on the GPU host (no Fortran compiler), so its C++ restatement runs "
+                                       "(FP64, OpenMP over pixels)" % ncols},
             "e2e": {"value": v, "unit": "radiances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -242,12 +262,14 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    from aeroapps_gb300 import _lib, mie
+    from aeroapps_gb300 import _lib, autotune, mie, synth
     L = _lib.lib()
     stream = torch.cuda.current_stream().cuda_stream
+    dev_name = torch.cuda.get_device_name(local)
+    autotune.apply_cached(dev_name)
     tabs = mie.generate_tables(list(CHANNELS), nmom=32)
     chem = mie.ChemMie(tabs)
-    names = __import__("aeroapps_gb300.synth", fromlist=["x"]).tracer_names()
+    names = synth.tracer_names()
     qt = np.array([chem.query_idx(n)[0] for n in names], np.int32)
     qb = np.array([chem.query_idx(n)[1] for n in names], np.int32)
     ch32 = np.array(CHANNELS, np.float32)
@@ -262,56 +284,69 @@ def main():
         idx = idx[np.argsort(-batch["nlayers"][idx], kind="stable")]  # similar layer counts share a warp
         g = subset(batch, idx)
         km, n = g["km"], g["ncol"]
-        nmom = 2 * N
-        d = {"N": N, "km": km, "n": n, "nmom": nmom, "host": g,
+        d = {"N": N, "km": km, "n": n, "nmom": 2 * N, "host": g,
              "qm": dev(g["qm"], np.float32), "rh": dev(g["rh"], np.float32), "ROT": dev(g["ROT"], np.float64),
              "depol": dev(g["depol"], np.float64), "he": dev(g["he"], np.float64),
              "albedo": dev(g["albedo"], np.float64), "sza": dev(g["sza"], np.float64),
-             "raa": dev(g["raa"], np.float64), "vza": dev(g["vza"], np.float64),
-             "nlay": dev(g["nlayers"], np.int32)}
+             "raa": dev(g["raa"], np.float64), "vza": dev(g["vza"], np.float64), "nlay": dev(g["nlayers"], np.int32)}
         d["tau"] = torch.zeros(km * nch * n, dtype=torch.float32, device="cuda")
         d["ssa"] = torch.zeros_like(d["tau"])
         d["g"] = torch.zeros_like(d["tau"])
-        d["pmom"] = torch.zeros(km * nch * n * nmom, dtype=torch.float32, device="cuda")
-        d["rad"] = torch.zeros(n * nch, dtype=torch.float64, device="cuda")
-        d["refl"] = torch.zeros_like(d["rad"])
-        d["nf"] = torch.zeros(n * nch, dtype=torch.int32, device="cuda")
-        d["st"] = torch.zeros_like(d["nf"])
+        d["pmom"] = torch.zeros(km * nch * n * 2 * N, dtype=torch.float32, device="cuda")
+        for p in ("m", "d"):
+            d["rad" + p] = torch.zeros(n * nch, dtype=torch.float64, device="cuda")
+            d["refl" + p] = torch.zeros_like(d["rad" + p])
+            d["nf" + p] = torch.zeros(n * nch, dtype=torch.int32, device="cuda")
+            d["st" + p] = torch.zeros_like(d["nf" + p])
         groups.append(d)
     P = lambda t: t.data_ptr()
     ev = lambda: torch.cuda.Event(enable_timing=True)
-    rt_events = []
 
-    def step(record=False):
+    def run_group(d, prec):
+        p = "m" if prec == _lib.PREC_MIXED else "d"
+        fn = (L.aerort_vlidort_scalar_lambert_mixed_batch_dev if prec == _lib.PREC_MIXED
+              else L.aerort_vlidort_scalar_lambert_batch_dev)
+        rc = fn(d["km"], nch, d["n"], d["N"], 0, d["nmom"], P(d["nlay"]), P(d["ROT"]), P(d["depol"]), None, None, None,
+                P(d["tau"]), P(d["ssa"]), P(d["pmom"]), P(d["he"]), P(d["albedo"]), P(d["sza"]), P(d["raa"]),
+                P(d["vza"]), -1.0e15, P(d["rad" + p]), P(d["refl" + p]), P(d["nf" + p]), P(d["st" + p]), stream)
+        assert rc == 0, _lib.last_error()
+
+    def step(prec, rt_events=None):
         for d in groups:
             rc = L.aerort_get_aop_vector_dev(chem.handle, d["km"], d["n"], nch, 20, _lib.ptr(ch32, _lib.P_f),
                                              _lib.ptr(qt, _lib.P_i), _lib.ptr(qb, _lib.P_i), P(d["qm"]), P(d["rh"]),
                                              d["nmom"], 1, P(d["tau"]), P(d["ssa"]), P(d["g"]), P(d["pmom"]), stream)
             assert rc == 0, _lib.last_error()
-            if record:
+            if rt_events is not None:
                 e0, e1 = ev(), ev()
                 e0.record()
-            rc = L.aerort_vlidort_scalar_lambert_batch_dev(
-                d["km"], nch, d["n"], d["N"], 0, d["nmom"], P(d["nlay"]), P(d["ROT"]), P(d["depol"]), None, None,
-                None, P(d["tau"]), P(d["ssa"]), P(d["pmom"]), P(d["he"]), P(d["albedo"]), P(d["sza"]), P(d["raa"]),
-                P(d["vza"]), -1.0e15, P(d["rad"]), P(d["refl"]), P(d["nf"]), P(d["st"]), stream)
-            assert rc == 0, _lib.last_error()
-            if record:
+            run_group(d, prec)
+            if rt_events is not None:
                 e1.record()
                 rt_events.append((d["N"], e0, e1))
 
+    tuned = {}
+    if args.tune:
+        for d in groups:
+            for prec in (_lib.PREC_MIXED, _lib.PREC_FP64):
+                r = autotune.tune(lambda: run_group(d, prec), d["N"], prec, dev_name,
+                                  budget_s=20.0 if prec == _lib.PREC_MIXED else 40.0)
+                tuned["%s N%d" % ("mixed" if prec else "fp64", d["N"])] = (r["threads"], r["blocks_per_sm"])
+
+    # ---------------------------------------------------------------- mixed (headline)
     for _ in range(args.warmup):
-        step()
+        step(_lib.PREC_MIXED)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     clocks = ClockSampler(local)
     clocks.start()
     t0, t1 = ev(), ev()
+    rt_m = []
     torch.cuda.synchronize()
     t0.record()
     for _ in range(args.steps):
-        step(record=True)
+        step(_lib.PREC_MIXED, rt_m)
     t1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -322,28 +357,54 @@ def main():
         ms = float(tt.item())
     solves = args.cols * nch
     value = solves * world / (ms * 1e-3)
-    # per-kernel time of the RT launches and their algorithmic flops
-    rt_ms = sum(e0.elapsed_time(e1) for (_, e0, e1) in rt_events) / args.steps
-    flops = 0.0
-    status_bad = 0
+    rt_ms_m = sum(e0.elapsed_time(e1) for (_, e0, e1) in rt_m) / args.steps
+
+    # ---------------------------------------------------------------- plain FP64 on the same batch
+    step(_lib.PREC_FP64)
+    torch.cuda.synchronize()
+    rt_d = []
+    p0, p1 = ev(), ev()
+    p0.record()
+    for _ in range(args.plain_steps):
+        step(_lib.PREC_FP64, rt_d)
+    p1.record()
+    torch.cuda.synchronize()
+    ms_plain = p0.elapsed_time(p1) / args.plain_steps
+    rt_ms_d = sum(e0.elapsed_time(e1) for (_, e0, e1) in rt_d) / args.plain_steps
+    plain_value = solves * world / (ms_plain * 1e-3)
+
+    # ---------------------------------------------------------------- accuracy of mixed vs FP64, flops
+    errs, bad, flops = [], 0, 0.0
     for d in groups:
-        nf = d["nf"].cpu().numpy().reshape(d["n"], nch, order="F")
-        st = d["st"].cpu().numpy()
-        status_bad += int((st != 0).sum())
+        rm, rd = d["radm"].cpu().numpy(), d["radd"].cpu().numpy()
+        stm, std_ = d["stm"].cpu().numpy(), d["std"].cpu().numpy()
+        bad += int((stm != 0).sum() + (std_ != 0).sum())
+        ok = (rd != -1.0e15) & (stm == 0) & (std_ == 0)
+        errs.append(np.abs(rm[ok] / rd[ok] - 1.0))
+        nf = d["nfd"].cpu().numpy().reshape(d["n"], nch, order="F")
         nl = d["host"]["nlayers"]
         for j in range(d["n"]):
             for i in range(nch):
                 flops += alg_flops(d["N"], int(nl[j]), int(nf[j, i]))
-    fp64_probe, dgemm = fp64_peak(torch, L, stream)
-    achieved = flops / (rt_ms * 1e-3) / 1e12
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": fp64_probe, "unit": "TFLOP/s",
-                "frac": achieved / fp64_probe, "traffic": None,
-                "peak_source": "measured live: DFMA issue-rate probe (8 FMA chains/thread); cuBLAS DGEMM %.3f TFLOP/s" % dgemm,
-                "note": "achieved counts the reference algorithm's flops (banded LU BVP, nonsymmetric eigen-solve); "
-                        "the kernel executes fewer (block BVP sweep, symmetric eigen-reduction), so frac can exceed 1",
-                "kernel": "k_scalar_lambert<NS> (all stream counts)", "kernel_ms_per_step": rt_ms}
-    # end to end through the host-pointer C ABI (reference-facing drop-in): inputs from host memory,
-    # copies inside the timed region, FP32 optics returned to the host and widened like dble()
+    err = np.concatenate(errs)
+    fp64_peak, fp32_peak, dgemm = pipe_peaks(torch, L, stream)
+    ach_m = flops / (rt_ms_m * 1e-3) / 1e12
+    ach_d = flops / (rt_ms_d * 1e-3) / 1e12
+    roofline = {"bound": "fp32", "achieved": ach_m, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach_m / fp32_peak,
+                "traffic": None, "kernel": "k_scalar_lambert<NS, float> (mixed; all stream counts)",
+                "kernel_ms_per_step": rt_ms_m,
+                "peak_source": "measured live: FFMA issue-rate probe (8 FMA chains/thread), of measured",
+                "note": "achieved = reference-algorithm flops (banded-LU BVP, nonsymmetric eigen-solve) of the solves "
+                        "/ kernel time; the kernel executes a different, mostly FP32 operation mix"}
+    roofline_plain = {"bound": "fp64", "achieved": ach_d, "peak": fp64_peak, "unit": "TFLOP/s",
+                      "frac": ach_d / fp64_peak, "kernel": "k_scalar_lambert<NS, double> (plain FP64)",
+                      "kernel_ms_per_step": rt_ms_d,
+                      "peak_source": "measured live: DFMA issue-rate probe, of measured; cuBLAS DGEMM %.3f TFLOP/s"
+                                     % dgemm,
+                      "note": "reference-algorithm flops; the kernel executes fewer (block BVP sweep, symmetric "
+                              "eigen-reduction), so frac can exceed 1"}
+
+    # ---------------------------------------------------------------- end to end through the host C ABI
     from aeroapps_gb300 import vlidort
     e2e_val, h2d, d2h = None, 0, 0
     if args.e2e_steps > 0:
@@ -351,17 +412,17 @@ def main():
             nbi = nbo = 0
             for d in groups:
                 g = d["host"]
-                tau, ssa, gg, pm, rc = mie.get_aop_vector(chem, d["km"], d["n"], nch, 20, ch32, names, 0, g["qm"], g["rh"],
-                                                          d["nmom"], 1)
+                tau, ssa, gg, pm, rc = mie.get_aop_vector(chem, d["km"], d["n"], nch, 20, ch32, names, 0, g["qm"],
+                                                          g["rh"], d["nmom"], 1)
                 nbi += g["qm"].nbytes + g["rh"].nbytes
                 nbo += tau.nbytes * 3 + pm.nbytes
                 rad, refl, rc2, _, _ = vlidort.vlidort_scalar_lambert_batch(
                     d["km"], nch, d["n"], d["N"], d["nmom"], g["nlayers"], g["ROT"], g["depol"],
                     tau.astype(np.float64), ssa.astype(np.float64), pm[..., 0].astype(np.float64), g["he"],
-                    g["albedo"], g["sza"], g["raa"], g["vza"])
-                nbi += (g["ROT"].nbytes + 8 * (3 * tau.size + pm.size) + g["he"].nbytes + g["albedo"].nbytes +
-                        3 * g["sza"].nbytes + 8 * nch)
-                nbo += rad.nbytes + refl.nbytes
+                    g["albedo"], g["sza"], g["raa"], g["vza"], precision="mixed")
+                nbi += (g["ROT"].nbytes + 8 * (2 * tau.size + pm[..., 0].size) + g["he"].nbytes + g["albedo"].nbytes
+                        + 3 * g["sza"].nbytes + 8 * nch + 4 * d["n"])
+                nbo += rad.nbytes + refl.nbytes + 8 * rad.size
             return nbi, nbo
         e2e_step()
         torch.cuda.synchronize()
@@ -370,25 +431,62 @@ def main():
             h2d, d2h = e2e_step()
         torch.cuda.synchronize()
         e2e_val = solves / ((time.perf_counter() - t) / args.e2e_steps)
+
+    # ---------------------------------------------------------------- serving
+    serving = None
+    if not args.no_serve and rank == 0 and args.serve_requests > 0:
+        from aeroapps_gb300 import serve
+        rng = np.random.default_rng(4)
+        sizes = np.exp(rng.uniform(np.log(64), np.log(args.serve_max_cols), args.serve_requests)).astype(int)
+        nchs = rng.integers(1, 5, args.serve_requests)
+        mk = lambda: [serve.make_swath(i, int(sizes[i]), list(CHANNELS[: nchs[i]]), seed=5000 + i)
+                      for i in range(args.serve_requests)]
+        srv = serve.Server(tabs, nslots=4, precision="mixed", hbm_budget_gb=120.0)
+        warm = serve.make_swath(999, 64, list(CHANNELS), seed=1)
+        srv.submit(warm)
+        srv.drain()
+        srv.done.clear()
+        sw = mk()
+        done, wall = serve.run_poisson(srv, sw, args.serve_rate, seed=9)
+        stats = serve.latency_stats(done)
+        rads = sum(s.radiances for s in done)
+        # the same mix as one offline batch (all submitted at once)
+        sw2 = mk()
+        srv.done.clear()
+        t = time.perf_counter()
+        for s in sw2:
+            srv.submit(s)
+        srv.drain()
+        offline = sum(s.radiances for s in sw2) / (time.perf_counter() - t)
+        srv.close()
+        serving = dict(stats)
+        serving.update({"arrival_rate_per_s": args.serve_rate, "sustained_radiances_per_s": rads / wall,
+                        "offline_batch_radiances_per_s": offline, "slots": 4, "precision": "mixed",
+                        "swath_columns": "log-uniform %d..%d" % (64, args.serve_max_cols),
+                        "wavelengths_per_request": "1-4", "hbm_budget_gb": 120.0})
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(batch, args.cpu_cols or 64)
-    launches_per_step = sum(4 for _ in groups)  # aop, scheduler init, nadir flag, RT solve per stream group
+        cpu = cpu_baseline(batch, args.cpu_cols or 32)
+    # AOP + scheduler init + nadir flag + RT per stream group and step, both timed passes
+    launches = 4 * len(groups) * (args.steps + args.plain_steps)
     line = {
         "metric": METRIC, "value": value, "unit": "radiances/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "batching FP64: columns of the 262,144-column config, 20-72 layers, streams "
-                               "{4,6,8,12,16} (moments 2x streams), 4 wavelengths; one step = %d columns x 4 wavelengths "
-                               "per GPU" % args.cols,
+        "dtype": "f32+f64 (mixed: FP64 set-up and single scatter, FP32 Fourier series)", "data": "synthetic",
+        "config": {"workload": WORKLOAD + "; one step = %d columns x 4 wavelengths per GPU" % args.cols,
                    "columns_per_step": args.cols, "solves_per_step": solves, "wavelengths": list(CHANNELS),
-                   "l2": "working set > L2 (inputs + optics + scratch of a step are hundreds of MB)",
-                   "failed_solves": status_bad},
-        "roofline": roofline, "cpu_baseline": cpu,
+                   "l2": "inputs larger than L2 (optics + scratch of a step: hundreds of MB)",
+                   "failed_solves": bad, "tuned_schedules": tuned or None},
+        "accuracy": {"max_rel_err_vs_fp64": float(err.max()), "median_rel_err_vs_fp64": float(np.median(err)),
+                     "radiances_compared": int(err.size), "bar": 1e-4},
+        "plain_fp64": {"value": plain_value, "unit": "radiances/s", "ms_per_step": ms_plain,
+                       "steps": args.plain_steps, "mixed_over_plain": value / plain_value},
+        "roofline": roofline, "roofline_plain": roofline_plain, "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "radiances/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "host-pointer C ABI: aerort_get_aop_vector + aerort_vlidort_scalar_lambert_batch per stream "
-                        "group (FP32 optics widened to FP64 on the host as the reference driver does)"},
-        "gpu_launches": launches_per_step * args.steps, "clocks": clk,
+                "path": "host-pointer C ABI: aerort_get_aop_vector + aerort_vlidort_scalar_lambert_mixed_batch per "
+                        "stream group (FP32 optics widened to FP64 on the host as the reference driver does)"},
+        "serving": serving, "gpu_launches": launches, "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line))

@@ -13,6 +13,8 @@
 #ifndef AERORT_H
 #define AERORT_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -164,6 +166,29 @@ int aerort_vlidort_scalar_lambert_mixed_batch(int km, int nch, int nobs, int nst
                                               double MISSING, double* radiance_VL, double* reflectance_VL,
                                               int* nfourier, int* status);
 
+/* Caller-owned RT workspace (device scratch for one launch at a time).  No
+ * counterpart in the reference.  aerort_workspace_create allocates `bytes` of
+ * device memory once; launches through aerort_vlidort_scalar_lambert_ws_dev
+ * then allocate nothing, and launches on different workspaces may overlap on
+ * different streams (the batched entry points above share one library
+ * scratch and are serialised).  The grid is capped to the threads whose
+ * scratch fits: bytes_per_thread(km, nstreams, precision) x threads; one
+ * block (32-128 threads) must fit.  The precision argument selects
+ * AERORT_PREC_FP64 or AERORT_PREC_MIXED; the other arguments are those of
+ * aerort_vlidort_scalar_lambert_batch_dev. */
+typedef struct aerort_workspace aerort_workspace;
+int aerort_workspace_create(size_t bytes, aerort_workspace** ws);
+int aerort_workspace_destroy(aerort_workspace* ws);
+long aerort_workspace_bytes_per_thread(int km, int nstreams, int precision);
+int aerort_vlidort_scalar_lambert_ws_dev(aerort_workspace* ws, int precision, int km, int nch, int nobs, int nstreams,
+                                         int plane_parallel, int nMom, const int* nlay, const double* ROT,
+                                         const double* depol, const double* tau, const double* ssa,
+                                         const double* pmom, const float* tau_f, const float* ssa_f,
+                                         const float* pmom_f, const double* he, const double* albedo,
+                                         const double* solar_zenith, const double* relat_azymuth,
+                                         const double* sensor_zenith, double MISSING, double* radiance_VL,
+                                         double* reflectance_VL, int* nfourier, int* status, void* stream);
+
 /* Launch schedule of the RT kernel per (stream count, precision): threads per
  * block (32, 64, 96 or 128) and resident blocks per SM (0 = occupancy limit).
  * Set by the autotuner (aeroapps_gb300/autotune.py); no counterpart in the
@@ -212,6 +237,8 @@ int aerort_vlidort_scalar_lambert_batch(int km, int nch, int nobs, int nstreams,
  * threads each running 8 independent FP64 FMA chains for `iters` rounds
  * (16 * iters flops per thread); timing it gives the FP64 pipe rate. */
 int aerort_probe_dfma(int blocks, int threads, int iters, double* out_dev, void* stream);
+/* Same with FP32 FMA chains (the FP32 pipe rate that bounds the mixed solve). */
+int aerort_probe_ffma(int blocks, int threads, int iters, float* out_dev, void* stream);
 
 const char* aerort_last_error(void);  /* last error message of the calling thread */
 int aerort_version(void);             /* 100 * major + minor */
