@@ -54,6 +54,8 @@ _SIGNATURES = {
     "aerort_vlidort_scalar_lambert_ws_dev": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int] +
                                              [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
     "aerort_get_schedule": (c_int, [c_int, c_int, P_i, P_i]),
+    "aerort_set_kernel": (c_int, [c_int, c_int, c_int]),
+    "aerort_get_kernel": (c_int, [c_int, c_int]),
     "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_probe_ffma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_last_error": (ctypes.c_char_p, []),
@@ -66,6 +68,8 @@ _SIGNATURES = {
 
 PREC_FP64 = 0
 PREC_MIXED = 1
+KERNEL_THREAD = 0
+KERNEL_TEAM = 1
 
 
 def library_path():

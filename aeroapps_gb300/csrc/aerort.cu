@@ -431,6 +431,16 @@ RtOptions lambert_options(int plane_parallel) {
 template <typename T>
 int dispatch_lambert_t(Context& c, int nstreams, const RtOptions& opt, const LambertInputs& in, double* rad,
                        double* refl, int* nf, int* st, cudaStream_t s) {
+  const int si = stream_index(nstreams);
+  if (si >= 0 && c.sched[sizeof(T) == sizeof(float) ? 1 : 0][si].kernel == 1) {
+    switch (nstreams) {
+      case 4: return launch_scalar_lambert_team<4, T>(c, opt, in, rad, refl, nf, st, s);
+      case 6: return launch_scalar_lambert_team<6, T>(c, opt, in, rad, refl, nf, st, s);
+      case 8: return launch_scalar_lambert_team<8, T>(c, opt, in, rad, refl, nf, st, s);
+      case 12: return launch_scalar_lambert_team<12, T>(c, opt, in, rad, refl, nf, st, s);
+      case 16: return launch_scalar_lambert_team<16, T>(c, opt, in, rad, refl, nf, st, s);
+    }
+  }
   switch (nstreams) {
     case 4: return launch_scalar_lambert<4, T>(c, opt, in, rad, refl, nf, st, s);
     case 6: return launch_scalar_lambert<6, T>(c, opt, in, rad, refl, nf, st, s);
@@ -528,6 +538,27 @@ extern "C" int aerort_set_schedule(int nstreams, int precision, int threads_per_
   c.sched[precision][si].threads = threads_per_block;
   c.sched[precision][si].blocks_per_sm = blocks_per_sm;
   return AERORT_OK;
+}
+
+extern "C" int aerort_set_kernel(int nstreams, int precision, int kernel) {
+  const int si = stream_index(nstreams);
+  if (si < 0) return set_error(AERORT_RC_UNSUPPORTED, "set_kernel: nstreams must be one of 4, 6, 8, 12, 16");
+  if ((precision != AERORT_PREC_FP64 && precision != AERORT_PREC_MIXED) ||
+      (kernel != AERORT_KERNEL_THREAD && kernel != AERORT_KERNEL_TEAM))
+    return set_error(AERORT_RC_ARG, "set_kernel: bad precision or kernel");
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lk(c.mu);
+  c.sched[precision][si].kernel = kernel;
+  return AERORT_OK;
+}
+
+extern "C" int aerort_get_kernel(int nstreams, int precision) {
+  const int si = stream_index(nstreams);
+  if (si < 0 || (precision != AERORT_PREC_FP64 && precision != AERORT_PREC_MIXED))
+    return set_error(AERORT_RC_ARG, "get_kernel: bad argument") * -1;
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lk(c.mu);
+  return c.sched[precision][si].kernel;
 }
 
 extern "C" int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int* blocks_per_sm) {

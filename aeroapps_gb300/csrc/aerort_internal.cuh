@@ -32,9 +32,12 @@ struct DevBuf {
 // Launch schedule of the RT kernel for one (precision, stream count):
 // threads per block (a multiple of 32, <= 128) and resident blocks per SM
 // (0 = as many as the occupancy calculator allows).
+// kernel: 0 = thread per solve, 1 = team (one warp per solve for the Fourier
+// series, rt_team.cuh).
 struct Schedule {
   int threads = 64;
   int blocks_per_sm = 0;
+  int kernel = 0;
 };
 int stream_index(int nstreams);  // 0..4 for 4, 6, 8, 12, 16; -1 otherwise
 
@@ -47,6 +50,9 @@ struct Context {
   cudaStream_t stream = nullptr;
   DevBuf scratch, counter, stage[24];
   Schedule sched[2][5];  // [precision][stream index]
+  Context() {
+    for (auto& p : sched) { p[3].kernel = 1; p[4].kernel = 1; }  // team kernel for 12 and 16 streams
+  }
   int setup();
   void release();
 };
@@ -64,6 +70,9 @@ template <int NS, typename T>
 int launch_scalar_lambert(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
                           double* refl, int* nf, int* st, cudaStream_t s);
 
+template <int NS, typename T>
+int launch_scalar_lambert_team(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
+                               double* refl, int* nf, int* st, cudaStream_t s);
 template <int NS, typename T>
 int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::LambertInputs& in, void* arena,
                                 size_t arena_bytes, int* sched, int num_sms, const Schedule& sc, double* rad,

@@ -2,6 +2,7 @@
 // rt_ns{4,6,8,12,16}.cu so the instantiations compile in parallel.
 #pragma once
 #include "aerort_internal.cuh"
+#include "rt_team.cuh"
 
 namespace aerort_internal {
 using namespace aerort;
@@ -30,6 +31,93 @@ __global__ void __launch_bounds__(128) k_scalar_lambert(RtOptions opt, LambertIn
     if (s < nsolve) solve_lambert<NS, T>(opt, in, s, q.qx, q.qw, q.tu, q.wu, S, rad, refl, nf, st);
     __syncwarp();
   }
+}
+
+// Team kernel: each warp takes 32 solves, runs their set-up thread per solve,
+// then runs their Fourier series one after another as a team (rt_team.cuh).
+// WPB warps per block, one TeamMem per warp in dynamic shared memory.
+template <int NS, typename T, int WPB>
+__global__ void __launch_bounds__(32 * WPB) k_scalar_lambert_team(RtOptions opt, LambertInputs in, Quad q,
+                                                                   void* scratch, long nthreads, T* sweep,
+                                                                   long sweep_per_warp, int nsolve, int* counter,
+                                                                   double* rad, double* refl, int* nf, int* st) {
+  extern __shared__ __align__(16) unsigned char team_smem[];
+  const int lane = threadIdx.x & 31;
+  TeamMem<NS, T>& M = reinterpret_cast<TeamMem<NS, T>*>(team_smem)[threadIdx.x >> 5];
+  const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long tid0 = tid - lane;
+  T* sw = sweep + (tid >> 5) * sweep_per_warp;
+  const ScratchLayout<NS> lay(in.km, false);
+  const SolveScratch<T> S = make_scratch<NS, T>(scratch, tid, nthreads, in.km, false);
+  const Team tm{lane, nullptr, nullptr};
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(counter, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= nsolve) break;
+    const int s = base + lane;
+    bool live = false;
+    if (s < nsolve) {
+      SetupRecord r;
+      live = solve_setup<NS, T>(opt, in, s, q.tu, q.wu, S, rad, refl, nf, st, r);
+      if (live) r.store(S.D, lay.rec);
+    }
+    unsigned mask = __ballot_sync(0xffffffffu, live);
+    __syncwarp();
+    while (mask) {
+      const int b = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const SolveScratch<T> Sb = make_scratch<NS, T>(scratch, tid0 + b, nthreads, in.km, false);
+      SetupRecord rb;
+      rb.load(Sb.D, lay.rec);
+      team_fourier_series<NS, T>(tm, M, opt, in, rb, q.qx, q.qw, Sb.W, lay, sw, rad, refl, nf, st);
+    }
+  }
+}
+
+template <int NS, typename T>
+int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
+                               int* nf, int* st, cudaStream_t s) {
+  constexpr int WPB = 2;
+  const int nsolve = in.nobs * in.nch;
+  if (nsolve == 0) return 0;
+  Quad q;
+  std::memset(&q, 0, sizeof(q));
+  gauss_legendre01(NS, q.qx, q.qw);
+  if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
+  const int bs = 32 * WPB;
+  const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
+  CUDA_TRY(cudaFuncSetAttribute(k_scalar_lambert_team<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+  int per_sm = 0;
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert_team<NS, T, WPB>, bs, smem));
+  if (per_sm < 1) return set_error(AERORT_RC_CUDA, "team kernel does not fit on an SM");
+  const Schedule& sc = c.sched[sizeof(T) == sizeof(float) ? 1 : 0][stream_index(NS)];
+  if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
+  long nblocks = (nsolve + bs - 1) / bs;
+  if (nblocks > (long)per_sm * c.num_sms) nblocks = (long)per_sm * c.num_sms;
+  const long nthreads = nblocks * bs;
+  const ScratchLayout<NS> lay(in.km, false);
+  const SweepLayout<NS> swl(in.km);
+  const size_t thread_bytes = (size_t)lay.template bytes<T>() * nthreads;
+  const size_t sweep_off = (thread_bytes + 255) / 256 * 256;
+  const size_t sweep_bytes = sizeof(T) * (size_t)swl.total * (nthreads / 32);
+  if (int rc = c.scratch.ensure(sweep_off + sweep_bytes)) return rc;
+  if (int rc = c.counter.ensure(2 * sizeof(int))) return rc;
+  int* counter = (int*)c.counter.p;
+  int* first = counter + 1;
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+  k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
+                                                       first);
+  CUDA_TRY(cudaGetLastError());
+  LambertInputs in2 = in;
+  in2.nadir_first = first;
+  T* sweep = (T*)((char*)c.scratch.p + sweep_off);
+  k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(opt, in2, q, c.scratch.p, nthreads, sweep,
+                                                                        swl.total, nsolve, counter, rad, refl, nf,
+                                                                        st);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
 }
 
 template <int NS, typename T>
@@ -116,6 +204,12 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
       int*, cudaStream_t);                                                                                      \
   template int aerort_internal::launch_scalar_lambert<NS, float>(                                              \
+      aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
+      int*, cudaStream_t);                                                                                      \
+  template int aerort_internal::launch_scalar_lambert_team<NS, double>(                                        \
+      aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
+      int*, cudaStream_t);                                                                                      \
+  template int aerort_internal::launch_scalar_lambert_team<NS, float>(                                         \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
       int*, cudaStream_t);                                                                                      \
   template int aerort_internal::launch_scalar_lambert_fixed<NS, double>(                                       \

@@ -47,12 +47,14 @@ struct LambertInputs {
 template <int NS>
 struct ScratchLayout {
   static constexpr int NMX = 2 * NS;  // NMOMENTS + 1 <= 2 NS
-  long hgt, ext, escat, dts, dtau, avsec, itrans, d_total;                              // FP64
+  long hgt, ext, escat, dts, dtau, avsec, itrans, rec, d_total;                         // FP64
   long og, om1, lnz, tdtau, tavsec, titrans, tmubar, tuser, emult, F, f, C, c, a, b, s, t_total;  // working precision
-  RT_HD explicit ScratchLayout(int L) {
+  // sweep = false leaves out F, f, C, c, a, b, s (kept elsewhere by the team kernel)
+  RT_HD explicit ScratchLayout(int L, bool sweep = true) {
     long o = 0;
     hgt = o; o += L + 1; ext = o; o += L; escat = o; o += L; dts = o; o += L;
     dtau = o; o += L; avsec = o; o += L; itrans = o; o += L;
+    rec = o; o += 16;  // SetupRecord
     d_total = o;
     o = 0;
     og = o; o += (long)NMX * L;
@@ -60,9 +62,13 @@ struct ScratchLayout {
     lnz = o; o += L;
     tdtau = o; o += L; tavsec = o; o += L; titrans = o; o += L; tmubar = o; o += L;
     tuser = o; o += L; emult = o; o += L;
-    F = o; o += (long)NS * NS * L; f = o; o += (long)NS * L;
-    C = o; o += (long)NS * NS * L; c = o; o += (long)NS * L;
-    a = o; o += (long)NS * L; b = o; o += (long)NS * L; s = o; o += L;
+    if (sweep) {
+      F = o; o += (long)NS * NS * L; f = o; o += (long)NS * L;
+      C = o; o += (long)NS * NS * L; c = o; o += (long)NS * L;
+      a = o; o += (long)NS * L; b = o; o += (long)NS * L; s = o; o += L;
+    } else {
+      F = f = C = c = a = b = s = -1;
+    }
     t_total = o;
   }
   // bytes of scratch one thread needs with working precision T
@@ -80,8 +86,8 @@ struct SolveScratch {
 };
 
 template <int NS, typename T>
-RT_HD SolveScratch<T> make_scratch(void* buffer, long tid, long nthreads, int km) {
-  const ScratchLayout<NS> lay(km);
+RT_HD SolveScratch<T> make_scratch(void* buffer, long tid, long nthreads, int km, bool sweep = true) {
+  const ScratchLayout<NS> lay(km, sweep);
   double* d = (double*)buffer;
   T* w = (T*)(d + lay.d_total * nthreads);
   return SolveScratch<T>{Scratch{d + tid, nthreads}, ScratchT<T>{w + tid, nthreads}};
@@ -1033,15 +1039,90 @@ RT_HD bool fo_single_scatter_chord(const RtOptions& opt, bool enhanced, int L, d
   return true;
 }
 
-// Full solve of pixel (obs j, channel i) = solve index sidx = j * nch + i in the
-// reference loop order (VLIDORT_LAMBERT.F90:106-165).  Writes radiance,
-// reflectance, last Fourier index and status.  qx/qw: Gauss-Legendre streams on
-// (0,1); tu/wu: unit fine-layer quadrature for the enhanced-PS line of sight.
-// T is the working precision of the Fourier series.
+// What the Fourier series of one solve needs from its set-up, besides the
+// per-layer arrays left in scratch (stored in the FP64 scratch record so that
+// another thread can run the series).
+struct SetupRecord {
+  double ss, db, raa, sza, mu_u, sec_u, cos_sza, albedo, trans_solar_beam;
+  long o;
+  int L, NM, cutoff, n_fouriers;
+  bool msmode, refl_directbeam;
+  RT_HD void store(const Scratch& S, long at) const {
+    double v[16] = {ss, db, raa, sza, mu_u, sec_u, cos_sza, albedo, trans_solar_beam, (double)o, (double)L,
+                    (double)NM, (double)cutoff, (double)n_fouriers, msmode ? 1.0 : 0.0, refl_directbeam ? 1.0 : 0.0};
+    for (int k = 0; k < 16; ++k) S[at + k] = v[k];
+  }
+  RT_HD void load(const Scratch& S, long at) {
+    ss = S[at]; db = S[at + 1]; raa = S[at + 2]; sza = S[at + 3]; mu_u = S[at + 4]; sec_u = S[at + 5];
+    cos_sza = S[at + 6]; albedo = S[at + 7]; trans_solar_beam = S[at + 8]; o = (long)S[at + 9];
+    L = (int)S[at + 10]; NM = (int)S[at + 11]; cutoff = (int)S[at + 12]; n_fouriers = (int)S[at + 13];
+    msmode = S[at + 14] != 0.0; refl_directbeam = S[at + 15] != 0.0;
+  }
+};
+
+// Fourier-series context in the working precision from a set-up record.
 template <int NS, typename T>
-RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sidx, const double* qx,
-                          const double* qw, const double* tu, const double* wu, const SolveScratch<T>& SS,
-                          double* radiance, double* reflectance, int* nfourier, int* status) {
+RT_HD void make_ctx(const SetupRecord& r, const double* qx, const double* qw, SolveCtx<NS, T>& c) {
+  c.L = r.L; c.NM = r.NM; c.cutoff = r.cutoff; c.msmode = r.msmode; c.refl_directbeam = r.refl_directbeam;
+  for (int q = 0; q < NS; ++q) {
+    c.qx[q] = (T)qx[q]; c.qw[q] = (T)qw[q]; c.sqw[q] = (T)sqrt(qw[q]); c.pimm_q[q] = 0;
+  }
+  c.pimm_u = 0; c.pimm_0 = 0;
+  c.mu_u = (T)r.mu_u; c.sec_u = (T)r.sec_u; c.cos_sza = (T)r.cos_sza; c.albedo = (T)r.albedo;
+  c.trans_solar_beam = (T)r.trans_solar_beam;
+}
+
+// Azimuthal Fourier sum with the reference's double convergence test
+// (VLIDORT_CONVERGE_OBSGEO, vlidort_converge.f90:825-1236).  Returns true when
+// the series has converged after term m.
+struct FourierSum {
+  double stokes = 0.0;
+  int testconv = 0;
+  RT_HD bool add(const RtOptions& opt, const SetupRecord& r, int m, double sf) {
+    if (m == 0) {
+      stokes = sf;
+      if (opt.do_focorr) stokes += r.ss + r.db;
+      return false;
+    }
+    double tazm = cos(r.raa * (double)m * kDTR) * sf;
+    double tnew = stokes + tazm;
+    bool conv = (tazm != 0.0) ? (fabs(tazm / tnew) < opt.accuracy) : true;
+    stokes = tnew;
+    if (conv) {
+      ++testconv;
+      if (!opt.do_double_convtest || testconv == 2) return true;
+    } else {
+      testconv = 0;
+    }
+    return false;
+  }
+};
+
+// Outputs of a finished series (status RT_OK) or of a failed term.
+RT_HD void solve_finish(const RtOptions& opt, const LambertInputs& in, const SetupRecord& r, int st, int m,
+                        double stokes, double* radiance, double* reflectance, int* nfourier, int* status) {
+  const long o = r.o;
+  if (st != RT_OK) {
+    radiance[o] = in.missing; reflectance[o] = in.missing;
+    if (status) status[o] = st;
+    if (nfourier) nfourier[o] = m;
+    return;
+  }
+  if (m > r.n_fouriers) m = r.n_fouriers;
+  if (nfourier) nfourier[o] = m;
+  radiance[o] = stokes;
+  reflectance[o] = (kPiSingle * stokes) / (cos(r.sza * kPiSingle / 180.0) * opt.flux_factor);
+}
+
+// Set-up of pixel (obs j, channel i) = solve index sidx = j * nch + i in the
+// reference loop order (VLIDORT_LAMBERT.F90:106-165): layer mixing, delta-M,
+// first-order single scatter, beam attenuation.  Leaves the per-layer inputs of
+// the Fourier series in scratch and fills r.  Returns false when the pixel is
+// finished already (MISSING inputs or a bad layer: outputs written).
+template <int NS, typename T>
+RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, const double* tu, const double* wu,
+                       const SolveScratch<T>& SS, double* radiance, double* reflectance, int* nfourier,
+                       int* status, SetupRecord& r) {
   const Scratch& S = SS.D;
   const ScratchT<T>& W = SS.W;
   const int nch = in.nch, j = sidx / nch, i = sidx % nch;
@@ -1054,23 +1135,21 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
   if (status) status[o] = RT_OK;
   if (is_missing(sza) || is_missing(vza) || is_missing(raa) || is_missing(alb)) {
     radiance[o] = in.missing; reflectance[o] = in.missing;
-    return;
+    return false;
   }
-  SolveCtx<NS, T> c;
-  c.L = L;
-  c.NM = (2 * NS - 1 < ngreek) ? 2 * NS - 1 : ngreek;
-  c.msmode = opt.do_focorr != 0;
-  c.albedo = (T)alb;
-  for (int q = 0; q < NS; ++q) {
-    c.qx[q] = (T)qx[q]; c.qw[q] = (T)qw[q]; c.sqw[q] = (T)sqrt(qw[q]); c.pimm_q[q] = 0;
-  }
-  c.pimm_u = 0; c.pimm_0 = 0;
+  r.o = o;
+  r.L = L;
+  r.NM = (2 * NS - 1 < ngreek) ? 2 * NS - 1 : ngreek;
+  r.msmode = opt.do_focorr != 0;
+  r.albedo = alb;
+  r.raa = raa;
+  r.sza = sza;
   const double mu_u = cos(kDTR * vza), cos_sza = cos(sza * kDTR);
   const double sec_u = 1.0 / mu_u;
-  c.mu_u = (T)mu_u;
-  c.sec_u = (T)sec_u;
-  c.cos_sza = (T)cos_sza;
-  const int NM = c.NM;
+  r.mu_u = mu_u;
+  r.sec_u = sec_u;
+  r.cos_sza = cos_sza;
+  const int NM = r.NM;
   const bool nadir_fo = in.nadir_first ? (j >= *in.nadir_first) : false;
   // scattering angle for the exact single-scatter phase function
   double cosscat;
@@ -1103,7 +1182,7 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
     if (!(tau_ext > 0.0) || !(tau_scat > 0.0)) {
       radiance[o] = in.missing; reflectance[o] = in.missing;
       if (status) status[o] = RT_BAD_INPUT;
-      return;
+      return false;
     }
     double om_in = tau_scat / tau_ext;
     if (om_in > kSsaCap) om_in = kSsaCap;
@@ -1162,6 +1241,7 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
   }
   // ---------------------------------------------------------------- single scatter
   double ss = 0.0, db = 0.0;
+  r.ss = 0.0; r.db = 0.0;
   if (opt.do_focorr) {
     const bool enhanced = !opt.do_plane_parallel && !nadir_fo;
     double phi = raa;
@@ -1233,9 +1313,9 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
         refl_directbeam = ts < kMaxTau;
       }
     }
-    c.cutoff = cutoff;
-    c.trans_solar_beam = (T)trans_solar_beam;
-    c.refl_directbeam = refl_directbeam;
+    r.cutoff = cutoff;
+    r.trans_solar_beam = trans_solar_beam;
+    r.refl_directbeam = refl_directbeam;
     for (int n = 0; n < L; ++n) {
       const double dtn = S[lay.dtau + n];
       double tmu = 0.0, em = 0.0;
@@ -1257,41 +1337,36 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
       W[lay.emult + n] = (T)em;
     }
   }
-  // ---------------------------------------------------------------- Fourier series
-  // vlidort_masters_V2p8p3.f90:2305-2700 with VLIDORT_CONVERGE_OBSGEO (vlidort_converge.f90:825)
-  const int n_fouriers = (vza == 0.0 && !opt.do_focorr) ? 0 : (opt.max_fourier >= 0 && opt.max_fourier < NM ? opt.max_fourier : NM);
-  double stokes = 0.0;
-  int testconv = 0, m = 0;
-  for (m = 0; m <= n_fouriers; ++m) {
-    T sf_t = 0;
-    int st = fourier_term<NS, T>(c, opt, m, W, lay, &sf_t);
-    const double sf = (double)sf_t;
-    if (st != RT_OK) {
-      radiance[o] = in.missing; reflectance[o] = in.missing;
-      if (status) status[o] = st;
-      if (nfourier) nfourier[o] = m;
-      return;
-    }
-    if (m == 0) {
-      stokes = sf;
-      if (opt.do_focorr) stokes += ss + db;
-    } else {
-      double tazm = cos(raa * (double)m * kDTR) * sf;
-      double tnew = stokes + tazm;
-      bool conv = (tazm != 0.0) ? (fabs(tazm / tnew) < opt.accuracy) : true;
-      stokes = tnew;
-      if (conv) {
-        ++testconv;
-        if (!opt.do_double_convtest || testconv == 2) break;
-      } else {
-        testconv = 0;
-      }
-    }
+  r.ss = ss;
+  r.db = db;
+  // vlidort_masters_V2p8p3.f90:2305-2700: Fourier terms 0..NMOMENTS (only m = 0
+  // without single-scatter correction at nadir view)
+  r.n_fouriers = (vza == 0.0 && !opt.do_focorr) ? 0
+                 : (opt.max_fourier >= 0 && opt.max_fourier < NM ? opt.max_fourier : NM);
+  return true;
+}
+
+// Full solve of one pixel by one thread: set-up, then the Fourier series with
+// the double convergence test.  qx/qw: Gauss-Legendre streams on (0,1); tu/wu:
+// unit fine-layer quadrature for the enhanced-PS line of sight.  T is the
+// working precision of the series.
+template <int NS, typename T>
+RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sidx, const double* qx,
+                          const double* qw, const double* tu, const double* wu, const SolveScratch<T>& SS,
+                          double* radiance, double* reflectance, int* nfourier, int* status) {
+  SetupRecord r;
+  if (!solve_setup<NS, T>(opt, in, sidx, tu, wu, SS, radiance, reflectance, nfourier, status, r)) return;
+  const ScratchLayout<NS> lay(in.km);
+  SolveCtx<NS, T> c;
+  make_ctx<NS, T>(r, qx, qw, c);
+  FourierSum sum;
+  int m = 0, st = RT_OK;
+  for (m = 0; m <= r.n_fouriers; ++m) {
+    T sf = 0;
+    st = fourier_term<NS, T>(c, opt, m, SS.W, lay, &sf);
+    if (st != RT_OK || sum.add(opt, r, m, (double)sf)) break;
   }
-  if (m > n_fouriers) m = n_fouriers;
-  if (nfourier) nfourier[o] = m;
-  radiance[o] = stokes;
-  reflectance[o] = (kPiSingle * stokes) / (cos(sza * kPiSingle / 180.0) * opt.flux_factor);
+  solve_finish(opt, in, r, st, m, sum.stokes, radiance, reflectance, nfourier, status);
 }
 
 }  // namespace aerort

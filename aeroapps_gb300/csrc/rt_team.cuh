@@ -1,0 +1,781 @@
+// Team-cooperative Fourier series: the 32 lanes of one warp run the Fourier
+// series of one solve together, with the layer matrices in shared memory.
+//
+// Why: the thread-per-solve series keeps ~15 N^2 values per solve live (layer
+// eigen-solution, two layer solutions, the 2N x 2N interface system); at 12-16
+// streams that is 20-45 KB per thread, far beyond what an SM can hold for the
+// thread count that hides FP64 latency, so the working set streams from L2 or
+// HBM.  With one solve per warp the same working set (per solve) sits in
+// shared memory, and every step is parallel over matrix elements, matrix rows,
+// eigenvectors or Jacobi rotation pairs, so the FP64/FP32 pipes stay busy with
+// a handful of warps per SM.  The arithmetic is that of rt_solve.cuh (same
+// formulation, same pivot choices); only the schedule over lanes differs.
+//
+// The per-solve set-up (layer mixing, delta-M, single scatter, beam
+// attenuation) stays thread-per-solve (solve_setup); its per-layer outputs are
+// read from the set-up thread's scratch.
+#pragma once
+#include "rt_solve.cuh"
+
+namespace aerort {
+
+constexpr int kTeam = 32;
+
+// Lane index and warp barrier of a team.  On the host (the CPU test harness
+// runs one std::thread per lane) the barrier and the lane exchange go through
+// a callback and shared memory.
+struct Team {
+  int lane;
+  void (*host_sync)(void*);
+  void* host_arg;
+  RT_HD void sync() const {
+#ifdef __CUDA_ARCH__
+    __syncwarp();
+#else
+    host_sync(host_arg);
+#endif
+  }
+};
+
+// Sum of v over aligned groups of G lanes (G a power of two); every lane of a
+// group gets the group's sum.  red: kTeam scratch values in shared memory.
+template <int G, typename T>
+RT_HD T group_sum(const Team& tm, T v, T* red) {
+#ifdef __CUDA_ARCH__
+  (void)red;
+  for (int o = 1; o < G; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+#else
+  red[tm.lane] = v;
+  tm.sync();
+  T s = 0;
+  const int b = tm.lane & ~(G - 1);
+  for (int k = 0; k < G; ++k) s += red[b + k];
+  tm.sync();
+  return s;
+#endif
+}
+
+// Whether pred holds on any lane (every lane gets the answer).
+RT_HD bool team_any(const Team& tm, bool pred, int* flag) {
+#ifdef __CUDA_ARCH__
+  (void)flag;
+  return __any_sync(0xffffffffu, pred) != 0;
+#else
+  if (tm.lane == 0) *flag = 0;
+  tm.sync();
+  if (pred) *flag = 1;
+  tm.sync();
+  bool r = *flag != 0;
+  tm.sync();
+  return r;
+#endif
+}
+
+// Index of the largest v over the lanes, the smallest index among equals (the
+// first maximum of a serial scan); every lane gets it.  v < 0 marks a lane
+// without a candidate.
+template <typename T>
+RT_HD int team_argmax(const Team& tm, T v, int idx, T* red, int* ired, T* vmax) {
+#ifdef __CUDA_ARCH__
+  (void)red; (void)ired;
+  for (int o = 1; o < kTeam; o <<= 1) {
+    T ov = __shfl_xor_sync(0xffffffffu, v, o);
+    int oi = __shfl_xor_sync(0xffffffffu, idx, o);
+    if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+  }
+  *vmax = v;
+  return idx;
+#else
+  red[tm.lane] = v;
+  ired[tm.lane] = idx;
+  tm.sync();
+  T bv = red[0];
+  int bi = ired[0];
+  for (int k = 1; k < kTeam; ++k)
+    if (red[k] > bv || (red[k] == bv && ired[k] < bi)) { bv = red[k]; bi = ired[k]; }
+  tm.sync();
+  *vmax = bv;
+  return bi;
+#endif
+}
+
+// Shared-memory working set of one team.  Matrices are column-major with a
+// padded leading dimension (LD = N + 1, LK = 2N + 1) so that lanes working on
+// different columns hit different banks.
+template <int NS, typename T>
+struct TeamMem {
+  static constexpr int LD = NS + 1;
+  static constexpr int LK = 2 * NS + 1;
+  // eigen phase: Sp, Bs, H, G, V (N x LD each); interface: K (2N x LK), R (LK x (N+1))
+  static constexpr int NWORK = (5 * NS * LD > LK * (3 * NS + 1)) ? 5 * NS * LD : LK * (3 * NS + 1);
+  T piq[NS][2 * NS];                 // P~_l^m at the quadrature cosines
+  T piu[2 * NS], pi0[2 * NS];        // at the user and solar cosines
+  T pimq[NS], pimu, pim0;            // P~_m^m carried across terms
+  T lra[2 * NS], lrb[2 * NS], lr1;   // Legendre recurrence coefficients of term m
+  T og[2 * NS];                      // omega * beta_l of the current layer
+  T lsc[8];                          // dtau, 1 - omega, tuser, secbar, itrans, tmubar, emult, lnz
+  T work[NWORK];                     // eigen phase: Sp Bs H G V | interface: K R
+  T kv[NS], norm[NS], uhd[NS], uhu[NS], hm1[NS], hm2[NS], gup[NS], gdn[NS], dpi[NS], dmi[NS], rv[NS];
+  T rbeta;
+  T P[2][NS * LD], Q[2][NS * LD];    // layer solutions (prev / cur)
+  T t[2][NS], wt[2][2 * NS], wb[2][2 * NS];
+  T F[NS * LD], f[NS];               // L = F M + f of the current interface
+  T red[kTeam];
+  int ired[kTeam];
+  int flag;
+};
+
+// Per-solve sweep storage in global memory (one region per warp, contiguous,
+// element-parallel access): F_n, f_n, C_n, c_n, a_n, b_n, s_n for every layer.
+template <int NS>
+struct SweepLayout {
+  long F, f, C, c, a, b, s, total;
+  RT_HD explicit SweepLayout(int L) {
+    long o = 0;
+    F = o; o += (long)NS * NS * L; f = o; o += (long)NS * L;
+    C = o; o += (long)NS * NS * L; c = o; o += (long)NS * L;
+    a = o; o += (long)NS * L; b = o; o += (long)NS * L; s = o; o += L;
+    total = o;
+  }
+};
+
+// ---------------------------------------------------------------------------------- dense steps
+// Cholesky A = L L^T (lower triangle, leading dimension LDA), right-looking.
+// Returns false (on every lane) if a pivot is not positive.
+template <int LDA, typename T>
+RT_HD bool team_cholesky(const Team& tm, int n, T* A) {
+  for (int j = 0; j < n; ++j) {
+    const T d = A[j + LDA * j];
+    if (!(d > (T)0)) return false;
+    const T ljj = sqrt(d), inv = (T)1 / ljj;
+    tm.sync();
+    if (tm.lane == 0) A[j + LDA * j] = ljj;
+    for (int i = j + 1 + tm.lane; i < n; i += kTeam) A[i + LDA * j] *= inv;
+    tm.sync();
+    const int m2 = n - j - 1;
+    for (int e = tm.lane; e < m2 * m2; e += kTeam) {
+      const int i = j + 1 + e / m2, k = j + 1 + e % m2;
+      if (k <= i) A[i + LDA * k] -= A[i + LDA * j] * A[k + LDA * j];
+    }
+    tm.sync();
+  }
+  return true;
+}
+
+// In-place LU with partial pivoting of the n x n matrix A and solution of nrhs
+// right-hand sides B (leading dimension LDA for both); pivots as lu_solve.
+template <int LDA, typename T>
+RT_HD bool team_lu_solve(const Team& tm, int n, T* A, T* B, int nrhs, T* red, int* ired) {
+  for (int k = 0; k < n; ++k) {
+    const int i = k + tm.lane;
+    T vmax;
+    const int piv = team_argmax(tm, (i < n) ? fabs(A[i + LDA * k]) : (T)-1, i, red, ired, &vmax);
+    if (vmax == (T)0) return false;
+    if (piv != k) {
+      for (int j = tm.lane; j < n + nrhs; j += kTeam) {
+        T* X = (j < n) ? A + LDA * j : B + LDA * (j - n);
+        const T tmp = X[k];
+        X[k] = X[piv];
+        X[piv] = tmp;
+      }
+      tm.sync();
+    }
+    const T inv = (T)1 / A[k + LDA * k];
+    const int m2 = n - k - 1;
+    // multipliers, then the trailing update of A and B (each element once per k)
+    for (int e = tm.lane; e < m2; e += kTeam) A[k + 1 + e + LDA * k] *= inv;
+    tm.sync();
+    const int cols = m2 + nrhs;
+    for (int e = tm.lane; e < m2 * cols; e += kTeam) {
+      const int r = k + 1 + e % m2, cj = e / m2;
+      const T fm = A[r + LDA * k];
+      if (cj < m2) A[r + LDA * (k + 1 + cj)] -= fm * A[k + LDA * (k + 1 + cj)];
+      else B[r + LDA * (cj - m2)] -= fm * B[k + LDA * (cj - m2)];
+    }
+    tm.sync();
+  }
+  // back substitution, right-looking over rows
+  for (int i = n - 1; i >= 0; --i) {
+    const T inv = (T)1 / A[i + LDA * i];
+    for (int j = tm.lane; j < nrhs; j += kTeam) B[i + LDA * j] *= inv;
+    tm.sync();
+    for (int e = tm.lane; e < i * nrhs; e += kTeam) {
+      const int r = e % i, j = e / i;
+      B[r + LDA * j] -= A[r + LDA * i] * B[i + LDA * j];
+    }
+    tm.sync();
+  }
+  return true;
+}
+
+// One-sided Jacobi on the columns of G (leading dimension LD) with rotations
+// accumulated in V, in round-robin order: each round rotates n/2 disjoint
+// column pairs at once, LPP lanes per pair.  sigma[a] = |G e_a| on return.
+template <int NS, int LD, typename T>
+RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int* flag) {
+  constexpr int NP = NS / 2;
+  constexpr int LPP = (kTeam / NP >= 16) ? 16 : (kTeam / NP >= 8) ? 8 : (kTeam / NP >= 4) ? 4 : 2;
+  for (int e = tm.lane; e < n * n; e += kTeam) V[e % n + LD * (e / n)] = (e % n == e / n) ? (T)1 : (T)0;
+  tm.sync();
+  const int pr = tm.lane / LPP, sub = tm.lane % LPP;
+  const bool act = pr < NP;
+  const T tol = Eps<T>::v * (T)n;
+  bool done = false;
+  for (int sweep = 0; sweep < 30 && !done; ++sweep) {
+    bool rotated = false;
+    for (int round = 0; round < n - 1; ++round) {
+      int p = 0, q = 0;
+      if (act) {
+        p = (pr == 0) ? 0 : 1 + (pr - 1 + round) % (n - 1);
+        q = 1 + (n - 2 - pr + round) % (n - 1);
+        if (pr == 0) q = 1 + (n - 2 + round) % (n - 1);
+      }
+      T al = 0, be = 0, ga = 0;
+      if (act)
+        for (int i = sub; i < n; i += LPP) {
+          const T gp = G[i + LD * p], gq = G[i + LD * q];
+          al += gp * gp; be += gq * gq; ga += gp * gq;
+        }
+      al = group_sum<LPP>(tm, al, red);
+      be = group_sum<LPP>(tm, be, red);
+      ga = group_sum<LPP>(tm, ga, red);
+      if (act && fabs(ga) > tol * sqrt(al * be)) {
+        rotated = true;
+        const T zeta = (be - al) / ((T)2 * ga);
+        const T t = copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+        const T cs = (T)1 / sqrt((T)1 + t * t), sn = cs * t;
+        for (int i = sub; i < n; i += LPP) {
+          const T gp = G[i + LD * p], gq = G[i + LD * q];
+          G[i + LD * p] = cs * gp - sn * gq;
+          G[i + LD * q] = sn * gp + cs * gq;
+          const T vp = V[i + LD * p], vq = V[i + LD * q];
+          V[i + LD * p] = cs * vp - sn * vq;
+          V[i + LD * q] = sn * vp + cs * vq;
+        }
+      }
+      tm.sync();
+    }
+    done = !team_any(tm, rotated, flag);
+  }
+  if (tm.lane < n) {
+    T s = 0;
+    for (int i = 0; i < n; ++i) s += G[i + LD * tm.lane] * G[i + LD * tm.lane];
+    sigma[tm.lane] = sqrt(s);
+  }
+  tm.sync();
+  return done;
+}
+
+// ---------------------------------------------------------------------------------- layer solution
+// Legendre functions of term m at the N quadrature cosines (lanes 0..N-1), the
+// user cosine (lane N) and the solar cosine (lane N+1).
+template <int NS, typename T>
+RT_HD void team_legendre(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T>& c, int m) {
+  const int NM = c.NM;
+  for (int l = m + 2 + tm.lane; l <= NM; l += kTeam) {
+    const T d = (T)1 / sqrt((T)(l * l - m * m));
+    M.lra[l] = (T)(2 * l - 1) * d;
+    M.lrb[l] = sqrt((T)((l - 1) * (l - 1) - m * m)) * d;
+  }
+  if (tm.lane == 0) M.lr1 = sqrt((T)(2 * m + 1));
+  tm.sync();
+  const int i = tm.lane;
+  if (i < NS + 2) {
+    T x, *pim, *out;
+    if (i < NS) { x = c.qx[i]; pim = &M.pimq[i]; out = M.piq[i]; }
+    else if (i == NS) { x = c.mu_u; pim = &M.pimu; out = M.piu; }
+    else { x = c.cos_sza; pim = &M.pim0; out = M.pi0; }
+    for (int l = 0; l < m && l <= NM; ++l) out[l] = 0;
+    if (m <= NM) {
+      const T s = (x == (T)1) ? (T)0 : sqrt((T)1 - x * x);
+      const T pmm = (m == 0) ? (T)1 : *pim * s * sqrt((T)(2 * m - 1) / (T)(2 * m));
+      *pim = pmm;
+      out[m] = pmm;
+      if (m + 1 <= NM) out[m + 1] = x * M.lr1 * pmm;
+      for (int l = m + 2; l <= NM; ++l) out[l] = M.lra[l] * x * out[l - 1] - M.lrb[l] * out[l - 2];
+    }
+  }
+  tm.sync();
+}
+
+// Eigen-solution of layer n for term m into P/Q/t of slot `cur`, with the
+// Green's-function norms and user-angle homogeneous solutions (layer_eigen).
+template <int NS, typename T>
+RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T>& c, int m, int cur) {
+  constexpr int LD = TeamMem<NS, T>::LD;
+  const int N = NS, NM = c.NM;
+  T* Sp = M.work;
+  T* Bs = M.work + NS * LD;
+  T* H = M.work + 2 * NS * LD;
+  T* G = M.work + 3 * NS * LD;
+  T* V = M.work + 4 * NS * LD;
+  const T dtau = M.lsc[0], om1 = M.lsc[1];
+  // Sp (even l-m) and Sm (odd l-m) contractions of omega*beta_l P_l(mu_i) P_l(mu_j)
+  for (int e = tm.lane; e < N * N; e += kTeam) {
+    const int i = e % N, j = e / N;
+    T se = 0, so = 0;
+    for (int l = m; l <= NM; ++l) {
+      const T t = M.og[l] * M.piq[i][l] * M.piq[j][l];
+      if (((l - m) & 1) == 0) se += t; else so += t;
+    }
+    Sp[i + LD * j] = se;
+    T b = -c.sqw[i] * c.sqw[j] * so;
+    if (i == j) b += (T)1;
+    Bs[i + LD * j] = b;
+  }
+  tm.sync();
+  if (!team_cholesky<LD>(tm, N, Bs)) return RT_EIGEN_FAIL;
+  // R = M^-1 Lb
+  for (int e = tm.lane; e < N * N; e += kTeam) {
+    const int i = e % N, j = e / N;
+    if (i >= j) Bs[i + LD * j] /= c.qx[i];
+  }
+  // As = I - W^1/2 Sp W^1/2 (full)
+  for (int e = tm.lane; e < N * N; e += kTeam) {
+    const int i = e % N, j = e / N;
+    T a = -c.sqw[i] * Sp[i + LD * j] * c.sqw[j];
+    if (i == j) a += (T)1;
+    H[i + LD * j] = a;
+  }
+  tm.sync();
+  if (m == 0) {
+    // exact split of the conservative mode (see layer_eigen): Q As Q, reflector v
+    T ns = 0;
+    for (int i = 0; i < N; ++i) ns += c.sqw[i] * c.sqw[i];
+    ns = sqrt(ns);
+    T vv = 0;
+    for (int i = 0; i < N; ++i) {
+      const T vi = c.sqw[i] + (i == 0 ? ns : (T)0);
+      vv += vi * vi;
+    }
+    const T beta = (T)2 / vv;
+    if (tm.lane < N) M.rv[tm.lane] = c.sqw[tm.lane] + (tm.lane == 0 ? ns : (T)0);
+    if (tm.lane == 0) M.rbeta = beta;
+    tm.sync();
+    // p = beta A v ; w = p - (beta/2)(p.v) v ; A -= v w^T + w v^T
+    if (tm.lane < N) {
+      T s = 0;
+      for (int j = 0; j < N; ++j) s += H[tm.lane + LD * j] * M.rv[j];
+      M.dpi[tm.lane] = beta * s;
+    }
+    tm.sync();
+    T pv = 0;
+    for (int i = 0; i < N; ++i) pv += M.dpi[i] * M.rv[i];
+    const T half = (T)0.5 * beta * pv;
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e % N, j = e / N;
+      const T wi = M.dpi[i] - half * M.rv[i], wj = M.dpi[j] - half * M.rv[j];
+      H[i + LD * j] -= M.rv[i] * wj + wi * M.rv[j];
+    }
+    tm.sync();
+    if (tm.lane == 0) H[0] = om1;
+    if (tm.lane >= 1 && tm.lane < N) { H[tm.lane] = 0; H[LD * tm.lane] = 0; }
+    tm.sync();
+    if (!(om1 > (T)0)) return RT_EIGEN_FAIL;
+  }
+  if (!team_cholesky<LD>(tm, N, H)) return RT_EIGEN_FAIL;
+  if (m == 0) {
+    // QR = Q R into V (temporary), then G = L~^T QR
+    const T beta = M.rbeta;
+    if (tm.lane < N) {
+      const int j = tm.lane;
+      T d = 0;
+      for (int k = j; k < N; ++k) d += M.rv[k] * Bs[k + LD * j];
+      M.dmi[j] = d * beta;
+    }
+    tm.sync();
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e % N, j = e / N;
+      V[i + LD * j] = ((i >= j) ? Bs[i + LD * j] : (T)0) - M.dmi[j] * M.rv[i];
+    }
+    tm.sync();
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e % N, j = e / N;
+      T s = 0;
+      for (int k = i; k < N; ++k) s += H[k + LD * i] * V[k + LD * j];
+      G[i + LD * j] = s;
+    }
+  } else {
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e % N, j = e / N;
+      T s = 0;
+      for (int k = (i > j ? i : j); k < N; ++k) s += H[k + LD * i] * Bs[k + LD * j];
+      G[i + LD * j] = s;
+    }
+  }
+  tm.sync();
+  if (!team_jacobi<NS, LD>(tm, N, G, V, M.kv, M.red, &M.flag)) return RT_EIGEN_FAIL;
+  // per eigenvector a (lane a): La u_a in place of G[:, a], x, dif, X+, norm, user solutions
+  int fail = 0;
+  const int a = tm.lane;
+  if (a < N) {
+    const T k = M.kv[a];
+    if (!(k > (T)0)) {
+      fail = 1;
+    } else {
+      T* g = G + LD * a;
+      const T inv = (T)1 / k;
+      for (int i = N - 1; i >= 0; --i) {  // lower-triangular product in place, bottom up
+        T s = 0;
+        for (int kk = 0; kk <= i; ++kk) s += H[i + LD * kk] * g[kk];
+        g[i] = s * inv;
+      }
+      if (m == 0) {
+        T d = 0;
+        for (int i = 0; i < N; ++i) d += M.rv[i] * g[i];
+        d *= M.rbeta;
+        for (int i = 0; i < N; ++i) g[i] -= d * M.rv[i];
+      }
+      T x[NS], nrm = 0;
+      for (int i = 0; i < N; ++i) {
+        T s = 0;
+        for (int j = 0; j <= i; ++j) s += Bs[i + LD * j] * V[j + LD * a];
+        x[i] = s / c.sqw[i];
+        nrm += x[i] * x[i];
+      }
+      nrm = (T)1 / sqrt(nrm);
+      T nr = 0;
+      for (int i = 0; i < N; ++i) {
+        x[i] *= nrm;
+        const T dif = g[i] / (c.qx[i] * c.sqw[i]) * nrm;
+        g[i] = dif;  // keep dif for the user-angle solutions
+        M.P[cur][i + LD * a] = (T)0.5 * (x[i] + dif);
+        M.Q[cur][i + LD * a] = (T)0.5 * (x[i] - dif);
+        nr += c.qx[i] * c.qw[i] * x[i] * dif;
+      }
+      M.norm[a] = nr;
+      const T help = k * dtau;
+      M.t[cur][a] = help > (T)kMaxTau ? (T)0 : exp(-help);
+      T dn = 0, up = 0;
+      for (int l = m; l <= NM; ++l) {
+        const bool even = ((l - m) & 1) == 0;
+        T sps = 0;
+        for (int j = 0; j < N; ++j) sps += c.qw[j] * M.piq[j][l] * (even ? x[j] : g[j]);
+        const T h = (T)0.5 * M.og[l] * sps;
+        dn += (even ? M.piu[l] : -M.piu[l]) * h;
+        up += M.piu[l] * h;
+      }
+      M.uhd[a] = dn;
+      M.uhu[a] = up;
+    }
+  }
+  if (team_any(tm, fail != 0, &M.flag)) return RT_EIGEN_FAIL;
+  return RT_OK;
+}
+
+// Layer n of term m: eigen-solution, multipliers, Green's particular solution,
+// source coefficients a, b, s into the sweep storage (layer_solution).
+template <int NS, typename T>
+RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T>& c, const RtOptions& opt,
+                              int m, int n, bool laysc, int cur, T* sw, const SweepLayout<NS>& swl) {
+  constexpr int LD = TeamMem<NS, T>::LD;
+  const int N = NS, NM = c.NM;
+  int st = team_layer_eigen<NS, T>(tm, M, c, m, cur);
+  if (st != RT_OK) return st;
+  const T dtau = M.lsc[0], tuser = M.lsc[2], smu = c.sec_u;
+  const int a = tm.lane;
+  if (a < N) {
+    if (!laysc) { M.uhd[a] = 0; M.uhu[a] = 0; }
+    const T zdel = M.t[cur][a], kk = M.kv[a];
+    const T rho_p = smu + kk, rho_m = smu - kk;
+    if constexpr (sizeof(T) == sizeof(float)) {
+      M.hm2[a] = smu * dtau * e1_fn(rho_p * dtau);
+      M.hm1[a] = smu * dd1_neg(kk, smu, dtau);
+    } else {
+      M.hm2[a] = smu * (1.0 - zdel * tuser) * (1.0 / rho_p);
+      if (fabs(rho_m) < kTaylorSmall) M.hm1[a] = taylor1<T>(opt.taylor_order, rho_m, dtau, tuser, smu);
+      else M.hm1[a] = smu * (zdel - tuser) * (1.0 / rho_m);
+    }
+    sw[swl.a + a + N * (long)n] = M.uhd[a] * M.hm2[a];
+    sw[swl.b + a + N * (long)n] = M.uhu[a] * M.hm1[a];
+  }
+  for (int e = tm.lane; e < 2 * N; e += kTeam) { M.wt[cur][e] = 0; M.wb[cur][e] = 0; }
+  tm.sync();
+  const bool active = (n < c.cutoff) && laysc;
+  T spart = 0;
+  if (active) {
+    const T F1 = (T)(opt.flux_factor / kPI4);
+    const T secbar = M.lsc[3], cnst = M.lsc[4], wdel = M.lsc[5], emult = M.lsc[6];
+    // dpi/dmi: lanes over quadrature rows
+    if (tm.lane < N) {
+      const int i = tm.lane;
+      T sp = 0, sm = 0;
+      for (int l = m; l <= NM; ++l) {
+        const T t = M.piq[i][l] * (M.og[l] * M.pi0[l]);
+        sp += t;
+        sm += (((l - m) & 1) ? -t : t);
+      }
+      M.dpi[i] = F1 * sp;
+      M.dmi[i] = F1 * sm;
+    }
+    tm.sync();
+    T part = 0;
+    if (a < N) {
+      const T zdel = M.t[cur][a], kk = M.kv[a];
+      const T gp = secbar + kk, gm = secbar - kk, sigp = secbar + smu, itw = -cnst * wdel;
+      const bool tay = fabs(gm) < (T)kTaylorSmall;
+      T cf, df, sd, su;
+      if constexpr (sizeof(T) == sizeof(float)) {
+        cf = cnst * dd1_neg(kk, secbar, dtau);
+        df = cnst * dtau * e1_fn(gp * dtau);
+        sd = cnst * smu * dd2(kk + smu, sigp, dtau);
+        su = cnst * smu * dd2(gp, sigp, dtau);
+      } else {
+        cf = tay ? taylor1<T>(opt.taylor_order, gm, dtau, wdel, cnst) : cnst * (zdel - wdel) / gm;
+        df = cnst * (1.0 - zdel * wdel) / gp;
+        if (tay) sd = (cnst * smu) * taylor2<T>(opt.taylor_order, gm, sigp, dtau, (T)1, wdel * tuser, (T)1);
+        else sd = (cnst * M.hm2[a] - emult) / gm;
+        su = (itw * M.hm1[a] + emult) / gp;
+      }
+      T s1 = 0, s2 = 0;
+      for (int i = 0; i < N; ++i) {
+        s1 += c.qw[i] * (M.dpi[i] * M.P[cur][i + LD * a] + M.dmi[i] * M.Q[cur][i + LD * a]);
+        s2 += c.qw[i] * (M.dmi[i] * M.P[cur][i + LD * a] + M.dpi[i] * M.Q[cur][i + LD * a]);
+      }
+      const T at = s1 / M.norm[a], bt = s2 / M.norm[a];
+      M.gdn[a] = cf * at;
+      M.gup[a] = df * bt;
+      part = M.uhd[a] * sd * at + M.uhu[a] * su * bt;
+    }
+    M.red[tm.lane] = part;
+    tm.sync();
+    for (int k = 0; k < N; ++k) spart += M.red[k];
+    if (tm.lane < N) {
+      const int i = tm.lane;
+      T wu1 = 0, wu2 = 0, wl1 = 0, wl2 = 0;
+      for (int k = 0; k < N; ++k) {
+        wu1 += M.gup[k] * M.Q[cur][i + LD * k]; wu2 += M.gup[k] * M.P[cur][i + LD * k];
+        wl1 += M.gdn[k] * M.P[cur][i + LD * k]; wl2 += M.gdn[k] * M.Q[cur][i + LD * k];
+      }
+      M.wt[cur][i] = wu1; M.wt[cur][N + i] = wu2;
+      M.wb[cur][i] = wl1; M.wb[cur][N + i] = wl2;
+    }
+    if (!c.msmode) {
+      T upar = 0;
+      for (int l = m; l <= NM; ++l) upar += (F1 * M.og[l] * M.pi0[l]) * ((((l - m) & 1) ? (T)-1 : (T)1) * M.piu[l]);
+      spart += upar * emult;
+    }
+  }
+  if (tm.lane == 0) sw[swl.s + n] = laysc ? spart : (T)0;
+  tm.sync();
+  return RT_OK;
+}
+
+// One Fourier term (fourier_term): layer solutions, block interface sweep,
+// surface closure, bottom-up recovery with the TOA source recursion.
+// Per-layer inputs come from the set-up thread's scratch W; the sweep arrays
+// live in sw.  Every lane returns the same status and *out.
+template <int NS, typename T>
+RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& c, const RtOptions& opt, int m,
+                            const ScratchT<T>& W, const ScratchLayout<NS>& lay, T* sw, const SweepLayout<NS>& swl,
+                            T* out) {
+  constexpr int LD = TeamMem<NS, T>::LD;
+  constexpr int LK = TeamMem<NS, T>::LK;
+  const int N = NS, NM = c.NM, L = c.L;
+  const bool incl_surface = (m == 0) && (c.albedo != (T)0);
+  const T surface_factor = (m == 0) ? (T)2 : (T)1;
+  const T delta_factor = (m == 0) ? (T)1 : (T)2;
+  const bool localbeam = incl_surface && c.refl_directbeam;
+  T direct_beam = 0;
+  if (localbeam) {
+    T x0 = (T)4 * c.cos_sza / delta_factor;
+    x0 = (T)opt.flux_factor * x0 / (T)kPI4;
+    direct_beam = x0 * c.trans_solar_beam * c.albedo;
+  }
+  team_legendre<NS, T>(tm, M, c, m);
+  T* K = M.work;
+  T* R = M.work + 2 * NS * LK;
+  int cur = 1, prev = 0;
+  for (int n = 0; n < L; ++n) {
+    // per-layer inputs of layer n
+    for (int l = tm.lane; l <= NM; l += kTeam) M.og[l] = (l >= m) ? W[lay.og + l + 2 * NS * (long)n] : (T)0;
+    if (tm.lane < 8) {
+      const long src[8] = {lay.tdtau, lay.om1, lay.tuser, lay.tavsec, lay.titrans, lay.tmubar, lay.emult, lay.lnz};
+      M.lsc[tm.lane] = W[src[tm.lane] + n];
+    }
+    tm.sync();
+    const bool lsc = (m < 3) || ((T)m <= M.lsc[7]);
+    int st = team_layer_solution<NS, T>(tm, M, c, opt, m, n, lsc, cur, sw, swl);
+    if (st != RT_OK) return st;
+    if (n == 0) {
+      for (int e = tm.lane; e < N * N; e += kTeam) {
+        const int i = e % N, j = e / N;
+        K[i + LK * j] = M.P[cur][i + LD * j];
+        R[i + LK * j] = -M.Q[cur][i + LD * j] * M.t[cur][j];
+      }
+      for (int i = tm.lane; i < N; i += kTeam) R[i + LK * N] = -M.wt[cur][i];
+      tm.sync();
+      if (!team_lu_solve<LK>(tm, N, K, R, N + 1, M.red, M.ired)) return RT_BVP_SINGULAR;
+      for (int e = tm.lane; e < N * N; e += kTeam) {
+        const int i = e % N, j = e / N;
+        M.F[i + LD * j] = R[i + LK * j];
+        sw[swl.F + i + NS * j + (long)NS * NS * n] = R[i + LK * j];
+      }
+      for (int i = tm.lane; i < N; i += kTeam) { M.f[i] = R[i + LK * N]; sw[swl.f + i + NS * (long)n] = M.f[i]; }
+      tm.sync();
+    } else {
+      for (int e = tm.lane; e < N * N; e += kTeam) {
+        const int i = e % N, j = e / N;
+        T gt = M.Q[prev][i + LD * j], gb = M.P[prev][i + LD * j];
+        for (int k = 0; k < N; ++k) {
+          const T tf = M.t[prev][k] * M.F[k + LD * j];
+          gt += M.P[prev][i + LD * k] * tf;
+          gb += M.Q[prev][i + LD * k] * tf;
+        }
+        K[i + LK * j] = gt;
+        K[N + i + LK * j] = gb;
+        K[i + LK * (N + j)] = -M.P[cur][i + LD * j];
+        K[N + i + LK * (N + j)] = -M.Q[cur][i + LD * j];
+        R[i + LK * j] = M.Q[cur][i + LD * j] * M.t[cur][j];
+        R[N + i + LK * j] = M.P[cur][i + LD * j] * M.t[cur][j];
+      }
+      for (int i = tm.lane; i < N; i += kTeam) {
+        T gt = 0, gb = 0;
+        for (int k = 0; k < N; ++k) {
+          const T tf = M.t[prev][k] * M.f[k];
+          gt += M.P[prev][i + LD * k] * tf;
+          gb += M.Q[prev][i + LD * k] * tf;
+        }
+        R[i + LK * N] = M.wt[cur][i] - M.wb[prev][i] - gt;
+        R[N + i + LK * N] = M.wt[cur][N + i] - M.wb[prev][N + i] - gb;
+      }
+      tm.sync();
+      if (!team_lu_solve<LK>(tm, 2 * N, K, R, N + 1, M.red, M.ired)) return RT_BVP_SINGULAR;
+      const long oC = swl.C + (long)NS * NS * (n - 1), oc = swl.c + (long)NS * (n - 1);
+      const long oF = swl.F + (long)NS * NS * n, of = swl.f + (long)NS * n;
+      for (int e = tm.lane; e < N * N; e += kTeam) {
+        const int i = e % N, j = e / N;
+        sw[oC + i + NS * j] = R[i + LK * j];
+        M.F[i + LD * j] = R[N + i + LK * j];
+        sw[oF + i + NS * j] = R[N + i + LK * j];
+      }
+      for (int i = tm.lane; i < N; i += kTeam) {
+        sw[oc + i] = R[i + LK * N];
+        M.f[i] = R[N + i + LK * N];
+        sw[of + i] = M.f[i];
+      }
+      tm.sync();
+    }
+    prev = cur;
+    cur = 1 - cur;
+  }
+  // surface closure on the bottom layer (slot prev)
+  const int bl = prev;
+  const T kmult = incl_surface ? surface_factor * c.albedo : (T)0;
+  if (tm.lane < N) {
+    const int k = tm.lane;
+    T sp = 0, sm = 0;
+    for (int j = 0; j < N; ++j) {
+      sp += c.qx[j] * c.qw[j] * M.P[bl][j + LD * k];
+      sm += c.qx[j] * c.qw[j] * M.Q[bl][j + LD * k];
+    }
+    M.dpi[k] = sp * kmult;   // r2p
+    M.dmi[k] = sm * kmult;   // r2m
+  }
+  T r2b = 0;
+  for (int j = 0; j < N; ++j) r2b += c.qx[j] * c.qw[j] * M.wb[bl][j];
+  r2b *= kmult;
+  tm.sync();
+  for (int e = tm.lane; e < N * N; e += kTeam) {
+    const int i = e % N, j = e / N;
+    T s = M.P[bl][i + LD * j] - M.dmi[j];
+    for (int k = 0; k < N; ++k) s += (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.F[k + LD * j];
+    K[i + LK * j] = s;
+  }
+  if (tm.lane < N) {
+    const int i = tm.lane;
+    T s = -M.wb[bl][N + i] + r2b + (localbeam ? direct_beam : (T)0);
+    for (int k = 0; k < N; ++k) s -= (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.f[k];
+    R[i] = s;
+  }
+  tm.sync();
+  if (!team_lu_solve<LK>(tm, N, K, R, 1, M.red, M.ired)) return RT_BVP_SINGULAR;
+  // Mc in R[0..N), Lc in M.gup, Mn in M.gdn
+  T* Mc = M.hm1;
+  T* Lc = M.gup;
+  T* Mn = M.gdn;
+  if (tm.lane < N) Mc[tm.lane] = R[tm.lane];
+  tm.sync();
+  if (tm.lane < N) {
+    const int i = tm.lane;
+    T s = M.f[i];
+    for (int k = 0; k < N; ++k) s += M.F[i + LD * k] * Mc[k];
+    Lc[i] = s;
+  }
+  tm.sync();
+  T cum = 0;
+  if (incl_surface) {
+    if (tm.lane < N) {
+      const int i = tm.lane;
+      T h = M.wb[bl][i];
+      for (int k = 0; k < N; ++k) h += Lc[k] * M.P[bl][i + LD * k] * M.t[bl][k] + Mc[k] * M.Q[bl][i + LD * k];
+      M.red[i] = c.qx[i] * c.qw[i] * h;
+    }
+    tm.sync();
+    T s = 0;
+    for (int i = 0; i < N; ++i) s += M.red[i];
+    cum = kmult * s;
+    const bool incl_directrf = localbeam && !opt.do_focorr && !c.msmode;
+    if (incl_directrf) cum += direct_beam;
+    tm.sync();
+  }
+  for (int n = L - 1; n >= 0; --n) {
+    if (n < L - 1) {
+      const long oC = swl.C + (long)NS * NS * n, oc = swl.c + (long)NS * n;
+      const long oF = swl.F + (long)NS * NS * n, of = swl.f + (long)NS * n;
+      if (tm.lane < N) {
+        const int i = tm.lane;
+        T s = sw[oc + i];
+        for (int k = 0; k < N; ++k) s += sw[oC + i + NS * k] * Mc[k];
+        Mn[i] = s;
+      }
+      tm.sync();
+      if (tm.lane < N) {
+        const int i = tm.lane;
+        T s = sw[of + i];
+        for (int k = 0; k < N; ++k) s += sw[oF + i + NS * k] * Mn[k];
+        Lc[i] = s;
+        Mc[i] = Mn[i];
+      }
+      tm.sync();
+    }
+    if (tm.lane < N) {
+      const int k = tm.lane;
+      M.red[k] = Lc[k] * sw[swl.a + k + N * (long)n] + Mc[k] * sw[swl.b + k + N * (long)n];
+    }
+    tm.sync();
+    T src = sw[swl.s + n];
+    for (int k = 0; k < N; ++k) src += M.red[k];
+    cum = src + W[lay.tuser + n] * cum;
+    tm.sync();
+  }
+  *out = delta_factor * cum;
+  return RT_OK;
+}
+
+// The Fourier series of one set-up solve, run by the whole team; lane 0 writes
+// the outputs.
+template <int NS, typename T>
+RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOptions& opt, const LambertInputs& in,
+                               const SetupRecord& r, const double* qx, const double* qw, const ScratchT<T>& W,
+                               const ScratchLayout<NS>& lay, T* sw, double* radiance, double* reflectance,
+                               int* nfourier, int* status) {
+  SolveCtx<NS, T> c;
+  make_ctx<NS, T>(r, qx, qw, c);
+  if (tm.lane < NS) M.pimq[tm.lane] = 0;
+  if (tm.lane == 0) { M.pimu = 0; M.pim0 = 0; }
+  tm.sync();
+  const SweepLayout<NS> swl(r.L);
+  FourierSum sum;
+  int m = 0, st = RT_OK;
+  for (m = 0; m <= r.n_fouriers; ++m) {
+    T sf = 0;
+    st = team_fourier_term<NS, T>(tm, M, c, opt, m, W, lay, sw, swl, &sf);
+    if (st != RT_OK || sum.add(opt, r, m, (double)sf)) break;
+  }
+  if (tm.lane == 0) solve_finish(opt, in, r, st, m, sum.stokes, radiance, reflectance, nfourier, status);
+  tm.sync();
+}
+
+}  // namespace aerort

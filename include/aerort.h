@@ -196,6 +196,17 @@ int aerort_vlidort_scalar_lambert_ws_dev(aerort_workspace* ws, int precision, in
 int aerort_set_schedule(int nstreams, int precision, int threads_per_block, int blocks_per_sm);
 int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int* blocks_per_sm);
 
+/* RT kernel per (stream count, precision): AERORT_KERNEL_THREAD runs each
+ * solve on one thread; AERORT_KERNEL_TEAM runs the set-up thread per solve and
+ * the Fourier series on a whole warp per solve with the layer matrices in
+ * shared memory (the better choice where the per-solve working set is large).
+ * Defaults: team for 12 and 16 streams.  Results agree to round-off.
+ * aerort_get_kernel returns the kernel, or a negative rc. */
+#define AERORT_KERNEL_THREAD 0
+#define AERORT_KERNEL_TEAM 1
+int aerort_set_kernel(int nstreams, int precision, int kernel);
+int aerort_get_kernel(int nstreams, int precision);
+
 /* Allocation-free form of aerort_vlidort_scalar_lambert_batch_dev (same
  * arguments, same results).  No counterpart in the reference: it exists for
  * callers that must not have the library allocate or free device memory

@@ -1,0 +1,81 @@
+// Test harness: the team-cooperative Fourier series of the CUDA kernel run on
+// the host, one std::thread per lane with a barrier for the warp
+// synchronisation, so that the CPU test suite can compare it with the
+// thread-per-solve solver.  Never linked by the package.
+#include "../../aeroapps_gb300/csrc/rt_team.cuh"
+#include <barrier>
+#include <memory>
+#include <thread>
+#include <vector>
+using namespace aerort;
+static void gl(int n, double* x, double* w) {
+  for (int i = 0; i < n; ++i) {
+    double z = std::cos(M_PI * (i + 0.75) / (n + 0.5)), pp = 0;
+    for (int it = 0; it < 100; ++it) {
+      double p1 = 1, p2 = 0;
+      for (int j = 1; j <= n; ++j) { double p3 = p2; p2 = p1; p1 = ((2.0*j-1)*z*p2 - (j-1.0)*p3)/j; }
+      pp = n * (z*p1 - p2) / (z*z - 1);
+      double z1 = z; z = z1 - p1/pp; if (std::fabs(z-z1) < 1e-15) break;
+    }
+    x[n-1-i] = 0.5 - 0.5*z; w[n-1-i] = 1.0/((1-z*z)*pp*pp);
+  }
+}
+static void bar_sync(void* b) { static_cast<std::barrier<>*>(b)->arrive_and_wait(); }
+template <int NS, typename T>
+static int run(const RtOptions& opt, const LambertInputs& in, double* rad, double* refl, int* nf, int* st) {
+  double qx[NS], qw[NS], tu[4], wu[4];
+  gl(NS, qx, qw);
+  gl(opt.nfine > 0 ? opt.nfine : 1, tu, wu);
+  ScratchLayout<NS> lay(in.km, false);
+  SweepLayout<NS> swl(in.km);
+  std::vector<double> scr((lay.template bytes<T>() + 7) / 8);
+  std::vector<T> sweep(swl.total);
+  auto M = std::make_unique<TeamMem<NS, T>>();
+  const SolveScratch<T> S = make_scratch<NS, T>(scr.data(), 0, 1, in.km, false);
+  for (int s = 0; s < in.nobs * in.nch; ++s) {
+    SetupRecord r;
+    if (!solve_setup<NS, T>(opt, in, s, tu, wu, S, rad, refl, nf, st, r)) continue;
+    r.store(S.D, lay.rec);
+    SetupRecord rb;
+    rb.load(S.D, lay.rec);
+    std::barrier<> bar(kTeam);
+    std::vector<std::thread> th;
+    for (int lane = 0; lane < kTeam; ++lane)
+      th.emplace_back([&, lane] {
+        const Team tm{lane, bar_sync, &bar};
+        team_fourier_series<NS, T>(tm, *M, opt, in, rb, qx, qw, S.W, lay, sweep.data(), rad, refl, nf, st);
+      });
+    for (auto& t : th) t.join();
+  }
+  return 0;
+}
+template <typename T>
+static int dispatch(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
+    const double* tau, const double* ssa, const double* pmom, const double* he, const double* albedo, const double* sza,
+    const double* raa, const double* vza, const int* nadir, double missing, int max_fourier,
+    double* rad, double* refl, int* nf, int* st) {
+  RtOptions opt{1, 1, 0, 1, 3, 3, kAccuracySingle, 6371.0, 1.0, max_fourier};
+  LambertInputs in{km, nch, nobs, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nullptr, nullptr, nullptr, nullptr, nadir, missing};
+  switch (nstreams) {
+    case 4: return run<4, T>(opt, in, rad, refl, nf, st);
+    case 6: return run<6, T>(opt, in, rad, refl, nf, st);
+    case 8: return run<8, T>(opt, in, rad, refl, nf, st);
+    case 12: return run<12, T>(opt, in, rad, refl, nf, st);
+    case 16: return run<16, T>(opt, in, rad, refl, nf, st);
+  }
+  return -1;
+}
+extern "C" int team_scalar_lambert(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
+    const double* tau, const double* ssa, const double* pmom, const double* he, const double* albedo, const double* sza,
+    const double* raa, const double* vza, const int* nadir, double missing, int max_fourier,
+    double* rad, double* refl, int* nf, int* st) {
+  return dispatch<double>(km, nch, nobs, nstreams, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nadir,
+                          missing, max_fourier, rad, refl, nf, st);
+}
+extern "C" int team_scalar_lambert_mixed(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
+    const double* tau, const double* ssa, const double* pmom, const double* he, const double* albedo, const double* sza,
+    const double* raa, const double* vza, const int* nadir, double missing, int max_fourier,
+    double* rad, double* refl, int* nf, int* st) {
+  return dispatch<float>(km, nch, nobs, nstreams, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nadir,
+                         missing, max_fourier, rad, refl, nf, st);
+}
