@@ -1,8 +1,9 @@
 """The per-thread RT solver of the CUDA kernel (aeroapps_gb300/csrc/rt_solve.cuh),
-compiled for the host by this test only, against the oracle.  This checks the
-GPU formulation (symmetric eigen-reduction, block boundary-value sweep,
-top-down single-scatter integration) on the CPU; the GPU tests check the
-kernel itself."""
+compiled for the host by this test only, against the oracle, in both working
+precisions; and the team solver (rt_team.cuh, one std::thread per lane)
+against the per-thread one.  This checks the GPU formulation (graded Jacobi
+eigen-solution, block boundary-value sweep, team schedule) on the CPU; the
+GPU tests check the kernels themselves."""
 import ctypes
 import os
 import subprocess
@@ -27,7 +28,16 @@ def host_lib():
     return ctypes.CDLL(so)
 
 
-def _host(lib, c, nstreams):
+@pytest.fixture(scope="module")
+def team_lib():
+    d = tempfile.mkdtemp(prefix="aerort_team_")
+    so = os.path.join(d, "librtteam.so")
+    subprocess.run(["g++", "-O1", "-std=c++20", "-pthread", "-fPIC", "-shared", "-o", so,
+                    os.path.join(HERE, "host_harness", "rt_team_host.cpp")], check=True)
+    return ctypes.CDLL(so)
+
+
+def _host(lib, c, nstreams, fn="host_scalar_lambert"):
     P = lambda a: np.asfortranarray(a, np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     keep = [np.asfortranarray(c[k], np.float64) for k in ("ROT", "depol", "tau", "ssa", "pmom", "he", "albedo", "sza",
                                                             "raa", "vza")]
@@ -39,7 +49,7 @@ def _host(lib, c, nstreams):
     st = np.zeros_like(nf)
     first = np.array([nobs], np.int32)
     Ip = ctypes.POINTER(ctypes.c_int)
-    lib.host_scalar_lambert(c["km"], nch, nobs, nstreams, c["nmom"], *ptrs, first.ctypes.data_as(Ip),
+    getattr(lib, fn)(c["km"], nch, nobs, nstreams, c["nmom"], *ptrs, first.ctypes.data_as(Ip),
                             ctypes.c_double(MISSING), -1, rad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                             refl.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nf.ctypes.data_as(Ip),
                             st.ctypes.data_as(Ip))
@@ -53,3 +63,24 @@ def test_host_build_of_kernel_matches_oracle(host_lib, nstreams, km):
     orad, orefl, orc, onf, ost = oracle.scalar_lambert(*rt_args(c, nstreams), MISSING)
     assert np.array_equal(nf, onf) and np.all(st == 0)
     assert np.max(np.abs(rad / orad - 1)) < 1e-9
+
+
+@pytest.mark.parametrize("nstreams,km", [(8, 24), (16, 8)])
+def test_mixed_precision_solver_within_1e4(host_lib, nstreams, km):
+    c = random_aop_case(nstreams, km, nobs=4, nch=1, seed=km + 3 * nstreams, ssa_range=(0.999, 1.0))
+    rad, nf, st = _host(host_lib, c, nstreams, "host_scalar_lambert_mixed")
+    orad = oracle.scalar_lambert(*rt_args(c, nstreams), MISSING)[0]
+    assert np.all(st == 0)
+    assert np.max(np.abs(rad / orad - 1)) < 1e-4
+
+
+@pytest.mark.parametrize("nstreams,km", [(4, 6), (12, 3)])
+def test_team_solver_matches_thread_solver(host_lib, team_lib, nstreams, km):
+    c = random_aop_case(nstreams, km, nobs=1, nch=1, seed=km + 7 * nstreams)
+    rad, nf, st = _host(host_lib, c, nstreams)
+    trad, tnf, tst = _host(team_lib, c, nstreams, "team_scalar_lambert")
+    assert np.array_equal(nf, tnf) and np.array_equal(st, tst)
+    assert np.max(np.abs(trad / rad - 1)) < 1e-13
+    mrad, _, mst = _host(host_lib, c, nstreams, "host_scalar_lambert_mixed")
+    tmrad, _, tmst = _host(team_lib, c, nstreams, "team_scalar_lambert_mixed")
+    assert np.all(tmst == 0) and np.max(np.abs(tmrad / mrad - 1)) < 1e-5
