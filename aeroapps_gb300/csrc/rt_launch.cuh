@@ -166,6 +166,44 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
                                 int* st, cudaStream_t s) {
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
+  if (sc.kernel == 1) {
+    // team kernel: per warp 32 set-up scratches + one sweep region, all inside the arena
+    constexpr int WPB = 2;
+    const ScratchLayout<NS> tlay(in.km, false);
+    const SweepLayout<NS> swl(in.km);
+    const size_t per_warp = 32 * (size_t)tlay.template bytes<T>() + sizeof(T) * (size_t)swl.total + 256;
+    const long fit_blocks_t = (long)(arena_bytes / (per_warp * WPB));
+    if (fit_blocks_t < 1)
+      return set_error(AERORT_RC_ARG, "scalar_lambert: one team block needs more scratch than the workspace holds");
+    Quad q;
+    std::memset(&q, 0, sizeof(q));
+    gauss_legendre01(NS, q.qx, q.qw);
+    if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
+    const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
+    CUDA_TRY(cudaFuncSetAttribute(k_scalar_lambert_team<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert_team<NS, T, WPB>, 32 * WPB, smem));
+    if (per_sm < 1) return set_error(AERORT_RC_CUDA, "team kernel does not fit on an SM");
+    if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
+    long nblocks = (nsolve + 32 * WPB - 1) / (32 * WPB);
+    if (nblocks > (long)per_sm * num_sms) nblocks = (long)per_sm * num_sms;
+    if (nblocks > fit_blocks_t) nblocks = fit_blocks_t;
+    const long nthreads = nblocks * 32 * WPB;
+    const size_t sweep_off = ((size_t)tlay.template bytes<T>() * nthreads + 255) / 256 * 256;
+    int* counter = sched;
+    int* first = sched + 1;
+    k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+    k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo,
+                                                         in.missing, first);
+    CUDA_TRY(cudaGetLastError());
+    LambertInputs in2 = in;
+    in2.nadir_first = first;
+    k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, 32 * WPB, smem, s>>>(
+        opt, in2, q, arena, nthreads, (T*)((char*)arena + sweep_off), swl.total, nsolve, counter, rad, refl, nf, st);
+    CUDA_TRY(cudaGetLastError());
+    return 0;
+  }
   const int bs = sc.threads;
   const ScratchLayout<NS> lay(in.km);
   const long fit_blocks = (long)(arena_bytes / ((size_t)lay.template bytes<T>() * bs));
