@@ -686,7 +686,13 @@ extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
   if (int rc = static_arena(&arena, &arena_doubles, &sched, &num_sms)) return rc;
   LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
                    sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
-  const Schedule sc;  // 64 threads per block, occupancy-limited
+  Schedule sc;  // the library's kernel choice for this stream count; 64 threads per block, occupancy-limited
+  {
+    Context& c = ctx();
+    std::lock_guard<std::mutex> lk(c.mu);
+    const int si = stream_index(nstreams);
+    if (si >= 0) sc.kernel = c.sched[AERORT_PREC_FP64][si].kernel;
+  }
   return dispatch_fixed(AERORT_PREC_FP64, nstreams, lambert_options(plane_parallel), in, arena,
                         arena_doubles * sizeof(double), sched, num_sms, sc, radiance_VL, reflectance_VL, nfourier,
                         status, (cudaStream_t)stream);
