@@ -33,14 +33,33 @@ __global__ void __launch_bounds__(128) k_scalar_lambert(RtOptions opt, LambertIn
   }
 }
 
-// Team kernel: each warp takes 32 solves, runs their set-up thread per solve,
-// then runs their Fourier series one after another as a team (rt_team.cuh).
-// WPB warps per block, one TeamMem per warp in dynamic shared memory.
+// Solves per warp grab for the team kernel and the grid: enough warps for the
+// batch, at most the resident ones (resident_blocks x wpb warps), and at most
+// 32 solves per grab (one set-up lane per solve).
+inline int team_chunk(int nsolve, long resident_blocks, int wpb, long* nblocks) {
+  const long resident_warps = resident_blocks * wpb;
+  long chunk = (nsolve + resident_warps - 1) / resident_warps;
+  if (chunk < 1) chunk = 1;
+  if (chunk > 32) chunk = 32;
+  const long warps = (nsolve + chunk - 1) / chunk;
+  long need = (warps + wpb - 1) / wpb;
+  if (need > resident_blocks) need = resident_blocks;
+  if (need < 1) need = 1;
+  *nblocks = need;
+  return (int)chunk;
+}
+
+// Team kernel: each warp takes `chunk` (1..32) solves, runs their set-up
+// thread per solve (lanes 0..chunk-1), then runs their Fourier series one after
+// another as a team (rt_team.cuh).  The chunk is chosen so that every resident
+// warp gets work.  WPB warps per block, one TeamMem per warp in dynamic shared
+// memory.
 template <int NS, typename T, int WPB>
 __global__ void __launch_bounds__(32 * WPB) k_scalar_lambert_team(RtOptions opt, LambertInputs in, Quad q,
                                                                    void* scratch, long nthreads, T* sweep,
-                                                                   long sweep_per_warp, int nsolve, int* counter,
-                                                                   double* rad, double* refl, int* nf, int* st) {
+                                                                   long sweep_per_warp, int nsolve, int chunk,
+                                                                   int* counter, double* rad, double* refl, int* nf,
+                                                                   int* st) {
   extern __shared__ __align__(16) unsigned char team_smem[];
   const int lane = threadIdx.x & 31;
   TeamMem<NS, T>& M = reinterpret_cast<TeamMem<NS, T>*>(team_smem)[threadIdx.x >> 5];
@@ -52,12 +71,12 @@ __global__ void __launch_bounds__(32 * WPB) k_scalar_lambert_team(RtOptions opt,
   const Team tm{lane, nullptr, nullptr};
   for (;;) {
     int base = 0;
-    if (lane == 0) base = atomicAdd(counter, 32);
+    if (lane == 0) base = atomicAdd(counter, chunk);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= nsolve) break;
     const int s = base + lane;
     bool live = false;
-    if (s < nsolve) {
+    if (lane < chunk && s < nsolve) {
       SetupRecord r;
       live = solve_setup<NS, T>(opt, in, s, q.tu, q.wu, S, rad, refl, nf, st, r);
       if (live) r.store(S.D, lay.rec);
@@ -94,8 +113,8 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   if (per_sm < 1) return set_error(AERORT_RC_CUDA, "team kernel does not fit on an SM");
   const Schedule& sc = c.sched[sizeof(T) == sizeof(float) ? 1 : 0][stream_index(NS)];
   if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
-  long nblocks = (nsolve + bs - 1) / bs;
-  if (nblocks > (long)per_sm * c.num_sms) nblocks = (long)per_sm * c.num_sms;
+  long nblocks = 0;
+  const int chunk = team_chunk(nsolve, (long)per_sm * c.num_sms, WPB, &nblocks);
   const long nthreads = nblocks * bs;
   const ScratchLayout<NS> lay(in.km, false);
   const SweepLayout<NS> swl(in.km);
@@ -114,8 +133,8 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   in2.nadir_first = first;
   T* sweep = (T*)((char*)c.scratch.p + sweep_off);
   k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(opt, in2, q, c.scratch.p, nthreads, sweep,
-                                                                        swl.total, nsolve, counter, rad, refl, nf,
-                                                                        st);
+                                                                        swl.total, nsolve, chunk, counter, rad, refl,
+                                                                        nf, st);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -186,9 +205,10 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_scalar_lambert_team<NS, T, WPB>, 32 * WPB, smem));
     if (per_sm < 1) return set_error(AERORT_RC_CUDA, "team kernel does not fit on an SM");
     if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
-    long nblocks = (nsolve + 32 * WPB - 1) / (32 * WPB);
-    if (nblocks > (long)per_sm * num_sms) nblocks = (long)per_sm * num_sms;
-    if (nblocks > fit_blocks_t) nblocks = fit_blocks_t;
+    long resident = (long)per_sm * num_sms;
+    if (resident > fit_blocks_t) resident = fit_blocks_t;
+    long nblocks = 0;
+    const int chunk = team_chunk(nsolve, resident, WPB, &nblocks);
     const long nthreads = nblocks * 32 * WPB;
     const size_t sweep_off = ((size_t)tlay.template bytes<T>() * nthreads + 255) / 256 * 256;
     int* counter = sched;
@@ -200,7 +220,8 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
     LambertInputs in2 = in;
     in2.nadir_first = first;
     k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, 32 * WPB, smem, s>>>(
-        opt, in2, q, arena, nthreads, (T*)((char*)arena + sweep_off), swl.total, nsolve, counter, rad, refl, nf, st);
+        opt, in2, q, arena, nthreads, (T*)((char*)arena + sweep_off), swl.total, nsolve, chunk, counter, rad, refl,
+        nf, st);
     CUDA_TRY(cudaGetLastError());
     return 0;
   }
