@@ -273,7 +273,15 @@ def main():
     qt = np.array([chem.query_idx(n)[0] for n in names], np.int32)
     qb = np.array([chem.query_idx(n)[1] for n in names], np.int32)
     ch32 = np.array(CHANNELS, np.float32)
-    batch = make_batch(args.cols, seed=20261204 + rank)
+    # weak scaling: a global batch of cols x world columns, each rank solving its
+    # cost-balanced contiguous share (aeroapps_gb300.shard); no data-path collective
+    from aeroapps_gb300 import shard
+    full = make_batch(args.cols * world, seed=20261204)
+    if world > 1:
+        batch = subset(full, shard.my_columns(full["nstreams"], full["nlayers"], rank, world))
+    else:
+        batch = full
+    my_cols = batch["ncol"]
     nch = len(CHANNELS)
     dev = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dt).ravel(order="F"))).cuda()
     groups = []
@@ -355,8 +363,13 @@ def main():
         tt = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         ms = float(tt.item())
-    solves = args.cols * nch
-    value = solves * world / (ms * 1e-3)
+    solves = my_cols * nch
+    total_solves = solves
+    if world > 1:
+        ts = torch.tensor([float(solves)], device="cuda")
+        torch.distributed.all_reduce(ts, op=torch.distributed.ReduceOp.SUM)
+        total_solves = float(ts.item())
+    value = total_solves / (ms * 1e-3)
     rt_ms_m = sum(e0.elapsed_time(e1) for (_, e0, e1) in rt_m) / args.steps
 
     # ---------------------------------------------------------------- plain FP64 on the same batch
@@ -371,7 +384,7 @@ def main():
     torch.cuda.synchronize()
     ms_plain = p0.elapsed_time(p1) / args.plain_steps
     rt_ms_d = sum(e0.elapsed_time(e1) for (_, e0, e1) in rt_d) / args.plain_steps
-    plain_value = solves * world / (ms_plain * 1e-3)
+    plain_value = total_solves / (ms_plain * 1e-3)
 
     # ---------------------------------------------------------------- accuracy of mixed vs FP64, flops
     errs, bad, flops = [], 0, 0.0
