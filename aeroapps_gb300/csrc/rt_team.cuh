@@ -109,7 +109,7 @@ struct TeamMem {
   static constexpr int LK = 2 * NS + 1;
   // eigen phase: Sp, Bs, H, G, V (N x LD each); interface: K (2N x LK), R (LK x (N+1))
   static constexpr int NWORK = (5 * NS * LD > LK * (3 * NS + 1)) ? 5 * NS * LD : LK * (3 * NS + 1);
-  T piq[NS][2 * NS];                 // P~_l^m at the quadrature cosines
+  T piq[NS][2 * NS + 1];             // P~_l^m at the quadrature cosines (row padded against bank conflicts)
   T piu[2 * NS], pi0[2 * NS];        // at the user and solar cosines
   T pimq[NS], pimu, pim0;            // P~_m^m carried across terms
   T lra[2 * NS], lrb[2 * NS], lr1;   // Legendre recurrence coefficients of term m
