@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--serve-max-cols", type=int, default=4096, help="largest swath of the serving run")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--tune", action="store_true", help="autotune the RT schedules before timing")
+    ap.add_argument("--graph", action="store_true", help="replay the mixed step from a captured CUDA graph")
     return ap.parse_args()
 
 
@@ -310,7 +311,8 @@ def main():
     P = lambda t: t.data_ptr()
     ev = lambda: torch.cuda.Event(enable_timing=True)
 
-    def run_group(d, prec):
+    def run_group(d, prec, stream=None):
+        stream = stream or torch.cuda.current_stream().cuda_stream
         p = "m" if prec == _lib.PREC_MIXED else "d"
         fn = (L.aerort_vlidort_scalar_lambert_mixed_batch_dev if prec == _lib.PREC_MIXED
               else L.aerort_vlidort_scalar_lambert_batch_dev)
@@ -320,6 +322,7 @@ def main():
         assert rc == 0, _lib.last_error()
 
     def step(prec, rt_events=None):
+        stream = torch.cuda.current_stream().cuda_stream
         for d in groups:
             rc = L.aerort_get_aop_vector_dev(chem.handle, d["km"], d["n"], nch, 20, _lib.ptr(ch32, _lib.P_f),
                                              _lib.ptr(qt, _lib.P_i), _lib.ptr(qb, _lib.P_i), P(d["qm"]), P(d["rh"]),
@@ -328,7 +331,7 @@ def main():
             if rt_events is not None:
                 e0, e1 = ev(), ev()
                 e0.record()
-            run_group(d, prec)
+            run_group(d, prec, stream)
             if rt_events is not None:
                 e1.record()
                 rt_events.append((d["N"], e0, e1))
@@ -345,6 +348,17 @@ def main():
     for _ in range(args.warmup):
         step(_lib.PREC_MIXED)
     torch.cuda.synchronize()
+    graph, graph_note = None, "eager launches"
+    if args.graph:
+        # the whole step (AOP + RT launches of every stream group) as one CUDA
+        # graph; the warm-up above sized every buffer, so nothing allocates here
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            step(_lib.PREC_MIXED)
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        graph, graph_note = g, "CUDA graph replay of the captured step"
     if world > 1:
         torch.distributed.barrier()
     clocks = ClockSampler(local)
@@ -354,10 +368,16 @@ def main():
     torch.cuda.synchronize()
     t0.record()
     for _ in range(args.steps):
-        step(_lib.PREC_MIXED, rt_m)
+        if graph is not None:
+            graph.replay()
+        else:
+            step(_lib.PREC_MIXED, rt_m)
     t1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
+    if graph is not None:  # per-kernel times from one eager step
+        step(_lib.PREC_MIXED, rt_m)
+        torch.cuda.synchronize()
     ms = t0.elapsed_time(t1) / args.steps
     if world > 1:
         tt = torch.tensor([ms], device="cuda")
@@ -370,7 +390,7 @@ def main():
         torch.distributed.all_reduce(ts, op=torch.distributed.ReduceOp.SUM)
         total_solves = float(ts.item())
     value = total_solves / (ms * 1e-3)
-    rt_ms_m = sum(e0.elapsed_time(e1) for (_, e0, e1) in rt_m) / args.steps
+    rt_ms_m = sum(e0.elapsed_time(e1) for (_, e0, e1) in rt_m) / (1 if graph is not None else args.steps)
 
     # ---------------------------------------------------------------- plain FP64 on the same batch
     step(_lib.PREC_FP64)
@@ -490,7 +510,7 @@ def main():
         "config": {"workload": WORKLOAD + "; one step = %d columns x 4 wavelengths per GPU" % args.cols,
                    "columns_per_step": args.cols, "solves_per_step": solves, "wavelengths": list(CHANNELS),
                    "l2": "inputs larger than L2 (optics + scratch of a step: hundreds of MB)",
-                   "failed_solves": bad, "tuned_schedules": tuned or None},
+                   "failed_solves": bad, "tuned_schedules": tuned or None, "launch": graph_note},
         "accuracy": {"max_rel_err_vs_fp64": float(err.max()), "median_rel_err_vs_fp64": float(np.median(err)),
                      "radiances_compared": int(err.size), "bar": 1e-4},
         "plain_fp64": {"value": plain_value, "unit": "radiances/s", "ms_per_step": ms_plain,
