@@ -48,7 +48,7 @@ template <int NS>
 struct ScratchLayout {
   static constexpr int NMX = 2 * NS;  // NMOMENTS + 1 <= 2 NS
   long hgt, ext, escat, dts, dtau, avsec, itrans, rec, d_total;                         // FP64
-  long og, om1, lnz, tdtau, tavsec, titrans, tmubar, tuser, emult, F, f, C, c, a, b, s, t_total;  // working precision
+  long og, om1, lnz, tdtau, tavsec, titrans, tmubar, tuser, emult, wh, we, F, f, C, c, a, b, s, t_total;  // working precision
   // sweep = false leaves out F, f, C, c, a, b, s (kept elsewhere by the team kernel)
   RT_HD explicit ScratchLayout(int L, bool sweep = true) {
     long o = 0;
@@ -62,6 +62,7 @@ struct ScratchLayout {
     lnz = o; o += L;
     tdtau = o; o += L; tavsec = o; o += L; titrans = o; o += L; tmubar = o; o += L;
     tuser = o; o += L; emult = o; o += L;
+    wh = o; o += L + 1; we = o; o += L;  // heights and extinctions for the working-precision geometry
     if (sweep) {
       F = o; o += (long)NS * NS * L; f = o; o += (long)NS * L;
       C = o; o += (long)NS * NS * L; c = o; o += (long)NS * L;
@@ -1247,9 +1248,17 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
     double phi = raa;
     if (phi < 0.0) phi = -phi;
     if (phi > 360.0) phi = 360.0 - phi - 360.0;
-    if constexpr (sizeof(T) == sizeof(float))
-      fo_single_scatter_chord(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts,
-                              &ss, &db);
+    if constexpr (sizeof(T) == sizeof(float)) {
+      if (enhanced) {
+        for (int k = 0; k <= L; ++k) W[lay.wh + k] = (float)S[lay.hgt + k];
+        for (int k = 0; k < L; ++k) W[lay.we + k] = (float)S[lay.ext + k];
+        fo_enhanced_f32(opt, L, sza, vza, phi, alb, tu, wu, W, lay.wh, lay.we, S, lay.hgt, lay.ext, lay.escat, &ss,
+                        &db);
+      } else {
+        fo_single_scatter_chord(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat,
+                                lay.dts, &ss, &db);
+      }
+    }
     else
       fo_single_scatter_ref(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts,
                             &ss, &db);
@@ -1344,6 +1353,124 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
   r.n_fouriers = (vza == 0.0 && !opt.do_focorr) ? 0
                  : (opt.max_fourier >= 0 && opt.max_fourier < NM ? opt.max_fourier : NM);
   return true;
+}
+
+// ---------------------------------------------------------------------------------- FP32 geometry
+// The enhanced-PS single scatter of the mixed method with its geometry in
+// FP32 (fo_single_scatter_chord is the FP64 form).  Radii ~6400 km carry
+// 0.4 m of FP32 rounding, so no path is formed as a difference of radii:
+// whole-layer chords use the layer thickness, dz (r_hi + r_lo) / (c_hi + c_lo),
+// and the partial segment above a fine point uses its offset above the layer
+// bottom, rf - r_lo = tf (2 c_lo + tf) / (rf + r_lo).  wh/we: heights above
+// the surface [km] and extinctions [1/km] in FP32.
+RT_HD float sun_path_f32(int nn, float off, float ct, float st, float R0, const ScratchT<float>& W, long wh, long we) {
+  auto rad = [&](int k) { return R0 + W[wh + k]; };
+  const float rs = rad(nn) + off;
+  const float p = rs * st;
+  float r_lo = rs, c_lo = rs * ct;
+  float r_hi = rad(nn - 1), c_hi = sqrtf((r_hi - p) * (r_hi + p));
+  const float dz0 = (W[wh + nn - 1] - W[wh + nn]) - off;
+  float tau = W[we + nn - 1] * (dz0 * (r_hi + r_lo) / (c_hi + c_lo));
+  r_lo = r_hi; c_lo = c_hi;
+  for (int k = nn - 1; k >= 1; --k) {
+    r_hi = rad(k - 1);
+    c_hi = sqrtf((r_hi - p) * (r_hi + p));
+    tau += W[we + k - 1] * ((W[wh + k - 1] - W[wh + k]) * (r_hi + r_lo) / (c_hi + c_lo));
+    r_lo = r_hi; c_lo = c_hi;
+  }
+  return tau;
+}
+
+// Enhanced-PS first-order single scatter and direct bounce (mixed method).
+// Tangent rays (sun below the local horizon at a fine point: rare at the
+// angles AeroApps uses) fall back to the FP64 path.
+RT_HD void fo_enhanced_f32(const RtOptions& opt, int L, double sza, double vza, double phi, double albedo,
+                           const double* tu, const double* wu, const ScratchT<float>& W, long wh, long we,
+                           const Scratch& S, long ohgt, long oext, long oescat, double* ss, double* db) {
+  const float R0 = (float)opt.earth_radius;
+  auto rad = [&](int k) { return R0 + W[wh + k]; };
+  const double flux = opt.flux_factor / kPI4;
+  const bool overhead = (sza == 0.0);
+  const double th_R = sza * kDTR;
+  double cthd, sthbd;
+  if (sza == 90.0) { cthd = 0.0; sthbd = 1.0; } else { sthbd = sin(th_R); cthd = cos(th_R); }
+  const float cth = (float)cthd, sthb = (float)sthbd;
+  const bool donadir = (vza == 0.0);
+  float raycon = 0.0f, caL = 1.0f, saL = 0.0f;
+  if (!donadir) {
+    const double alphaL = vza * kDTR;
+    saL = (vza == 90.0) ? 1.0f : (float)sin(alphaL);
+    caL = (vza == 90.0) ? 0.0f : (float)cos(alphaL);
+    raycon = saL * rad(L);
+  }
+  float sdir0 = 0.0f, sdir2 = 0.0f;
+  if (!overhead) { sdir0 = (float)(-sthbd * cos(phi * kDTR)); sdir2 = -cth; }
+  const float cutoff = (float)kFoCutoff;
+  float atten_boa;
+  {
+    float st;
+    if (overhead) {
+      st = 0.0f;
+      for (int k = L; k >= 1; --k) st += W[we + k - 1] * (W[wh + k - 1] - W[wh + k]);
+    } else {
+      st = sun_path_f32(L, 0.0f, cth, sthb, R0, W, wh, we);
+    }
+    atten_boa = st < cutoff ? expf(-st) : 0.0f;
+  }
+  float cum = 0.0f, trans_above = 1.0f;
+  float c_up = donadir ? 0.0f : sqrtf((rad(0) - raycon) * (rad(0) + raycon));
+  for (int n = 1; n <= L; ++n) {
+    const float r_up = rad(n - 1), r_lo = rad(n);
+    const float dzn = W[wh + n - 1] - W[wh + n];
+    float losw, c_lo;
+    if (donadir) {
+      losw = dzn;
+      c_lo = r_lo;
+    } else {
+      c_lo = (n == L) ? r_lo * caL : sqrtf((r_lo - raycon) * (r_lo + raycon));
+      losw = dzn * (r_up + r_lo) / (c_up + c_lo);
+    }
+    const float kn = W[we + n - 1];
+    const float lostau = kn * losw;
+    const float lostrans = lostau < cutoff ? expf(-lostau) : 0.0f;
+    const bool zero_sun_boa = overhead && (n == L || donadir);
+    float sum = 0.0f;
+    for (int j = 0; j < opt.nfine; ++j) {
+      const float tf = losw * (float)tu[j], wf = losw * (float)wu[j];
+      float off, ct, st;
+      if (donadir) {
+        off = tf;
+        ct = cth; st = sthb;
+      } else {
+        const float X = c_lo + tf;
+        const float rf = sqrtf(raycon * raycon + X * X);
+        off = tf * (2.0f * c_lo + tf) / (rf + r_lo);
+        const float caf = X / rf, saf = raycon / rf;
+        const float scum = saL * caf - caL * saf, ccum = caL * caf + saL * saf;
+        if (overhead) { ct = ccum; st = scum; }
+        else { ct = scum * sdir0 - ccum * sdir2; st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct)); }
+      }
+      const bool dsf = donadir || overhead || (ct >= 0.0f);
+      float sd;
+      if (zero_sun_boa) {
+        sd = W[we + n - 1] * (dzn - off);
+        for (int k = n - 1; k >= 1; --k) sd += W[we + k - 1] * (W[wh + k - 1] - W[wh + k]);
+      } else if (dsf) {
+        sd = sun_path_f32(n, off, ct, st, R0, W, wh, we);
+      } else {
+        const double rfd = (double)R0 + (double)W[wh + n] + (double)off;
+        sd = (float)sun_optical_path_chord(false, false, rfd, (double)ct, (double)st, n, opt.earth_radius, S, ohgt,
+                                           oext, L);
+      }
+      const float attf = sd < cutoff ? expf(-sd) : 0.0f;
+      sum += attf * expf(-kn * (losw - tf)) * wf;
+    }
+    cum += trans_above * (float)S[oescat + n - 1] * (sum * kn);
+    trans_above *= lostrans;
+    c_up = c_lo;
+  }
+  *ss = flux * (double)cum;
+  *db = flux * (4.0 * cthd * albedo * (double)atten_boa) * (double)trans_above;
 }
 
 // Full solve of one pixel by one thread: set-up, then the Fourier series with
