@@ -48,7 +48,7 @@ template <int NS>
 struct ScratchLayout {
   static constexpr int NMX = 2 * NS;  // NMOMENTS + 1 <= 2 NS
   long hgt, ext, escat, dts, dtau, avsec, itrans, rec, d_total;                         // FP64
-  long og, om1, lnz, tdtau, tavsec, titrans, tmubar, tuser, emult, wh, we, F, f, C, c, a, b, s, t_total;  // working precision
+  long og, om1, lnz, tdtau, tavsec, titrans, tmubar, tuser, emult, wh, we, wc, F, f, C, c, a, b, s, t_total;  // working precision
   // sweep = false leaves out F, f, C, c, a, b, s (kept elsewhere by the team kernel)
   RT_HD explicit ScratchLayout(int L, bool sweep = true) {
     long o = 0;
@@ -63,6 +63,7 @@ struct ScratchLayout {
     tdtau = o; o += L; tavsec = o; o += L; titrans = o; o += L; tmubar = o; o += L;
     tuser = o; o += L; emult = o; o += L;
     wh = o; o += L + 1; we = o; o += L;  // heights and extinctions for the working-precision geometry
+    wc = o; o += L + 1;                  // shell terms of the previous level (working-precision Chapman)
     if (sweep) {
       F = o; o += (long)NS * NS * L; f = o; o += (long)NS * L;
       C = o; o += (long)NS * NS * L; c = o; o += (long)NS * L;
@@ -1172,6 +1173,13 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
   const double dep = in.depol[i];
   const double raysmom2 = (1.0 - dep) / (2.0 + dep);
   const long nk = (long)in.km * in.nch * in.nobs;
+  // Legendre recursion factors (2l-1)/l and (l-1)/l of the single-scatter phase
+  // function (FO_VectorSS_Spherfuncs.f90 DF1/DF2), once per solve
+  double df1[2 * NS + 2], df2[2 * NS + 2];
+  for (int l = 2; l <= ngreek && l < 2 * NS + 2; ++l) {
+    df1[l] = (double)(2 * l - 1) / (double)l;
+    df2[l] = (double)(l - 1) / (double)l;
+  }
   for (int k = 0; k <= L; ++k) S[lay.hgt + k] = in.he[k + (long)(in.km + 1) * j] * kHeightScale;
   for (int k = 0; k < L; ++k) {
     const double ray = in.rot[k + (long)in.km * (j + (long)in.nobs * i)];
@@ -1234,7 +1242,7 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
     double tms = opt.do_deltam ? om_in / (1.0 - fdel * om_in) : om_in;
     double p0 = 1.0, p1 = cosscat, fm = beta_in(0) * p0 + (ngreek >= 1 ? beta_in(1) * p1 : 0.0);
     for (int l = 2; l <= ngreek; ++l) {
-      double p2 = ((double)(2 * l - 1) / (double)l) * p1 * cosscat - ((double)(l - 1) / (double)l) * p0;
+      double p2 = df1[l] * p1 * cosscat - df2[l] * p0;
       fm += p2 * beta_in(l);
       p0 = p1; p1 = p2;
     }
@@ -1264,6 +1272,7 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
                             &ss, &db);
   }
   // ---------------------------------------------------------------- beam attenuation
+  if constexpr (sizeof(T) == sizeof(double)) {
   // Chapman factors (vlidort_geometry.f90:119-317), QSPREP / PREPTRANS / EMULT
   // (vlidort_miscsetups.f90:813-1292, 3187-3421).  The solar zenith is the
   // input angle at every level n (regular pseudo-spherical): the ray through
@@ -1282,15 +1291,6 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
       if (opt.do_plane_parallel || sn_toa == 0.0) {
         double cf = opt.do_plane_parallel ? 1.0 / mu_toa : 1.0;
         for (int k = 1; k <= n; ++k) ts += S[lay.dtau + k - 1] * cf;
-      } else if constexpr (sizeof(T) == sizeof(float)) {
-        const double rn = S[lay.hgt + n] + R0;
-        const double p = sn_toa * rn;
-        double r_lo = rn, c_lo = rn * mu_toa;
-        for (int k = n; k >= 1; --k) {
-          const double r_hi = S[lay.hgt + k - 1] + R0, c_hi = shell_c(r_hi, p);
-          ts += S[lay.dtau + k - 1] * ((r_hi + r_lo) / (c_hi + c_lo));
-          r_lo = r_hi; c_lo = c_hi;
-        }
       } else {
         const double r0 = S[lay.hgt + 0] + R0;
         double sinth1 = sn_toa * (S[lay.hgt + n] + R0) / r0;
@@ -1334,9 +1334,7 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
       if (n < cutoff) {
         double spb = dtn * avs;
         tmu = spb > kMaxTau ? 0.0 : exp(-spb);
-        double su;
-        if constexpr (sizeof(T) == sizeof(float)) su = -expm1(-(avs + sec_u) * dtn) / (avs + sec_u);
-        else su = (1.0 - tmu * tus) / (avs + sec_u);
+        double su = (1.0 - tmu * tus) / (avs + sec_u);
         em = (itr * sec_u) * su;
       }
       W[lay.tavsec + n] = (T)avs;
@@ -1344,6 +1342,79 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
       W[lay.tmubar + n] = (T)tmu;
       W[lay.tuser + n] = (T)tus;
       W[lay.emult + n] = (T)em;
+    }
+  }
+  } else {
+    // FP32 beam attenuation of the mixed method: the chord form of the
+    // Chapman factors, each level's slant increment ts_n - ts_{n-1} formed
+    // from differences of the shell terms (c_j(n-1) - c_j(n) =
+    // (p_n^2 - p_{n-1}^2) / (c_j(n-1) + c_j(n)), p_n - p_{n-1} = -sin(sza) dz_n)
+    // instead of a difference of cumulative slant depths.
+    const float mu = (float)cos_sza, sn = (float)sqrt(1.0 - cos_sza * cos_sza);
+    const float R0 = (float)opt.earth_radius, secu = (float)sec_u, maxtau = (float)kMaxTau;
+    for (int k = 0; k <= L; ++k) W[lay.wh + k] = (float)S[lay.hgt + k];
+    auto rad = [&](int k) { return R0 + W[lay.wh + k]; };
+    const bool pp = opt.do_plane_parallel || sn == 0.0f;
+    const float cf = opt.do_plane_parallel ? 1.0f / mu : 1.0f;
+    int cutoff = L;
+    float ts = 0.0f, s_t_0 = 1.0f, s_t_1 = 0.0f;
+    for (int n = 1; n <= L; ++n) {
+      const float dtn = W[lay.tdtau + n - 1];
+      float dts = 0.0f;
+      if (pp) {
+        dts = dtn * cf;
+        ts += dts;
+      } else {
+        const float rn = rad(n), p = sn * rn, pprev = sn * rad(n - 1);
+        const float dp2 = -sn * (W[lay.wh + n - 1] - W[lay.wh + n]) * (p + pprev);  // p^2 - pprev^2
+        float r_lo = rn, c_lo = rn * mu, tsn = 0.0f;
+        for (int k = n; k >= 1; --k) {
+          const float r_hi = rad(k - 1), c_hi = sqrtf((r_hi - p) * (r_hi + p));
+          const float A = c_hi + c_lo, dt = W[lay.tdtau + k - 1];
+          tsn += dt * ((r_hi + r_lo) / A);
+          if (k == n) {
+            dts += dt * ((r_hi + r_lo) / A);
+          } else {
+            const float cp_hi = W[lay.wc + k - 1], cp_lo = W[lay.wc + k];
+            const float dA = dp2 / (cp_hi + c_hi) + dp2 / (cp_lo + c_lo);
+            dts += dt * (r_hi + r_lo) * dA / (A * (cp_hi + cp_lo));
+          }
+          W[lay.wc + k] = c_lo;
+          r_lo = r_hi; c_lo = c_hi;
+        }
+        W[lay.wc + 0] = c_lo;
+        ts = tsn;
+      }
+      float avsec = 0.0f, itr = 0.0f;
+      if (n <= cutoff) {
+        if (ts > maxtau) cutoff = n;
+        else s_t_1 = expf(-ts);
+        avsec = dts / dtn;
+        itr = s_t_0;
+        s_t_0 = s_t_1;
+      }
+      W[lay.tavsec + n - 1] = avsec;
+      W[lay.titrans + n - 1] = itr;
+      if (n == L) {
+        r.trans_solar_beam = ts < maxtau ? (double)expf(-ts) : 0.0;
+        r.refl_directbeam = ts < maxtau;
+      }
+    }
+    r.cutoff = cutoff;
+    for (int n = 0; n < L; ++n) {
+      const float dtn = W[lay.tdtau + n];
+      const float sp = dtn * secu;
+      const float tus = sp > maxtau ? 0.0f : expf(-sp);
+      const float avs = W[lay.tavsec + n], itr = W[lay.titrans + n];
+      float tmu = 0.0f, em = 0.0f;
+      if (n < cutoff) {
+        const float spb = dtn * avs;
+        tmu = spb > maxtau ? 0.0f : expf(-spb);
+        em = (itr * secu) * (-expm1f(-(avs + secu) * dtn) / (avs + secu));
+      }
+      W[lay.tmubar + n] = tmu;
+      W[lay.tuser + n] = tus;
+      W[lay.emult + n] = em;
     }
   }
   r.ss = ss;
