@@ -16,7 +16,9 @@ import time
 
 from . import _lib
 
-CANDIDATES = ((64, 0), (32, 0), (128, 0), (64, 2), (64, 1), (32, 2), (32, 1), (96, 1), (128, 1))
+# (kernel, threads per block, blocks per SM); the team kernel has 64-thread blocks
+CANDIDATES = ((_lib.KERNEL_TEAM, 64, 0), (_lib.KERNEL_THREAD, 64, 0), (_lib.KERNEL_THREAD, 32, 0),
+              (_lib.KERNEL_TEAM, 64, 2), (_lib.KERNEL_THREAD, 128, 0), (_lib.KERNEL_THREAD, 64, 2))
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "schedules.json")
 
 
@@ -40,8 +42,11 @@ def save_cache(cache, path=CACHE):
     os.replace(tmp, path)
 
 
-def apply(nstreams, precision, threads_per_block, blocks_per_sm):
-    rc = _lib.lib().aerort_set_schedule(nstreams, precision, threads_per_block, blocks_per_sm)
+def apply(nstreams, precision, threads_per_block, blocks_per_sm, kernel=None):
+    L = _lib.lib()
+    rc = L.aerort_set_schedule(nstreams, precision, threads_per_block, blocks_per_sm)
+    if rc == 0 and kernel is not None:
+        rc = L.aerort_set_kernel(nstreams, precision, kernel)
     if rc != 0:
         raise RuntimeError("aerort_set_schedule rc=%d: %s" % (rc, _lib.last_error()))
 
@@ -53,25 +58,26 @@ def apply_cached(device_name, path=CACHE):
         dev, ns, prec = k.split("|")
         if dev != device_name:
             continue
-        apply(int(ns[1:]), _lib.PREC_MIXED if prec == "mixed" else _lib.PREC_FP64, v["threads"], v["blocks_per_sm"])
+        apply(int(ns[1:]), _lib.PREC_MIXED if prec == "mixed" else _lib.PREC_FP64, v["threads"], v["blocks_per_sm"],
+              v.get("kernel"))
         n += 1
     return n
 
 
 def tune(run, nstreams, precision, device_name, candidates=CANDIDATES, reps=1, budget_s=60.0, path=CACHE):
     """Time `run()` (one launch of the bucket on the current CUDA stream) under
-    each candidate schedule; install and cache the fastest.
+    each candidate (kernel, schedule); install and cache the fastest.
 
     run: callable enqueuing the RT launch for this bucket (device-resident inputs).
-    Returns {"threads", "blocks_per_sm", "ms", "all": [(threads, bps, ms), ...]}.
+    Returns {"kernel", "threads", "blocks_per_sm", "ms", "all": [(kernel, threads, bps, ms), ...]}.
     """
     import torch
     results = []
     t0 = time.time()
-    for tpb, bps in candidates:
+    for kern, tpb, bps in candidates:
         if results and time.time() - t0 > budget_s:
             break
-        apply(nstreams, precision, tpb, bps)
+        apply(nstreams, precision, tpb, bps, kern)
         run()  # warm: scratch sized for this grid
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -80,11 +86,11 @@ def tune(run, nstreams, precision, device_name, candidates=CANDIDATES, reps=1, b
             run()
         e1.record()
         torch.cuda.synchronize()
-        results.append((tpb, bps, e0.elapsed_time(e1) / reps))
-    tpb, bps, ms = min(results, key=lambda r: r[2])
-    apply(nstreams, precision, tpb, bps)
+        results.append((kern, tpb, bps, e0.elapsed_time(e1) / reps))
+    kern, tpb, bps, ms = min(results, key=lambda r: r[3])
+    apply(nstreams, precision, tpb, bps, kern)
     cache = load_cache(path)
-    cache[_key(device_name, nstreams, precision)] = {"threads": tpb, "blocks_per_sm": bps, "ms": ms,
+    cache[_key(device_name, nstreams, precision)] = {"kernel": kern, "threads": tpb, "blocks_per_sm": bps, "ms": ms,
                                                     "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
     save_cache(cache, path)
-    return {"threads": tpb, "blocks_per_sm": bps, "ms": ms, "all": results}
+    return {"kernel": kern, "threads": tpb, "blocks_per_sm": bps, "ms": ms, "all": results}

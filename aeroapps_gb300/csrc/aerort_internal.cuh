@@ -51,7 +51,11 @@ struct Context {
   DevBuf scratch, counter, stage[24];
   Schedule sched[2][5];  // [precision][stream index]
   Context() {
-    for (auto& p : sched) { p[3].kernel = 1; p[4].kernel = 1; }  // team kernel for 12 and 16 streams
+    // measured on GB300: the team kernel wins from 6 streams up in the mixed
+    // method and from 12 streams up in FP64 (stream index 0..4 = 4, 6, 8, 12, 16)
+    for (int si = 1; si < 5; ++si) sched[1][si].kernel = 1;
+    sched[0][3].kernel = 1;
+    sched[0][4].kernel = 1;
   }
   int setup();
   void release();

@@ -342,7 +342,8 @@ def main():
             for prec in (_lib.PREC_MIXED, _lib.PREC_FP64):
                 r = autotune.tune(lambda: run_group(d, prec), d["N"], prec, dev_name,
                                   budget_s=20.0 if prec == _lib.PREC_MIXED else 40.0)
-                tuned["%s N%d" % ("mixed" if prec else "fp64", d["N"])] = (r["threads"], r["blocks_per_sm"])
+                tuned["%s N%d" % ("mixed" if prec else "fp64", d["N"])] = (
+                    "team" if r["kernel"] == _lib.KERNEL_TEAM else "thread", r["threads"], r["blocks_per_sm"])
 
     # ---------------------------------------------------------------- mixed (headline)
     for _ in range(args.warmup):

@@ -49,4 +49,4 @@ def test_kernel_api_validates():
     L = _lib.lib()
     assert L.aerort_set_kernel(7, 0, 0) == 1003
     assert L.aerort_set_kernel(8, 0, 2) == 1002
-    assert L.aerort_get_kernel(16, 0) == 1 and L.aerort_get_kernel(4, 0) == 0
+    assert L.aerort_get_kernel(16, 0) == 1 and L.aerort_get_kernel(4, 0) == 0 and L.aerort_get_kernel(6, 1) == 1
