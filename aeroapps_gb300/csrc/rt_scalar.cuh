@@ -186,7 +186,10 @@ RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
   const T tol = Eps<T>::v * (T)n;
   bool done = false;
   for (int sweep = 0; sweep < 30 && !done; ++sweep) {
-    done = true;
+    // converged when no pair rotated, or when the largest normalised
+    // off-diagonal of this sweep was below sqrt(tol): Jacobi converges
+    // quadratically, so the sweep that follows would not rotate
+    T off = 0;
     for (int p = 0; p + 1 < n; ++p)
       for (int q = p + 1; q < n; ++q) {
         T al = 0, be = 0, ga = 0;
@@ -194,8 +197,9 @@ RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
           const T gp = G[i + NS * p], gq = G[i + NS * q];
           al += gp * gp; be += gq * gq; ga += gp * gq;
         }
-        if (!(fabs(ga) > tol * sqrt(al * be))) continue;
-        done = false;
+        const T nb = sqrt(al * be);
+        if (!(fabs(ga) > tol * nb)) continue;
+        if (fabs(ga) > off * nb) off = fabs(ga) / nb;
         const T zeta = (be - al) / ((T)2 * ga);
         const T t = copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
         const T cs = (T)1 / sqrt((T)1 + t * t), sn = cs * t;
@@ -208,6 +212,7 @@ RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
           V[i + NS * q] = sn * vp + cs * vq;
         }
       }
+    done = off * off <= tol;
   }
   for (int a = 0; a < n; ++a) {
     T s = 0;

@@ -121,6 +121,8 @@ struct TeamMem {
   T P[2][NS * LD], Q[2][NS * LD];    // layer solutions (prev / cur)
   T t[2][NS], wt[2][2 * NS], wb[2][2 * NS];
   T F[NS * LD], f[NS];               // L = F M + f of the current interface
+  T Vp[NS * LD];                     // previous layer's Jacobi rotations (warm start)
+  int vp_valid;
   T red[kTeam];
   int ired[kTeam];
   int flag;
@@ -212,18 +214,20 @@ RT_HD bool team_lu_solve(const Team& tm, int n, T* A, T* B, int nrhs, T* red, in
 // One-sided Jacobi on the columns of G (leading dimension LD) with rotations
 // accumulated in V, in round-robin order: each round rotates n/2 disjoint
 // column pairs at once, LPP lanes per pair.  sigma[a] = |G e_a| on return.
+// warm = true: V already holds a starting rotation, applied to G by the caller.
 template <int NS, int LD, typename T>
-RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int* flag) {
+RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int* flag, bool warm = false) {
   constexpr int NP = NS / 2;
   constexpr int LPP = (kTeam / NP >= 16) ? 16 : (kTeam / NP >= 8) ? 8 : (kTeam / NP >= 4) ? 4 : 2;
-  for (int e = tm.lane; e < n * n; e += kTeam) V[e % n + LD * (e / n)] = (e % n == e / n) ? (T)1 : (T)0;
+  if (!warm)
+    for (int e = tm.lane; e < n * n; e += kTeam) V[e % n + LD * (e / n)] = (e % n == e / n) ? (T)1 : (T)0;
   tm.sync();
   const int pr = tm.lane / LPP, sub = tm.lane % LPP;
   const bool act = pr < NP;
   const T tol = Eps<T>::v * (T)n;
   bool done = false;
   for (int sweep = 0; sweep < 30 && !done; ++sweep) {
-    bool rotated = false;
+    T off = 0;  // largest normalised off-diagonal rotated in this sweep (see jacobi_svd)
     for (int round = 0; round < n - 1; ++round) {
       int p = 0, q = 0;
       if (act) {
@@ -240,8 +244,9 @@ RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int*
       al = group_sum<LPP>(tm, al, red);
       be = group_sum<LPP>(tm, be, red);
       ga = group_sum<LPP>(tm, ga, red);
-      if (act && fabs(ga) > tol * sqrt(al * be)) {
-        rotated = true;
+      const T nb = sqrt(al * be);
+      if (act && fabs(ga) > tol * nb) {
+        if (fabs(ga) > off * nb) off = fabs(ga) / nb;
         const T zeta = (be - al) / ((T)2 * ga);
         const T t = copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
         const T cs = (T)1 / sqrt((T)1 + t * t), sn = cs * t;
@@ -256,7 +261,7 @@ RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int*
       }
       tm.sync();
     }
-    done = !team_any(tm, rotated, flag);
+    done = !team_any(tm, off * off > tol, flag);
   }
   if (tm.lane < n) {
     T s = 0;
@@ -405,7 +410,27 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
     }
   }
   tm.sync();
-  if (!team_jacobi<NS, LD>(tm, N, G, V, M.kv, M.red, &M.flag)) return RT_EIGEN_FAIL;
+  // warm start from the previous layer of this term: its eigenvectors are
+  // usually close, so G V_prev is nearly column-orthogonal and few sweeps remain
+  const bool warm = M.vp_valid != 0;
+  if (warm) {
+    T* Wt = M.work + 4 * NS * LD;  // V slot as temporary for G V_prev
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e % N, j = e / N;
+      T s = 0;
+      for (int k = 0; k < N; ++k) s += G[i + LD * k] * M.Vp[k + LD * j];
+      Wt[i + LD * j] = s;
+    }
+    tm.sync();
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e % N, j = e / N;
+      G[i + LD * j] = Wt[i + LD * j];
+      V[i + LD * j] = M.Vp[i + LD * j];
+    }
+  }
+  if (!team_jacobi<NS, LD>(tm, N, G, V, M.kv, M.red, &M.flag, warm)) return RT_EIGEN_FAIL;
+  for (int e = tm.lane; e < N * N; e += kTeam) M.Vp[e % N + LD * (e / N)] = V[e % N + LD * (e / N)];
+  if (tm.lane == 0) M.vp_valid = 1;
   // per eigenvector a (lane a): La u_a in place of G[:, a], x, dif, X+, norm, user solutions
   int fail = 0;
   const int a = tm.lane;
@@ -587,6 +612,8 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
   T* K = M.work;
   T* R = M.work + 2 * NS * LK;
   int cur = 1, prev = 0;
+  if (tm.lane == 0) M.vp_valid = 0;
+  tm.sync();
   for (int n = 0; n < L; ++n) {
     // per-layer inputs of layer n
     for (int l = tm.lane; l <= NM; l += kTeam) M.og[l] = (l >= m) ? W[lay.og + l + 2 * NS * (long)n] : (T)0;
