@@ -35,7 +35,7 @@ struct DevBuf {
 // kernel: 0 = thread per solve, 1 = team (one warp per solve for the Fourier
 // series, rt_team.cuh).
 struct Schedule {
-  int threads = 64;
+  int threads = 32;  // one warp per block spreads small batches over more SMs
   int blocks_per_sm = 0;
   int kernel = 0;
 };
@@ -51,9 +51,11 @@ struct Context {
   DevBuf scratch, counter, stage[24];
   Schedule sched[2][5];  // [precision][stream index]
   Context() {
-    // measured on GB300: the team kernel wins from 6 streams up in the mixed
-    // method and from 12 streams up in FP64 (stream index 0..4 = 4, 6, 8, 12, 16)
-    for (int si = 1; si < 5; ++si) sched[1][si].kernel = 1;
+    // measured on GB300: the team kernel wins at 6, 12 and 16 streams in the
+    // mixed method and at 12 and 16 in FP64 (stream index 0..4 = 4, 6, 8, 12, 16)
+    sched[1][1].kernel = 1;
+    sched[1][3].kernel = 1;
+    sched[1][4].kernel = 1;
     sched[0][3].kernel = 1;
     sched[0][4].kernel = 1;
   }

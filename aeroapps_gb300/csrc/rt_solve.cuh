@@ -1242,7 +1242,10 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
     double tms = opt.do_deltam ? om_in / (1.0 - fdel * om_in) : om_in;
     double p0 = 1.0, p1 = cosscat, fm = beta_in(0) * p0 + (ngreek >= 1 ? beta_in(1) * p1 : 0.0);
     for (int l = 2; l <= ngreek; ++l) {
-      double p2 = df1[l] * p1 * cosscat - df2[l] * p0;
+      const bool tab = l < 2 * NS + 2;  // more input moments than the table holds: divide here
+      const double f1 = tab ? df1[l] : (double)(2 * l - 1) / (double)l;
+      const double f2 = tab ? df2[l] : (double)(l - 1) / (double)l;
+      double p2 = f1 * p1 * cosscat - f2 * p0;
       fm += p2 * beta_in(l);
       p0 = p1; p1 = p2;
     }

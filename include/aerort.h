@@ -200,8 +200,8 @@ int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int
  * solve on one thread; AERORT_KERNEL_TEAM runs the set-up thread per solve and
  * the Fourier series on a whole warp per solve with the layer matrices in
  * shared memory (the better choice where the per-solve working set is large).
- * Defaults: team from 6 streams (mixed) and from 12 streams (FP64), as
- * measured on GB300.  Results agree to round-off.
+ * Defaults: team at 6, 12 and 16 streams (mixed) and at 12 and 16 streams
+ * (FP64), as measured on GB300.  Results agree to round-off.
  * aerort_get_kernel returns the kernel, or a negative rc. */
 #define AERORT_KERNEL_THREAD 0
 #define AERORT_KERNEL_TEAM 1

@@ -123,4 +123,4 @@ def test_schedule_api_validates():
     assert L.aerort_set_schedule(8, 1, 96, 2) == 0
     assert L.aerort_get_schedule(8, 1, ctypes.byref(t), ctypes.byref(b)) == 0
     assert (t.value, b.value) == (96, 2)
-    assert L.aerort_set_schedule(8, 1, 64, 0) == 0
+    assert L.aerort_set_schedule(8, 1, 32, 0) == 0

@@ -84,3 +84,19 @@ def test_team_solver_matches_thread_solver(host_lib, team_lib, nstreams, km):
     mrad, _, mst = _host(host_lib, c, nstreams, "host_scalar_lambert_mixed")
     tmrad, _, tmst = _host(team_lib, c, nstreams, "team_scalar_lambert_mixed")
     assert np.all(tmst == 0) and np.max(np.abs(tmrad / mrad - 1)) < 1e-5
+
+
+def test_more_input_moments_than_streams(host_lib):
+    # nMom = 40 > 2N: delta-M truncates at 2N-1 while the single-scatter phase
+    # function uses every input moment
+    c = random_aop_case(6, 30, nobs=4, nch=1, seed=17)
+    nmom = 40
+    pm = np.zeros(c["g"].shape + (nmom, 1))
+    for l in range(nmom):
+        pm[..., l, 0] = (2 * l + 1) * c["g"] ** l
+    c["pmom"] = np.asfortranarray(pm)
+    c["nmom"] = nmom
+    orad = oracle.scalar_lambert(*rt_args(c, 6), MISSING)[0]
+    for fn, tol in (("host_scalar_lambert", 1e-9), ("host_scalar_lambert_mixed", 1e-4)):
+        rad, nf, st = _host(host_lib, c, 6, fn)
+        assert np.all(st == 0) and np.max(np.abs(rad / orad - 1)) < tol
