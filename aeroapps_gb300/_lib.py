@@ -55,6 +55,7 @@ _SIGNATURES = {
                                              [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
     "aerort_get_schedule": (c_int, [c_int, c_int, P_i, P_i]),
     "aerort_set_kernel": (c_int, [c_int, c_int, c_int]),
+    "aerort_refined_count": (c_int, [c_void_p, P_i]),
     "aerort_get_kernel": (c_int, [c_int, c_int]),
     "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_probe_ffma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),

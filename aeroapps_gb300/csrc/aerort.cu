@@ -405,9 +405,10 @@ __global__ void k_nadir_first(int nobs, int nch, const double* sza, const double
   for (int i = 0; i < nch; ++i)
     if (!miss(albedo[j + (long)nobs * i])) { atomicMin(first, j); return; }
 }
-__global__ void k_init_sched(int* counter, int* first, int nobs) {
+__global__ void k_init_sched(int* counter, int* first, int nobs, int* zero) {
   *counter = 0;
   *first = nobs;
+  if (zero) *zero = 0;
 }
 }  // namespace aerort_internal
 
@@ -430,32 +431,50 @@ RtOptions lambert_options(int plane_parallel) {
 
 template <typename T>
 int dispatch_lambert_t(Context& c, int nstreams, const RtOptions& opt, const LambertInputs& in, double* rad,
-                       double* refl, int* nf, int* st, cudaStream_t s) {
+                       double* refl, int* nf, int* st, cudaStream_t s, const Worklist& wl) {
   const int si = stream_index(nstreams);
   if (si >= 0 && c.sched[sizeof(T) == sizeof(float) ? 1 : 0][si].kernel == 1) {
     switch (nstreams) {
-      case 4: return launch_scalar_lambert_team<4, T>(c, opt, in, rad, refl, nf, st, s);
-      case 6: return launch_scalar_lambert_team<6, T>(c, opt, in, rad, refl, nf, st, s);
-      case 8: return launch_scalar_lambert_team<8, T>(c, opt, in, rad, refl, nf, st, s);
-      case 12: return launch_scalar_lambert_team<12, T>(c, opt, in, rad, refl, nf, st, s);
-      case 16: return launch_scalar_lambert_team<16, T>(c, opt, in, rad, refl, nf, st, s);
+      case 4: return launch_scalar_lambert_team<4, T>(c, opt, in, rad, refl, nf, st, s, wl);
+      case 6: return launch_scalar_lambert_team<6, T>(c, opt, in, rad, refl, nf, st, s, wl);
+      case 8: return launch_scalar_lambert_team<8, T>(c, opt, in, rad, refl, nf, st, s, wl);
+      case 12: return launch_scalar_lambert_team<12, T>(c, opt, in, rad, refl, nf, st, s, wl);
+      case 16: return launch_scalar_lambert_team<16, T>(c, opt, in, rad, refl, nf, st, s, wl);
     }
   }
   switch (nstreams) {
-    case 4: return launch_scalar_lambert<4, T>(c, opt, in, rad, refl, nf, st, s);
-    case 6: return launch_scalar_lambert<6, T>(c, opt, in, rad, refl, nf, st, s);
-    case 8: return launch_scalar_lambert<8, T>(c, opt, in, rad, refl, nf, st, s);
-    case 12: return launch_scalar_lambert<12, T>(c, opt, in, rad, refl, nf, st, s);
-    case 16: return launch_scalar_lambert<16, T>(c, opt, in, rad, refl, nf, st, s);
+    case 4: return launch_scalar_lambert<4, T>(c, opt, in, rad, refl, nf, st, s, wl);
+    case 6: return launch_scalar_lambert<6, T>(c, opt, in, rad, refl, nf, st, s, wl);
+    case 8: return launch_scalar_lambert<8, T>(c, opt, in, rad, refl, nf, st, s, wl);
+    case 12: return launch_scalar_lambert<12, T>(c, opt, in, rad, refl, nf, st, s, wl);
+    case 16: return launch_scalar_lambert<16, T>(c, opt, in, rad, refl, nf, st, s, wl);
   }
   return set_error(AERORT_RC_UNSUPPORTED, "nstreams must be one of 4, 6, 8, 12, 16");
 }
 
+// The mixed method is two launches on one stream: the FP32 series for every
+// solve, which lists the solves whose Fourier sum cancels by more than
+// kRefineRatio, then the FP64 series for the listed solves only (their outputs
+// overwrite the mixed ones).  The list and its count stay on the device.
 int dispatch_lambert(Context& c, int precision, int nstreams, const RtOptions& opt, const LambertInputs& in,
                      double* rad, double* refl, int* nf, int* st, cudaStream_t s) {
-  if (precision == AERORT_PREC_MIXED) return dispatch_lambert_t<float>(c, nstreams, opt, in, rad, refl, nf, st, s);
-  if (precision == AERORT_PREC_FP64) return dispatch_lambert_t<double>(c, nstreams, opt, in, rad, refl, nf, st, s);
-  return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
+  if (precision == AERORT_PREC_FP64)
+    return dispatch_lambert_t<double>(c, nstreams, opt, in, rad, refl, nf, st, s, Worklist());
+  if (precision != AERORT_PREC_MIXED)
+    return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
+  const int nsolve = in.nobs * in.nch;
+  if (int rc = c.redo.ensure(sizeof(int) * ((size_t)nsolve + 1))) return rc;
+  if (int rc = c.counter.ensure(4 * sizeof(int))) return rc;
+  int* count = (int*)c.counter.p + 2;
+  Worklist wm;
+  wm.out_list = (int*)c.redo.p;
+  wm.out_count = count;
+  wm.ratio = kRefineRatio;
+  if (int rc = dispatch_lambert_t<float>(c, nstreams, opt, in, rad, refl, nf, st, s, wm)) return rc;
+  Worklist wd;
+  wd.in_list = (const int*)c.redo.p;
+  wd.in_count = count;
+  return dispatch_lambert_t<double>(c, nstreams, opt, in, rad, refl, nf, st, s, wd);
 }
 
 int lambert_checks(int km, int nch, int nobs, int nstreams, int nMom) {
@@ -540,6 +559,17 @@ extern "C" int aerort_set_schedule(int nstreams, int precision, int threads_per_
   return AERORT_OK;
 }
 
+extern "C" int aerort_refined_count(void* stream, int* count) {
+  if (!count) return set_error(AERORT_RC_ARG, "refined_count: null pointer");
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lk(c.mu);
+  *count = 0;
+  if (!c.counter.p || c.counter.bytes < 4 * sizeof(int)) return AERORT_OK;
+  CUDA_TRY(cudaMemcpyAsync(count, (int*)c.counter.p + 2, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return AERORT_OK;
+}
+
 extern "C" int aerort_set_kernel(int nstreams, int precision, int kernel) {
   const int si = stream_index(nstreams);
   if (si < 0) return set_error(AERORT_RC_UNSUPPORTED, "set_kernel: nstreams must be one of 4, 6, 8, 12, 16");
@@ -576,24 +606,42 @@ extern "C" int aerort_get_schedule(int nstreams, int precision, int* threads_per
 namespace {
 template <typename T>
 int dispatch_fixed_t(int nstreams, const RtOptions& opt, const LambertInputs& in, void* arena, size_t bytes, int* sched,
-                     int num_sms, const Schedule& sc, double* r, double* f, int* nf, int* st, cudaStream_t s) {
+                     int num_sms, const Schedule& sc, double* r, double* f, int* nf, int* st, cudaStream_t s,
+                     const Worklist& wl) {
   switch (nstreams) {
-    case 4: return launch_scalar_lambert_fixed<4, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
-    case 6: return launch_scalar_lambert_fixed<6, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
-    case 8: return launch_scalar_lambert_fixed<8, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
-    case 12: return launch_scalar_lambert_fixed<12, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
-    case 16: return launch_scalar_lambert_fixed<16, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+    case 4: return launch_scalar_lambert_fixed<4, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s, wl);
+    case 6: return launch_scalar_lambert_fixed<6, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s, wl);
+    case 8: return launch_scalar_lambert_fixed<8, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s, wl);
+    case 12: return launch_scalar_lambert_fixed<12, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s, wl);
+    case 16: return launch_scalar_lambert_fixed<16, T>(opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s, wl);
   }
   return set_error(AERORT_RC_UNSUPPORTED, "nstreams must be one of 4, 6, 8, 12, 16");
 }
+// On fixed storage the refinement list of the mixed method takes the first
+// bytes of the arena (4 per solve) and its count the third scheduling int.
 int dispatch_fixed(int precision, int nstreams, const RtOptions& opt, const LambertInputs& in, void* arena,
-                   size_t bytes, int* sched, int num_sms, const Schedule& sc, double* r, double* f, int* nf, int* st,
-                   cudaStream_t s) {
-  if (precision == AERORT_PREC_MIXED)
-    return dispatch_fixed_t<float>(nstreams, opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
+                   size_t bytes, int* sched, int num_sms, const Schedule& sc, const Schedule& sc64, double* r,
+                   double* f, int* nf, int* st, cudaStream_t s) {
   if (precision == AERORT_PREC_FP64)
-    return dispatch_fixed_t<double>(nstreams, opt, in, arena, bytes, sched, num_sms, sc, r, f, nf, st, s);
-  return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
+    return dispatch_fixed_t<double>(nstreams, opt, in, arena, bytes, sched, num_sms, sc64, r, f, nf, st, s,
+                                    Worklist());
+  if (precision != AERORT_PREC_MIXED)
+    return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
+  const size_t list_bytes = (sizeof(int) * ((size_t)in.nobs * in.nch + 1) + 255) / 256 * 256;
+  if (bytes <= list_bytes) return set_error(AERORT_RC_ARG, "workspace too small for the refinement list");
+  Worklist wm;
+  wm.out_list = (int*)arena;
+  wm.out_count = sched + 2;
+  wm.ratio = kRefineRatio;
+  void* rest = (char*)arena + list_bytes;
+  if (int rc = dispatch_fixed_t<float>(nstreams, opt, in, rest, bytes - list_bytes, sched, num_sms, sc, r, f, nf, st,
+                                       s, wm))
+    return rc;
+  Worklist wd;
+  wd.in_list = (const int*)arena;
+  wd.in_count = sched + 2;
+  return dispatch_fixed_t<double>(nstreams, opt, in, rest, bytes - list_bytes, sched, num_sms, sc64, r, f, nf, st, s,
+                                  wd);
 }
 }  // namespace
 
@@ -656,17 +704,20 @@ extern "C" int aerort_vlidort_scalar_lambert_ws_dev(
   if ((!tau_f && (!tau || !ssa || !pmom)) || (tau_f && (!ssa_f || !pmom_f)))
     return set_error(AERORT_RC_ARG, "scalar_lambert_ws_dev: optics missing");
   if ((long)nobs * nch > 0x7fffff00L) return set_error(AERORT_RC_ARG, "scalar_lambert_ws_dev: nobs * nch too large");
-  Schedule sc;
+  Schedule sc, sc64;
   {
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
     const int si = stream_index(nstreams);
-    if (si >= 0 && (precision == AERORT_PREC_FP64 || precision == AERORT_PREC_MIXED)) sc = c.sched[precision][si];
+    if (si >= 0 && (precision == AERORT_PREC_FP64 || precision == AERORT_PREC_MIXED)) {
+      sc = c.sched[precision][si];
+      sc64 = c.sched[AERORT_PREC_FP64][si];
+    }
   }
   LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
                    sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
   return dispatch_fixed(precision, nstreams, lambert_options(plane_parallel), in, ws->arena, ws->bytes, ws->sched,
-                        ws->num_sms, sc, radiance_VL, reflectance_VL, nfourier, status, (cudaStream_t)stream);
+                        ws->num_sms, sc, sc64, radiance_VL, reflectance_VL, nfourier, status, (cudaStream_t)stream);
 }
 
 extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
@@ -694,7 +745,7 @@ extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
     if (si >= 0) sc.kernel = c.sched[AERORT_PREC_FP64][si].kernel;
   }
   return dispatch_fixed(AERORT_PREC_FP64, nstreams, lambert_options(plane_parallel), in, arena,
-                        arena_doubles * sizeof(double), sched, num_sms, sc, radiance_VL, reflectance_VL, nfourier,
+                        arena_doubles * sizeof(double), sched, num_sms, sc, sc, radiance_VL, reflectance_VL, nfourier,
                         status, (cudaStream_t)stream);
 }
 

@@ -48,7 +48,7 @@ struct Context {
   bool init = false;
   int device = -1, num_sms = 0;
   cudaStream_t stream = nullptr;
-  DevBuf scratch, counter, stage[24];
+  DevBuf scratch, counter, redo, stage[24];
   Schedule sched[2][5];  // [precision][stream index]
   Context() {
     // measured on GB300: the team kernel wins at 6, 12 and 16 streams in the
@@ -74,15 +74,15 @@ struct Quad {
 
 template <int NS, typename T>
 int launch_scalar_lambert(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
-                          double* refl, int* nf, int* st, cudaStream_t s);
+                          double* refl, int* nf, int* st, cudaStream_t s, const aerort::Worklist& wl);
 
 template <int NS, typename T>
 int launch_scalar_lambert_team(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
-                               double* refl, int* nf, int* st, cudaStream_t s);
+                               double* refl, int* nf, int* st, cudaStream_t s, const aerort::Worklist& wl);
 template <int NS, typename T>
 int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::LambertInputs& in, void* arena,
                                 size_t arena_bytes, int* sched, int num_sms, const Schedule& sc, double* rad,
-                                double* refl, int* nf, int* st, cudaStream_t s);
+                                double* refl, int* nf, int* st, cudaStream_t s, const aerort::Worklist& wl);
 
 // Static device arena of the allocation-free entry point (rt_static.cu):
 // address of the calling thread's current device's copy, set up on first use.

@@ -12,23 +12,25 @@ using namespace aerort;
 // solar zenith is exactly 0 and that has at least one valid albedo.
 __global__ void k_nadir_first(int nobs, int nch, const double* sza, const double* raa, const double* vza,
                               const double* albedo, double missing, int* first);
-// counter <- 0, first <- nobs (device-side, so launches need no host staging)
-__global__ void k_init_sched(int* counter, int* first, int nobs);
+// counter <- 0, first <- nobs, *zero <- 0 when given (device-side, so launches
+// need no host staging)
+__global__ void k_init_sched(int* counter, int* first, int nobs, int* zero);
 
 template <int NS, typename T>
 __global__ void __launch_bounds__(128) k_scalar_lambert(RtOptions opt, LambertInputs in, Quad q, void* scratch,
                                                         long nthreads, int nsolve, int* counter, double* rad,
-                                                        double* refl, int* nf, int* st) {
+                                                        double* refl, int* nf, int* st, Worklist wl) {
   const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const SolveScratch<T> S = make_scratch<NS, T>(scratch, tid, nthreads, in.km);
   const int lane = threadIdx.x & 31;
+  const int n = wl.count(nsolve);
   for (;;) {
     int base = 0;
     if (lane == 0) base = atomicAdd(counter, 32);
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= nsolve) break;
+    if (base >= n) break;
     const int s = base + lane;
-    if (s < nsolve) solve_lambert<NS, T>(opt, in, s, q.qx, q.qw, q.tu, q.wu, S, rad, refl, nf, st);
+    if (s < n) solve_lambert<NS, T>(opt, in, wl.solve(s), q.qx, q.qw, q.tu, q.wu, S, rad, refl, nf, st, wl);
     __syncwarp();
   }
 }
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(32 * WPB) k_scalar_lambert_team(RtOptions opt,
                                                                    void* scratch, long nthreads, T* sweep,
                                                                    long sweep_per_warp, int nsolve, int chunk,
                                                                    int* counter, double* rad, double* refl, int* nf,
-                                                                   int* st) {
+                                                                   int* st, Worklist wl) {
   extern __shared__ __align__(16) unsigned char team_smem[];
   const int lane = threadIdx.x & 31;
   TeamMem<NS, T>& M = reinterpret_cast<TeamMem<NS, T>*>(team_smem)[threadIdx.x >> 5];
@@ -69,16 +71,19 @@ __global__ void __launch_bounds__(32 * WPB) k_scalar_lambert_team(RtOptions opt,
   const ScratchLayout<NS> lay(in.km, false);
   const SolveScratch<T> S = make_scratch<NS, T>(scratch, tid, nthreads, in.km, false);
   const Team tm{lane, nullptr, nullptr};
+  const int n = wl.count(nsolve);
   for (;;) {
     int base = 0;
     if (lane == 0) base = atomicAdd(counter, chunk);
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= nsolve) break;
+    if (base >= n) break;
     const int s = base + lane;
     bool live = false;
-    if (lane < chunk && s < nsolve) {
+    int sidx = 0;
+    if (lane < chunk && s < n) {
+      sidx = wl.solve(s);
       SetupRecord r;
-      live = solve_setup<NS, T>(opt, in, s, q.tu, q.wu, S, rad, refl, nf, st, r);
+      live = solve_setup<NS, T>(opt, in, sidx, q.tu, q.wu, S, rad, refl, nf, st, r);
       if (live) r.store(S.D, lay.rec);
     }
     unsigned mask = __ballot_sync(0xffffffffu, live);
@@ -89,14 +94,15 @@ __global__ void __launch_bounds__(32 * WPB) k_scalar_lambert_team(RtOptions opt,
       const SolveScratch<T> Sb = make_scratch<NS, T>(scratch, tid0 + b, nthreads, in.km, false);
       SetupRecord rb;
       rb.load(Sb.D, lay.rec);
-      team_fourier_series<NS, T>(tm, M, opt, in, rb, q.qx, q.qw, Sb.W, lay, sw, rad, refl, nf, st);
+      const int sb = __shfl_sync(0xffffffffu, sidx, b);
+      team_fourier_series<NS, T>(tm, M, opt, in, rb, q.qx, q.qw, Sb.W, lay, sw, rad, refl, nf, st, wl, sb);
     }
   }
 }
 
 template <int NS, typename T>
 int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
-                               int* nf, int* st, cudaStream_t s) {
+                               int* nf, int* st, cudaStream_t s, const Worklist& wl) {
   constexpr int WPB = 2;
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
@@ -114,7 +120,11 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   const Schedule& sc = c.sched[sizeof(T) == sizeof(float) ? 1 : 0][stream_index(NS)];
   if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
   long nblocks = 0;
-  const int chunk = team_chunk(nsolve, (long)per_sm * c.num_sms, WPB, &nblocks);
+  // a refinement pass (solve list) holds few solves: one per warp grab
+  const int chunk = wl.in_list ? team_chunk(1, (long)per_sm * c.num_sms, WPB, &nblocks)
+                               : team_chunk(nsolve, (long)per_sm * c.num_sms, WPB, &nblocks);
+  if (wl.in_list) nblocks = (long)per_sm * c.num_sms < (nsolve + WPB - 1) / WPB ? (long)per_sm * c.num_sms
+                                                                                : (nsolve + WPB - 1) / WPB;
   const long nthreads = nblocks * bs;
   const ScratchLayout<NS> lay(in.km, false);
   const SweepLayout<NS> swl(in.km);
@@ -122,10 +132,10 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   const size_t sweep_off = (thread_bytes + 255) / 256 * 256;
   const size_t sweep_bytes = sizeof(T) * (size_t)swl.total * (nthreads / 32);
   if (int rc = c.scratch.ensure(sweep_off + sweep_bytes)) return rc;
-  if (int rc = c.counter.ensure(2 * sizeof(int))) return rc;
+  if (int rc = c.counter.ensure(4 * sizeof(int))) return rc;
   int* counter = (int*)c.counter.p;
   int* first = counter + 1;
-  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
   k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
                                                        first);
   CUDA_TRY(cudaGetLastError());
@@ -134,14 +144,14 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   T* sweep = (T*)((char*)c.scratch.p + sweep_off);
   k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(opt, in2, q, c.scratch.p, nthreads, sweep,
                                                                         swl.total, nsolve, chunk, counter, rad, refl,
-                                                                        nf, st);
+                                                                        nf, st, wl);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
 
 template <int NS, typename T>
 int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
-                          int* nf, int* st, cudaStream_t s) {
+                          int* nf, int* st, cudaStream_t s, const Worklist& wl) {
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
   Quad q;
@@ -154,22 +164,23 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   if (per_sm < 1) per_sm = 1;
   if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
   long maxblocks = (long)per_sm * c.num_sms;
+  if (wl.in_list && maxblocks > (64L * c.num_sms + bs - 1) / bs) maxblocks = (64L * c.num_sms + bs - 1) / bs;
   long nblocks = (nsolve + bs - 1) / bs;
   if (nblocks > maxblocks) nblocks = maxblocks;
   const long nthreads = nblocks * bs;
   const ScratchLayout<NS> lay(in.km);
   if (int rc = c.scratch.ensure((size_t)lay.template bytes<T>() * nthreads)) return rc;
-  if (int rc = c.counter.ensure(2 * sizeof(int))) return rc;
+  if (int rc = c.counter.ensure(4 * sizeof(int))) return rc;
   int* counter = (int*)c.counter.p;
   int* first = counter + 1;
-  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
   k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
                                                        first);
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
   k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, c.scratch.p, nthreads, nsolve, counter,
-                                                           rad, refl, nf, st);
+                                                           rad, refl, nf, st, wl);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -182,7 +193,7 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
 template <int NS, typename T>
 int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, void* arena, size_t arena_bytes,
                                 int* sched, int num_sms, const Schedule& sc, double* rad, double* refl, int* nf,
-                                int* st, cudaStream_t s) {
+                                int* st, cudaStream_t s, const Worklist& wl) {
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
   if (sc.kernel == 1) {
@@ -208,12 +219,13 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
     long resident = (long)per_sm * num_sms;
     if (resident > fit_blocks_t) resident = fit_blocks_t;
     long nblocks = 0;
-    const int chunk = team_chunk(nsolve, resident, WPB, &nblocks);
+    const int chunk = team_chunk(wl.in_list ? 1 : nsolve, resident, WPB, &nblocks);
+    if (wl.in_list) nblocks = resident < (nsolve + WPB - 1) / WPB ? resident : (nsolve + WPB - 1) / WPB;
     const long nthreads = nblocks * 32 * WPB;
     const size_t sweep_off = ((size_t)tlay.template bytes<T>() * nthreads + 255) / 256 * 256;
     int* counter = sched;
     int* first = sched + 1;
-    k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+    k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
     k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo,
                                                          in.missing, first);
     CUDA_TRY(cudaGetLastError());
@@ -221,7 +233,7 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
     in2.nadir_first = first;
     k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, 32 * WPB, smem, s>>>(
         opt, in2, q, arena, nthreads, (T*)((char*)arena + sweep_off), swl.total, nsolve, chunk, counter, rad, refl,
-        nf, st);
+        nf, st, wl);
     CUDA_TRY(cudaGetLastError());
     return 0;
   }
@@ -244,14 +256,14 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
   const long nthreads = nblocks * bs;
   int* counter = sched;
   int* first = sched + 1;
-  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs);
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
   k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
                                                        first);
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
   k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, arena, nthreads, nsolve, counter, rad, refl,
-                                                           nf, st);
+                                                           nf, st, wl);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -261,19 +273,19 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
 #define AERORT_INSTANTIATE_RT(NS)                                                                             \
   template int aerort_internal::launch_scalar_lambert<NS, double>(                                             \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
-      int*, cudaStream_t);                                                                                      \
+      int*, cudaStream_t, const aerort::Worklist&);                                                                                      \
   template int aerort_internal::launch_scalar_lambert<NS, float>(                                              \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
-      int*, cudaStream_t);                                                                                      \
+      int*, cudaStream_t, const aerort::Worklist&);                                                                                      \
   template int aerort_internal::launch_scalar_lambert_team<NS, double>(                                        \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
-      int*, cudaStream_t);                                                                                      \
+      int*, cudaStream_t, const aerort::Worklist&);                                                                                      \
   template int aerort_internal::launch_scalar_lambert_team<NS, float>(                                         \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
-      int*, cudaStream_t);                                                                                      \
+      int*, cudaStream_t, const aerort::Worklist&);                                                                                      \
   template int aerort_internal::launch_scalar_lambert_fixed<NS, double>(                                       \
       const aerort::RtOptions&, const aerort::LambertInputs&, void*, size_t, int*, int,                         \
-      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t);                            \
+      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t, const aerort::Worklist&);                            \
   template int aerort_internal::launch_scalar_lambert_fixed<NS, float>(                                        \
       const aerort::RtOptions&, const aerort::LambertInputs&, void*, size_t, int*, int,                         \
-      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t);
+      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t, const aerort::Worklist&);

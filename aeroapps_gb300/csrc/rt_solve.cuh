@@ -103,6 +103,7 @@ struct SolveCtx {
   T qx[NS], qw[NS], sqw[NS];
   T mu_u, sec_u, cos_sza, albedo, trans_solar_beam;
   T pimm_q[NS], pimm_u, pimm_0;  // normalised P_m^m carried across Fourier terms
+  T sin_q[NS], sin_u, sin_0;     // sqrt(1 - x^2) of the cosines, formed in FP64
 };
 
 // Homogeneous + particular solution of one layer for one Fourier term.
@@ -137,11 +138,12 @@ struct LegendreCoef {
 // l = m..NM, zero below m.  The normalised recursion never forms the
 // factorials, so it is safe in FP32.  pim carries P~_m^m from term m-1 to m:
 // the calls for one x must come in the order m = 0, 1, 2, ...
+// s = sqrt(1 - x^2), formed in FP64 by the caller (in FP32 the difference
+// 1 - x^2 loses its digits at near-nadir view or sun).
 template <int NS, typename T>
-RT_HD void legendre_m(int m, int NM, const LegendreCoef<NS, T>& lc, T x, T* pim, T* out) {
+RT_HD void legendre_m(int m, int NM, const LegendreCoef<NS, T>& lc, T x, T s, T* pim, T* out) {
   for (int l = 0; l < m && l <= NM; ++l) out[l] = 0;
   if (m > NM) return;
-  const T s = (x == (T)1) ? (T)0 : sqrt((T)1 - x * x);
   T pmm = (m == 0) ? (T)1 : *pim * s * sqrt((T)(2 * m - 1) / (T)(2 * m));
   *pim = pmm;
   out[m] = pmm;
@@ -524,9 +526,9 @@ RT_HD int fourier_term(SolveCtx<NS, T>& c, const RtOptions& opt, int m, const Sc
   {
     LegendreCoef<NS, T> lc;
     lc.init(m, NM);
-    for (int i = 0; i < N; ++i) legendre_m<NS, T>(m, NM, lc, c.qx[i], &c.pimm_q[i], &piq[2 * NS * i]);
-    legendre_m<NS, T>(m, NM, lc, c.mu_u, &c.pimm_u, piu);
-    legendre_m<NS, T>(m, NM, lc, c.cos_sza, &c.pimm_0, pi0);
+    for (int i = 0; i < N; ++i) legendre_m<NS, T>(m, NM, lc, c.qx[i], c.sin_q[i], &c.pimm_q[i], &piq[2 * NS * i]);
+    legendre_m<NS, T>(m, NM, lc, c.mu_u, c.sin_u, &c.pimm_u, piu);
+    legendre_m<NS, T>(m, NM, lc, c.cos_sza, c.sin_0, &c.pimm_0, pi0);
   }
 
   LayerSol<NS, T> A, B;
@@ -1066,10 +1068,14 @@ struct SetupRecord {
 template <int NS, typename T>
 RT_HD void make_ctx(const SetupRecord& r, const double* qx, const double* qw, SolveCtx<NS, T>& c) {
   c.L = r.L; c.NM = r.NM; c.cutoff = r.cutoff; c.msmode = r.msmode; c.refl_directbeam = r.refl_directbeam;
+  auto sine = [](double x) { return (x == 1.0) ? 0.0 : sqrt(1.0 - x * x); };
   for (int q = 0; q < NS; ++q) {
     c.qx[q] = (T)qx[q]; c.qw[q] = (T)qw[q]; c.sqw[q] = (T)sqrt(qw[q]); c.pimm_q[q] = 0;
+    c.sin_q[q] = (T)sine(qx[q]);
   }
   c.pimm_u = 0; c.pimm_0 = 0;
+  c.sin_u = (T)sine(r.mu_u);
+  c.sin_0 = (T)sine(r.cos_sza);
   c.mu_u = (T)r.mu_u; c.sec_u = (T)r.sec_u; c.cos_sza = (T)r.cos_sza; c.albedo = (T)r.albedo;
   c.trans_solar_beam = (T)r.trans_solar_beam;
 }
@@ -1079,14 +1085,20 @@ RT_HD void make_ctx(const SetupRecord& r, const double* qx, const double* qw, So
 // the series has converged after term m.
 struct FourierSum {
   double stokes = 0.0;
+  double sumabs = 0.0;  // sum of |contributions|: |stokes| / sumabs measures the cancellation
   int testconv = 0;
   RT_HD bool add(const RtOptions& opt, const SetupRecord& r, int m, double sf) {
     if (m == 0) {
       stokes = sf;
-      if (opt.do_focorr) stokes += r.ss + r.db;
+      sumabs = fabs(sf);
+      if (opt.do_focorr) {
+        stokes += r.ss + r.db;
+        sumabs += fabs(r.ss) + fabs(r.db);
+      }
       return false;
     }
     double tazm = cos(r.raa * (double)m * kDTR) * sf;
+    sumabs += fabs(tazm);
     double tnew = stokes + tazm;
     bool conv = (tazm != 0.0) ? (fabs(tazm / tnew) < opt.accuracy) : true;
     stokes = tnew;
@@ -1099,6 +1111,33 @@ struct FourierSum {
     return false;
   }
 };
+
+// Which solves a launch runs and which it hands on.  in_list (device, length
+// *in_count): run only these solve indices (the FP64 refinement pass);
+// out_list: append every solve whose Fourier sum cancels by more than `ratio`
+// (sum |terms| > ratio |radiance|), so that the FP64 pass re-solves it.  The
+// mixed method's terms carry ~1e-6 relative FP32 error each; a radiance that
+// is a near-cancellation of much larger terms would inherit it amplified.
+struct Worklist {
+  const int* in_list = nullptr;
+  const int* in_count = nullptr;
+  int* out_list = nullptr;
+  int* out_count = nullptr;
+  double ratio = 0.0;
+  RT_HD int count(int nsolve) const { return in_list ? *in_count : nsolve; }
+  RT_HD int solve(int s) const { return in_list ? in_list[s] : s; }
+  RT_HD void flag(const FourierSum& sum, int st, int sidx) const {
+    if (!out_list || st != RT_OK || !(sum.sumabs > ratio * fabs(sum.stokes))) return;
+#ifdef __CUDA_ARCH__
+    const int pos = atomicAdd(out_count, 1);
+#else
+    const int pos = (*out_count)++;
+#endif
+    out_list[pos] = sidx;
+  }
+};
+// Cancellation ratio above which a mixed-method radiance is re-solved in FP64.
+constexpr double kRefineRatio = 10.0;
 
 // Outputs of a finished series (status RT_OK) or of a failed term.
 RT_HD void solve_finish(const RtOptions& opt, const LambertInputs& in, const SetupRecord& r, int st, int m,
@@ -1554,7 +1593,8 @@ RT_HD void fo_enhanced_f32(const RtOptions& opt, int L, double sza, double vza, 
 template <int NS, typename T>
 RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sidx, const double* qx,
                           const double* qw, const double* tu, const double* wu, const SolveScratch<T>& SS,
-                          double* radiance, double* reflectance, int* nfourier, int* status) {
+                          double* radiance, double* reflectance, int* nfourier, int* status,
+                          const Worklist& wl = Worklist()) {
   SetupRecord r;
   if (!solve_setup<NS, T>(opt, in, sidx, tu, wu, SS, radiance, reflectance, nfourier, status, r)) return;
   const ScratchLayout<NS> lay(in.km);
@@ -1568,6 +1608,7 @@ RT_HDN void solve_lambert(const RtOptions& opt, const LambertInputs& in, int sid
     if (st != RT_OK || sum.add(opt, r, m, (double)sf)) break;
   }
   solve_finish(opt, in, r, st, m, sum.stokes, radiance, reflectance, nfourier, status);
+  wl.flag(sum, st, sidx);
 }
 
 }  // namespace aerort

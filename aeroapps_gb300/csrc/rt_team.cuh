@@ -287,13 +287,12 @@ RT_HD void team_legendre(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T
   tm.sync();
   const int i = tm.lane;
   if (i < NS + 2) {
-    T x, *pim, *out;
-    if (i < NS) { x = c.qx[i]; pim = &M.pimq[i]; out = M.piq[i]; }
-    else if (i == NS) { x = c.mu_u; pim = &M.pimu; out = M.piu; }
-    else { x = c.cos_sza; pim = &M.pim0; out = M.pi0; }
+    T x, s, *pim, *out;
+    if (i < NS) { x = c.qx[i]; s = c.sin_q[i]; pim = &M.pimq[i]; out = M.piq[i]; }
+    else if (i == NS) { x = c.mu_u; s = c.sin_u; pim = &M.pimu; out = M.piu; }
+    else { x = c.cos_sza; s = c.sin_0; pim = &M.pim0; out = M.pi0; }
     for (int l = 0; l < m && l <= NM; ++l) out[l] = 0;
     if (m <= NM) {
-      const T s = (x == (T)1) ? (T)0 : sqrt((T)1 - x * x);
       const T pmm = (m == 0) ? (T)1 : *pim * s * sqrt((T)(2 * m - 1) / (T)(2 * m));
       *pim = pmm;
       out[m] = pmm;
@@ -787,7 +786,7 @@ template <int NS, typename T>
 RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOptions& opt, const LambertInputs& in,
                                const SetupRecord& r, const double* qx, const double* qw, const ScratchT<T>& W,
                                const ScratchLayout<NS>& lay, T* sw, double* radiance, double* reflectance,
-                               int* nfourier, int* status) {
+                               int* nfourier, int* status, const Worklist& wl = Worklist(), int sidx = 0) {
   SolveCtx<NS, T> c;
   make_ctx<NS, T>(r, qx, qw, c);
   if (tm.lane < NS) M.pimq[tm.lane] = 0;
@@ -801,7 +800,10 @@ RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOption
     st = team_fourier_term<NS, T>(tm, M, c, opt, m, W, lay, sw, swl, &sf);
     if (st != RT_OK || sum.add(opt, r, m, (double)sf)) break;
   }
-  if (tm.lane == 0) solve_finish(opt, in, r, st, m, sum.stokes, radiance, reflectance, nfourier, status);
+  if (tm.lane == 0) {
+    solve_finish(opt, in, r, st, m, sum.stokes, radiance, reflectance, nfourier, status);
+    wl.flag(sum, st, sidx);
+  }
   tm.sync();
 }
 

@@ -148,8 +148,11 @@ int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstre
  * one-sided Jacobi on a graded factor (k to relative accuracy), the
  * conservative mode of Fourier term 0 split off exactly, and the
  * Green's-function multipliers as divided differences of exp(-x tau).
- * Radiance error against the FP64 method: <= 1e-5 on the synthetic configs,
- * <= 1e-4 with layer SSA in [0.999, 1). */
+ * A radiance whose Fourier sum cancels (sum of |terms| > 10 |radiance|, e.g.
+ * unconverged series near backscatter) would inherit the FP32 term error
+ * amplified; such solves are listed on the device and re-solved in FP64 by a
+ * second launch on the same stream.  Radiance error against the FP64 method:
+ * <= 1e-5 on the synthetic configs, <= 1e-4 with layer SSA in [0.999, 1). */
 int aerort_vlidort_scalar_lambert_mixed_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel,
                                                   int nMom, const int* nlay, const double* ROT, const double* depol,
                                                   const double* tau, const double* ssa, const double* pmom,
@@ -188,6 +191,11 @@ int aerort_vlidort_scalar_lambert_ws_dev(aerort_workspace* ws, int precision, in
                                          const double* solar_zenith, const double* relat_azymuth,
                                          const double* sensor_zenith, double MISSING, double* radiance_VL,
                                          double* reflectance_VL, int* nfourier, int* status, void* stream);
+
+/* Number of solves the last mixed call through the library's batched entry
+ * points re-solved in FP64 (synchronises `stream`).  No counterpart in the
+ * reference. */
+int aerort_refined_count(void* stream, int* count);
 
 /* Launch schedule of the RT kernel per (stream count, precision): threads per
  * block (32, 64, 96 or 128) and resident blocks per SM (0 = occupancy limit).

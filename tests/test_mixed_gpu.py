@@ -124,3 +124,35 @@ def test_schedule_api_validates():
     assert L.aerort_get_schedule(8, 1, ctypes.byref(t), ctypes.byref(b)) == 0
     assert (t.value, b.value) == (96, 2)
     assert L.aerort_set_schedule(8, 1, 32, 0) == 0
+
+
+@pytest.mark.gpu
+def test_cancelling_fourier_sum_is_refined_in_fp64():
+    # a 4-stream column near backscatter (relative azimuth 173 deg) whose 670 nm
+    # radiance is a 60x cancellation of its Fourier terms: the mixed method
+    # lists it and re-solves it in FP64 (aerort_refined_count >= 1)
+    import ctypes
+    import torch
+    import bench
+    full = bench.make_batch(8192, seed=20261204)
+    g = bench.subset(full, np.array([3167, 3168, 3169]))
+    N = int(g["nstreams"][0])
+    assert N == 4
+    tabs = mie.generate_tables(CH, nmom=32)
+    chem = mie.ChemMie(tabs)
+    qt, qb = zip(*[chem.query_idx(x) for x in synth.tracer_names()])
+    chem.destroy()
+    km, n = g["km"], 3
+    nl = np.ascontiguousarray(g["nlayers"], np.int32)
+    tau, ssa, gg, pm, rc = oracle.get_aop_vector(tabs, km, n, 4, 20, np.float32(CH), qt, qb, g["qm"], g["rh"], 2 * N, 1)
+    orad = oracle.scalar_lambert(km, 4, n, np.array(CH), N, 0, 2 * N, 1, g["ROT"], g["depol"], tau, ssa, gg, pm, g["pe"],
+                                 g["he"], g["te"], g["albedo"], g["sza"], g["raa"], g["vza"], MISSING, nlay=nl)[0]
+    rad, _, rc, _, st = vlidort.vlidort_scalar_lambert_batch(
+        km, 4, n, N, 2 * N, nl, g["ROT"], g["depol"], tau.astype(np.float64), ssa.astype(np.float64),
+        pm[..., 0].astype(np.float64), g["he"], g["albedo"], g["sza"], g["raa"], g["vza"], MISSING=MISSING,
+        precision="mixed")
+    cnt = ctypes.c_int()
+    assert _lib.lib().aerort_refined_count(torch.cuda.current_stream().cuda_stream, ctypes.byref(cnt)) == 0
+    assert rc == 0 and np.all(st == 0)
+    assert cnt.value >= 1
+    assert np.max(np.abs(rad / orad - 1.0)) <= RTOL
