@@ -71,6 +71,7 @@ PREC_FP64 = 0
 PREC_MIXED = 1
 KERNEL_THREAD = 0
 KERNEL_TEAM = 1
+KERNEL_AUTO = 2
 
 
 def library_path():

@@ -60,12 +60,50 @@ int Context::setup() {
 }
 
 void Context::release() {
-  scratch.release();
-  counter.release();
+  for (auto& p : pads) {
+    p.scratch.release();
+    p.counter.release();
+    p.redo.release();
+    if (p.done) cudaEventDestroy(p.done);
+    p = Pad();
+  }
+  pad = nullptr;
   for (auto& b : stage) b.release();
   if (stream) cudaStreamDestroy(stream);
   stream = nullptr;
   init = false;
+}
+
+Pad* Context::find(cudaStream_t s) {
+  for (auto& p : pads)
+    if (p.used && p.owner == s) return &p;
+  return nullptr;
+}
+
+int Context::bind(cudaStream_t s) {
+  Pad* p = find(s);
+  if (!p) {
+    for (auto& q : pads)
+      if (!q.used) { p = &q; break; }
+    if (!p) {  // all taken: the least recently used one
+      p = &pads[0];
+      for (auto& q : pads)
+        if (q.last < p->last) p = &q;
+    }
+    if (!p->done) CUDA_TRY(cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming));
+    if (p->used) CUDA_TRY(cudaStreamWaitEvent(s, p->done, 0));
+    p->owner = s;
+    p->used = true;
+  }
+  p->last = ++tick;
+  pad = p;
+  return 0;
+}
+
+int Context::unbind(cudaStream_t s) {
+  if (pad) CUDA_TRY(cudaEventRecord(pad->done, s));
+  pad = nullptr;
+  return 0;
 }
 
 Context& ctx() {
@@ -433,7 +471,9 @@ template <typename T>
 int dispatch_lambert_t(Context& c, int nstreams, const RtOptions& opt, const LambertInputs& in, double* rad,
                        double* refl, int* nf, int* st, cudaStream_t s, const Worklist& wl) {
   const int si = stream_index(nstreams);
-  if (si >= 0 && c.sched[sizeof(T) == sizeof(float) ? 1 : 0][si].kernel == 1) {
+  const int prec = sizeof(T) == sizeof(float) ? AERORT_PREC_MIXED : AERORT_PREC_FP64;
+  if (si >= 0 && resolve_kernel(c.sched[prec][si].kernel, prec, si, (long)in.nobs * in.nch, c.num_sms,
+                                wl.in_list != nullptr) == 1) {
     switch (nstreams) {
       case 4: return launch_scalar_lambert_team<4, T>(c, opt, in, rad, refl, nf, st, s, wl);
       case 6: return launch_scalar_lambert_team<6, T>(c, opt, in, rad, refl, nf, st, s, wl);
@@ -456,25 +496,34 @@ int dispatch_lambert_t(Context& c, int nstreams, const RtOptions& opt, const Lam
 // solve, which lists the solves whose Fourier sum cancels by more than
 // kRefineRatio, then the FP64 series for the listed solves only (their outputs
 // overwrite the mixed ones).  The list and its count stay on the device.
-int dispatch_lambert(Context& c, int precision, int nstreams, const RtOptions& opt, const LambertInputs& in,
-                     double* rad, double* refl, int* nf, int* st, cudaStream_t s) {
+int dispatch_lambert_on_pad(Context& c, int precision, int nstreams, const RtOptions& opt, const LambertInputs& in,
+                            double* rad, double* refl, int* nf, int* st, cudaStream_t s) {
   if (precision == AERORT_PREC_FP64)
     return dispatch_lambert_t<double>(c, nstreams, opt, in, rad, refl, nf, st, s, Worklist());
   if (precision != AERORT_PREC_MIXED)
     return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
   const int nsolve = in.nobs * in.nch;
-  if (int rc = c.redo.ensure(sizeof(int) * ((size_t)nsolve + 1))) return rc;
-  if (int rc = c.counter.ensure(4 * sizeof(int))) return rc;
-  int* count = (int*)c.counter.p + 2;
+  Pad& p = *c.pad;
+  if (int rc = p.redo.ensure(sizeof(int) * ((size_t)nsolve + 1))) return rc;
+  if (int rc = p.counter.ensure(4 * sizeof(int))) return rc;
+  int* count = (int*)p.counter.p + 2;
   Worklist wm;
-  wm.out_list = (int*)c.redo.p;
+  wm.out_list = (int*)p.redo.p;
   wm.out_count = count;
   wm.ratio = kRefineRatio;
   if (int rc = dispatch_lambert_t<float>(c, nstreams, opt, in, rad, refl, nf, st, s, wm)) return rc;
   Worklist wd;
-  wd.in_list = (const int*)c.redo.p;
+  wd.in_list = (const int*)p.redo.p;
   wd.in_count = count;
   return dispatch_lambert_t<double>(c, nstreams, opt, in, rad, refl, nf, st, s, wd);
+}
+
+int dispatch_lambert(Context& c, int precision, int nstreams, const RtOptions& opt, const LambertInputs& in,
+                     double* rad, double* refl, int* nf, int* st, cudaStream_t s) {
+  if (int rc = c.bind(s)) return rc;
+  const int rc = dispatch_lambert_on_pad(c, precision, nstreams, opt, in, rad, refl, nf, st, s);
+  const int rc2 = c.unbind(s);
+  return rc ? rc : rc2;
 }
 
 int lambert_checks(int km, int nch, int nobs, int nstreams, int nMom) {
@@ -564,8 +613,9 @@ extern "C" int aerort_refined_count(void* stream, int* count) {
   Context& c = ctx();
   std::lock_guard<std::mutex> lk(c.mu);
   *count = 0;
-  if (!c.counter.p || c.counter.bytes < 4 * sizeof(int)) return AERORT_OK;
-  CUDA_TRY(cudaMemcpyAsync(count, (int*)c.counter.p + 2, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  Pad* p = c.find((cudaStream_t)stream);
+  if (!p || !p->counter.p || p->counter.bytes < 4 * sizeof(int)) return AERORT_OK;
+  CUDA_TRY(cudaMemcpyAsync(count, (int*)p->counter.p + 2, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
   CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
   return AERORT_OK;
 }
@@ -574,7 +624,7 @@ extern "C" int aerort_set_kernel(int nstreams, int precision, int kernel) {
   const int si = stream_index(nstreams);
   if (si < 0) return set_error(AERORT_RC_UNSUPPORTED, "set_kernel: nstreams must be one of 4, 6, 8, 12, 16");
   if ((precision != AERORT_PREC_FP64 && precision != AERORT_PREC_MIXED) ||
-      (kernel != AERORT_KERNEL_THREAD && kernel != AERORT_KERNEL_TEAM))
+      (kernel != AERORT_KERNEL_THREAD && kernel != AERORT_KERNEL_TEAM && kernel != AERORT_KERNEL_AUTO))
     return set_error(AERORT_RC_ARG, "set_kernel: bad precision or kernel");
   Context& c = ctx();
   std::lock_guard<std::mutex> lk(c.mu);
@@ -622,8 +672,14 @@ int dispatch_fixed_t(int nstreams, const RtOptions& opt, const LambertInputs& in
 int dispatch_fixed(int precision, int nstreams, const RtOptions& opt, const LambertInputs& in, void* arena,
                    size_t bytes, int* sched, int num_sms, const Schedule& sc, const Schedule& sc64, double* r,
                    double* f, int* nf, int* st, cudaStream_t s) {
+  const int si = stream_index(nstreams);
+  const long nsolve = (long)in.nobs * in.nch;
+  Schedule s32 = sc, s64 = sc64, s64_list = sc64;
+  s32.kernel = resolve_kernel(sc.kernel, AERORT_PREC_MIXED, si, nsolve, num_sms, false);
+  s64.kernel = resolve_kernel(sc64.kernel, AERORT_PREC_FP64, si, nsolve, num_sms, false);
+  s64_list.kernel = resolve_kernel(sc64.kernel, AERORT_PREC_FP64, si, nsolve, num_sms, true);
   if (precision == AERORT_PREC_FP64)
-    return dispatch_fixed_t<double>(nstreams, opt, in, arena, bytes, sched, num_sms, sc64, r, f, nf, st, s,
+    return dispatch_fixed_t<double>(nstreams, opt, in, arena, bytes, sched, num_sms, s64, r, f, nf, st, s,
                                     Worklist());
   if (precision != AERORT_PREC_MIXED)
     return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
@@ -634,14 +690,14 @@ int dispatch_fixed(int precision, int nstreams, const RtOptions& opt, const Lamb
   wm.out_count = sched + 2;
   wm.ratio = kRefineRatio;
   void* rest = (char*)arena + list_bytes;
-  if (int rc = dispatch_fixed_t<float>(nstreams, opt, in, rest, bytes - list_bytes, sched, num_sms, sc, r, f, nf, st,
-                                       s, wm))
+  if (int rc = dispatch_fixed_t<float>(nstreams, opt, in, rest, bytes - list_bytes, sched, num_sms, s32, r, f, nf,
+                                       st, s, wm))
     return rc;
   Worklist wd;
   wd.in_list = (const int*)arena;
   wd.in_count = sched + 2;
-  return dispatch_fixed_t<double>(nstreams, opt, in, rest, bytes - list_bytes, sched, num_sms, sc64, r, f, nf, st, s,
-                                  wd);
+  return dispatch_fixed_t<double>(nstreams, opt, in, rest, bytes - list_bytes, sched, num_sms, s64_list, r, f, nf, st,
+                                  s, wd);
 }
 }  // namespace
 

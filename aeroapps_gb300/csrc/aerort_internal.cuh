@@ -33,34 +33,63 @@ struct DevBuf {
 // threads per block (a multiple of 32, <= 128) and resident blocks per SM
 // (0 = as many as the occupancy calculator allows).
 // kernel: 0 = thread per solve, 1 = team (one warp per solve for the Fourier
-// series, rt_team.cuh).
+// series, rt_team.cuh), 2 = automatic (resolve_kernel).
 struct Schedule {
   int threads = 32;  // one warp per block spreads small batches over more SMs
   int blocks_per_sm = 0;
-  int kernel = 0;
+  int kernel = 2;
 };
 int stream_index(int nstreams);  // 0..4 for 4, 6, 8, 12, 16; -1 otherwise
 
-// Library context: stream, scratch, staging buffers.  One per process; calls
-// are serialised by the mutex (the reference library is serial per process).
+// Automatic kernel choice.  The thread kernel runs 32 solves per warp, so it
+// needs a large batch to keep the SMs busy; the team kernel has the lower
+// per-solve latency.  Measured on GB300 (ragged columns, 20-72 layers), the
+// thread kernel wins only at these (precision, stream count) pairs and only
+// from this many warps of 32 solves per SM on ([precision][stream index
+// 0..4 = 4, 6, 8, 12, 16]; 0 = never).  The FP64 re-solve of a mixed launch's
+// short refinement list always takes the team kernel.
+constexpr int kThreadMinWarpsPerSm[2][5] = {{2, 3, 3, 0, 0}, {4, 0, 4, 0, 0}};
+inline int resolve_kernel(int kernel, int precision, int si, long nsolve, int num_sms, bool list) {
+  if (list) return 1;
+  if (kernel == 0 || kernel == 1) return kernel;
+  if (si < 0 || precision < 0 || precision > 1) return 0;
+  const int w = kThreadMinWarpsPerSm[precision][si];
+  return (w > 0 && nsolve >= 32L * w * num_sms) ? 0 : 1;
+}
+
+// Device scratch of the library's own RT launches for one caller stream:
+// per-thread solve scratch, the scheduling ints and the mixed method's
+// refinement list.
+struct Pad {
+  DevBuf scratch, counter, redo;
+  cudaStream_t owner = nullptr;
+  cudaEvent_t done = nullptr;  // recorded on `owner` after the last launch that used the pad
+  unsigned long last = 0;
+  bool used = false;
+};
+
+// Library context: stream, scratch pads, staging buffers.  One per process;
+// host calls are serialised by the mutex (the reference library is serial per
+// process).  Device work enqueued on different caller streams gets different
+// pads (up to kPads streams at once), so it may overlap on the GPU; a pad
+// handed from one stream to another makes the new stream wait, on the device,
+// for the work last enqueued on it.
 struct Context {
+  static constexpr int kPads = 8;
   std::mutex mu;
   bool init = false;
   int device = -1, num_sms = 0;
   cudaStream_t stream = nullptr;
-  DevBuf scratch, counter, redo, stage[24];
+  Pad pads[kPads];
+  Pad* pad = nullptr;  // the pad of the call in progress (set by bind)
+  unsigned long tick = 0;
+  DevBuf stage[24];
   Schedule sched[2][5];  // [precision][stream index]
-  Context() {
-    // measured on GB300: the team kernel wins at 6, 12 and 16 streams in the
-    // mixed method and at 12 and 16 in FP64 (stream index 0..4 = 4, 6, 8, 12, 16)
-    sched[1][1].kernel = 1;
-    sched[1][3].kernel = 1;
-    sched[1][4].kernel = 1;
-    sched[0][3].kernel = 1;
-    sched[0][4].kernel = 1;
-  }
   int setup();
   void release();
+  int bind(cudaStream_t s);    // select the pad of stream s
+  int unbind(cudaStream_t s);  // mark the pad busy until the work enqueued on s so far is done
+  Pad* find(cudaStream_t s);
 };
 
 Context& ctx();

@@ -131,9 +131,9 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   const size_t thread_bytes = (size_t)lay.template bytes<T>() * nthreads;
   const size_t sweep_off = (thread_bytes + 255) / 256 * 256;
   const size_t sweep_bytes = sizeof(T) * (size_t)swl.total * (nthreads / 32);
-  if (int rc = c.scratch.ensure(sweep_off + sweep_bytes)) return rc;
-  if (int rc = c.counter.ensure(4 * sizeof(int))) return rc;
-  int* counter = (int*)c.counter.p;
+  if (int rc = c.pad->scratch.ensure(sweep_off + sweep_bytes)) return rc;
+  if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
+  int* counter = (int*)c.pad->counter.p;
   int* first = counter + 1;
   k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
   k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
@@ -141,10 +141,10 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
-  T* sweep = (T*)((char*)c.scratch.p + sweep_off);
-  k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(opt, in2, q, c.scratch.p, nthreads, sweep,
-                                                                        swl.total, nsolve, chunk, counter, rad, refl,
-                                                                        nf, st, wl);
+  T* sweep = (T*)((char*)c.pad->scratch.p + sweep_off);
+  k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(opt, in2, q, c.pad->scratch.p, nthreads,
+                                                                        sweep, swl.total, nsolve, chunk, counter, rad,
+                                                                        refl, nf, st, wl);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }
@@ -169,9 +169,9 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   if (nblocks > maxblocks) nblocks = maxblocks;
   const long nthreads = nblocks * bs;
   const ScratchLayout<NS> lay(in.km);
-  if (int rc = c.scratch.ensure((size_t)lay.template bytes<T>() * nthreads)) return rc;
-  if (int rc = c.counter.ensure(4 * sizeof(int))) return rc;
-  int* counter = (int*)c.counter.p;
+  if (int rc = c.pad->scratch.ensure((size_t)lay.template bytes<T>() * nthreads)) return rc;
+  if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
+  int* counter = (int*)c.pad->counter.p;
   int* first = counter + 1;
   k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
   k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
@@ -179,7 +179,7 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
-  k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, c.scratch.p, nthreads, nsolve, counter,
+  k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, c.pad->scratch.p, nthreads, nsolve, counter,
                                                            rad, refl, nf, st, wl);
   CUDA_TRY(cudaGetLastError());
   return 0;

@@ -409,9 +409,13 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
     }
   }
   tm.sync();
-  // warm start from the previous layer of this term: its eigenvectors are
-  // usually close, so G V_prev is nearly column-orthogonal and few sweeps remain
-  const bool warm = M.vp_valid != 0;
+  // FP64: warm start from the previous layer of this term; its eigenvectors
+  // are usually close, so G V_prev is nearly column-orthogonal and few sweeps
+  // remain.  Not in FP32: V is then a product of the rotations of every layer
+  // so far, and its loss of orthogonality (a few ulp per rotation) grows along
+  // the layer chain to 1e-4 and more; the eigenvectors taken from it, and a
+  // radiance, go wrong by that much.
+  const bool warm = M.vp_valid != 0 && sizeof(T) == sizeof(double);
   if (warm) {
     T* Wt = M.work + 4 * NS * LD;  // V slot as temporary for G V_prev
     for (int e = tm.lane; e < N * N; e += kTeam) {

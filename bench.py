@@ -35,6 +35,12 @@ WORKLOAD = ("batching config: columns of the 262,144-column configuration, 20-72
             "(moments 2x streams), 4 wavelengths; Mie AOP (FP32) + scalar Lambertian RT per stream group")
 
 
+# per stream-count group: the column inputs copied host->device and the
+# outputs copied device->host in every end-to-end step
+E2E_IN = ("qm", "rh", "ROT", "depol", "he", "albedo", "sza", "raa", "vza", "nlay")
+E2E_OUT = ("rad", "refl", "nf", "st")
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -52,6 +58,8 @@ def parse():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--tune", action="store_true", help="autotune the RT schedules before timing")
     ap.add_argument("--graph", action="store_true", help="replay the mixed step from a captured CUDA graph")
+    ap.add_argument("--serial", action="store_true", help="run the stream-count groups one after another on one "
+                    "CUDA stream instead of concurrently on one stream each")
     return ap.parse_args()
 
 
@@ -307,6 +315,11 @@ def main():
             d["refl" + p] = torch.zeros_like(d["rad" + p])
             d["nf" + p] = torch.zeros(n * nch, dtype=torch.int32, device="cuda")
             d["st" + p] = torch.zeros_like(d["nf" + p])
+        # pinned host copies of the step's inputs and outputs (end-to-end timing)
+        for k in E2E_IN:
+            d["pin_" + k] = d[k].cpu().pin_memory()
+        for k in E2E_OUT:
+            d["pin_" + k] = torch.empty_like(d[k + "m"], device="cpu").pin_memory()
         groups.append(d)
     P = lambda t: t.data_ptr()
     ev = lambda: torch.cuda.Event(enable_timing=True)
@@ -321,20 +334,41 @@ def main():
                 P(d["vza"]), -1.0e15, P(d["rad" + p]), P(d["refl" + p]), P(d["nf" + p]), P(d["st" + p]), stream)
         assert rc == 0, _lib.last_error()
 
-    def step(prec, rt_events=None):
-        stream = torch.cuda.current_stream().cuda_stream
-        for d in groups:
-            rc = L.aerort_get_aop_vector_dev(chem.handle, d["km"], d["n"], nch, 20, _lib.ptr(ch32, _lib.P_f),
-                                             _lib.ptr(qt, _lib.P_i), _lib.ptr(qb, _lib.P_i), P(d["qm"]), P(d["rh"]),
-                                             d["nmom"], 1, P(d["tau"]), P(d["ssa"]), P(d["g"]), P(d["pmom"]), stream)
-            assert rc == 0, _lib.last_error()
-            if rt_events is not None:
-                e0, e1 = ev(), ev()
-                e0.record()
-            run_group(d, prec, stream)
-            if rt_events is not None:
-                e1.record()
-                rt_events.append((d["N"], e0, e1))
+    # every stream-count group on its own CUDA stream (the library keeps one
+    # scratch pad per stream), so the groups' launches overlap on the GPU
+    side = [torch.cuda.Stream() for _ in groups] if not args.serial else None
+
+    def group_work(d, prec, s, e2e=False):
+        if e2e:
+            for k in E2E_IN:
+                d[k].copy_(d["pin_" + k], non_blocking=True)
+        rc = L.aerort_get_aop_vector_dev(chem.handle, d["km"], d["n"], nch, 20, _lib.ptr(ch32, _lib.P_f),
+                                         _lib.ptr(qt, _lib.P_i), _lib.ptr(qb, _lib.P_i), P(d["qm"]), P(d["rh"]),
+                                         d["nmom"], 1, P(d["tau"]), P(d["ssa"]), P(d["g"]), P(d["pmom"]), s)
+        assert rc == 0, _lib.last_error()
+        run_group(d, prec, s)
+        if e2e:
+            for k in E2E_OUT:
+                d["pin_" + k].copy_(d[k + "m"], non_blocking=True)
+
+    def step(prec, rt_events=None, e2e=False):
+        main = torch.cuda.current_stream()
+        if rt_events is not None:
+            e0, e1 = ev(), ev()
+            e0.record()
+        if side is None:
+            for d in groups:
+                group_work(d, prec, main.cuda_stream, e2e)
+        else:
+            for d, ss in zip(groups, side):
+                ss.wait_stream(main)
+                with torch.cuda.stream(ss):
+                    group_work(d, prec, ss.cuda_stream, e2e)
+            for ss in side:
+                main.wait_stream(ss)
+        if rt_events is not None:
+            e1.record()
+            rt_events.append((0, e0, e1))
 
     tuned = {}
     if args.tune:
@@ -427,6 +461,7 @@ def main():
     roofline = {"bound": "fp32", "achieved": ach_m, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach_m / fp32_peak,
                 "traffic": None, "kernel": "k_scalar_lambert<NS, float> (mixed; all stream counts)",
                 "kernel_ms_per_step": rt_ms_m,
+                "kernel_time": "span of the step's launches (all stream groups, AOP kernels included at <1%)",
                 "peak_source": "measured live: FFMA issue-rate probe (8 FMA chains/thread), of measured",
                 "note": "achieved = reference-algorithm flops (banded-LU BVP, nonsymmetric eigen-solve) of the solves "
                         "/ kernel time; the kernel executes a different, mostly FP32 operation mix"}
@@ -438,33 +473,23 @@ def main():
                       "note": "reference-algorithm flops; the kernel executes fewer (block BVP sweep, symmetric "
                               "eigen-reduction), so frac can exceed 1"}
 
-    # ---------------------------------------------------------------- end to end through the host C ABI
-    from aeroapps_gb300 import vlidort
+    # ---------------------------------------------------------------- end to end from pinned host memory
+    # per group and step: host->device copy of the column inputs, the AOP and
+    # mixed RT entry points of the C ABI, device->host copy of radiance,
+    # reflectance, Fourier count and status; the host reads the results
     e2e_val, h2d, d2h = None, 0, 0
     if args.e2e_steps > 0:
-        def e2e_step():
-            nbi = nbo = 0
-            for d in groups:
-                g = d["host"]
-                tau, ssa, gg, pm, rc = mie.get_aop_vector(chem, d["km"], d["n"], nch, 20, ch32, names, 0, g["qm"],
-                                                          g["rh"], d["nmom"], 1)
-                nbi += g["qm"].nbytes + g["rh"].nbytes
-                nbo += tau.nbytes * 3 + pm.nbytes
-                rad, refl, rc2, _, _ = vlidort.vlidort_scalar_lambert_batch(
-                    d["km"], nch, d["n"], d["N"], d["nmom"], g["nlayers"], g["ROT"], g["depol"],
-                    tau.astype(np.float64), ssa.astype(np.float64), pm[..., 0].astype(np.float64), g["he"],
-                    g["albedo"], g["sza"], g["raa"], g["vza"], precision="mixed")
-                nbi += (g["ROT"].nbytes + 8 * (2 * tau.size + pm[..., 0].size) + g["he"].nbytes + g["albedo"].nbytes
-                        + 3 * g["sza"].nbytes + 8 * nch + 4 * d["n"])
-                nbo += rad.nbytes + refl.nbytes + 8 * rad.size
-            return nbi, nbo
-        e2e_step()
+        h2d = sum(d["pin_" + k].numel() * d["pin_" + k].element_size() for d in groups for k in E2E_IN)
+        d2h = sum(d["pin_" + k].numel() * d["pin_" + k].element_size() for d in groups for k in E2E_OUT)
+        step(_lib.PREC_MIXED, e2e=True)
         torch.cuda.synchronize()
         t = time.perf_counter()
         for _ in range(args.e2e_steps):
-            h2d, d2h = e2e_step()
-        torch.cuda.synchronize()
+            step(_lib.PREC_MIXED, e2e=True)
+            torch.cuda.synchronize()
+            got = sum(float(d["pin_rad"][0]) for d in groups)  # the host reads the step's results
         e2e_val = solves / ((time.perf_counter() - t) / args.e2e_steps)
+        assert np.isfinite(got)
 
     # ---------------------------------------------------------------- serving
     serving = None
@@ -515,8 +540,9 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(batch, args.cpu_cols or 32)
-    # AOP + scheduler init + nadir flag + RT per stream group and step, both timed passes
-    launches = 4 * len(groups) * (args.steps + args.plain_steps)
+    # inside the timed mixed steps, per stream group: the AOP kernel, then for the FP32 pass and for the FP64
+    # re-solve of its list each a scheduler init, the nadir flag and the RT kernel
+    launches = 7 * len(groups) * args.steps
     line = {
         "metric": METRIC, "value": value, "unit": "radiances/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -524,15 +550,17 @@ def main():
         "config": {"workload": WORKLOAD + "; one step = %d columns x 4 wavelengths per GPU" % args.cols,
                    "columns_per_step": args.cols, "solves_per_step": solves, "wavelengths": list(CHANNELS),
                    "l2": "inputs larger than L2 (optics + scratch of a step: hundreds of MB)",
-                   "failed_solves": bad, "tuned_schedules": tuned or None, "launch": graph_note},
+                   "failed_solves": bad, "tuned_schedules": tuned or None, "launch": graph_note,
+                   "groups": "concurrent, one CUDA stream per stream count" if side else "serial, one CUDA stream"},
         "accuracy": {"max_rel_err_vs_fp64": float(err.max()), "median_rel_err_vs_fp64": float(np.median(err)),
                      "radiances_compared": int(err.size), "bar": 1e-4},
         "plain_fp64": {"value": plain_value, "unit": "radiances/s", "ms_per_step": ms_plain,
                        "steps": args.plain_steps, "mixed_over_plain": value / plain_value},
         "roofline": roofline, "roofline_plain": roofline_plain, "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "radiances/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "path": "host-pointer C ABI: aerort_get_aop_vector + aerort_vlidort_scalar_lambert_mixed_batch per "
-                        "stream group (FP32 optics widened to FP64 on the host as the reference driver does)"},
+                "path": "pinned host inputs -> device copies, aerort_get_aop_vector_dev + "
+                        "aerort_vlidort_scalar_lambert_mixed_batch_dev per stream group (%s), device -> pinned host "
+                        "outputs, host read" % ("one CUDA stream per group" if side else "one stream")},
         "serving": serving, "gpu_launches": launches, "clocks": clk,
     }
     if rank == 0:

@@ -131,7 +131,10 @@ int aerort_vlidort_scalar_lambert_dev(int km, int nch, int nobs, int nstreams, i
  * from aerort_get_aop_vector_dev (tau_f, ssa_f, pmom_f; pass NULL for the FP64
  * tau, ssa, pmom), in which case the FP64 conversion the reference driver does
  * (dble(), geo_vlidort.F90:598-601) happens on load.  No counterpart routine in
- * the reference: it batches many VLIDORT_Scalar_Lambert calls into one launch. */
+ * the reference: it batches many VLIDORT_Scalar_Lambert calls into one launch.
+ * Calls on different streams use different library scratch (one pad per
+ * stream, up to 8 streams at once), so groups of different stream counts may
+ * be enqueued on separate streams and run concurrently. */
 int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
                                             const int* nlay, const double* ROT, const double* depol,
                                             const double* tau, const double* ssa, const double* pmom,
@@ -173,8 +176,9 @@ int aerort_vlidort_scalar_lambert_mixed_batch(int km, int nch, int nobs, int nst
  * counterpart in the reference.  aerort_workspace_create allocates `bytes` of
  * device memory once; launches through aerort_vlidort_scalar_lambert_ws_dev
  * then allocate nothing, and launches on different workspaces may overlap on
- * different streams (the batched entry points above share one library
- * scratch and are serialised).  The grid is capped to the threads whose
+ * different streams (the batched entry points above keep one library
+ * scratch pad per stream, for up to 8 streams at once, and allocate it on
+ * first use).  The grid is capped to the threads whose
  * scratch fits: bytes_per_thread(km, nstreams, precision) x threads; one
  * block (32-128 threads) must fit.  The precision argument selects
  * AERORT_PREC_FP64 or AERORT_PREC_MIXED; the other arguments are those of
@@ -208,11 +212,15 @@ int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int
  * solve on one thread; AERORT_KERNEL_TEAM runs the set-up thread per solve and
  * the Fourier series on a whole warp per solve with the layer matrices in
  * shared memory (the better choice where the per-solve working set is large).
- * Defaults: team at 6, 12 and 16 streams (mixed) and at 12 and 16 streams
- * (FP64), as measured on GB300.  Results agree to round-off.
- * aerort_get_kernel returns the kernel, or a negative rc. */
+ * AERORT_KERNEL_AUTO (the default) takes the thread kernel only where it was
+ * measured faster on GB300: FP64 at 4, 6 and 8 streams and mixed at 4 and 8
+ * streams, for batches that give every SM 2-4 warps of 32 solves or more;
+ * otherwise the team kernel.  The FP64 re-solve of a mixed launch's refinement list always runs
+ * on the team kernel.  Results agree to round-off.  aerort_get_kernel returns
+ * the setting, or a negative rc. */
 #define AERORT_KERNEL_THREAD 0
 #define AERORT_KERNEL_TEAM 1
+#define AERORT_KERNEL_AUTO 2
 int aerort_set_kernel(int nstreams, int precision, int kernel);
 int aerort_get_kernel(int nstreams, int precision);
 

@@ -156,3 +156,36 @@ def test_cancelling_fourier_sum_is_refined_in_fp64():
     assert rc == 0 and np.all(st == 0)
     assert cnt.value >= 1
     assert np.max(np.abs(rad / orad - 1.0)) <= RTOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N,cols", [(12, [2130, 2277, 2227]), (16, [7090, 7683])])
+def test_team_kernel_mixed_on_long_layer_chains(N, cols):
+    # columns of the bench batch whose mixed radiance went wrong by up to 3e-3
+    # when the FP32 team kernel warm-started each layer's Jacobi from the
+    # previous layer's rotations (orthogonality lost along the layer chain)
+    import bench
+    L = _lib.lib()
+    full = bench.make_batch(8192, seed=20261204)
+    g = bench.subset(full, np.array(cols))
+    assert np.all(g["nstreams"] == N)
+    tabs = mie.generate_tables(CH, nmom=32)
+    chem = mie.ChemMie(tabs)
+    qt, qb = zip(*[chem.query_idx(x) for x in synth.tracer_names()])
+    chem.destroy()
+    km, n = g["km"], len(cols)
+    nl = np.ascontiguousarray(g["nlayers"], np.int32)
+    tau, ssa, gg, pm, rc = oracle.get_aop_vector(tabs, km, n, 4, 20, np.float32(CH), qt, qb, g["qm"], g["rh"], 2 * N, 1)
+    orad = oracle.scalar_lambert(km, 4, n, np.array(CH), N, 0, 2 * N, 1, g["ROT"], g["depol"], tau, ssa, gg, pm, g["pe"],
+                                 g["he"], g["te"], g["albedo"], g["sza"], g["raa"], g["vza"], MISSING, nlay=nl)[0]
+    old = L.aerort_get_kernel(N, _lib.PREC_MIXED)
+    assert L.aerort_set_kernel(N, _lib.PREC_MIXED, _lib.KERNEL_TEAM) == 0
+    try:
+        rad, _, rc, _, st = vlidort.vlidort_scalar_lambert_batch(
+            km, 4, n, N, 2 * N, nl, g["ROT"], g["depol"], tau.astype(np.float64), ssa.astype(np.float64),
+            pm[..., 0].astype(np.float64), g["he"], g["albedo"], g["sza"], g["raa"], g["vza"], MISSING=MISSING,
+            precision="mixed")
+    finally:
+        L.aerort_set_kernel(N, _lib.PREC_MIXED, old)
+    assert rc == 0 and np.all(st == 0)
+    assert np.max(np.abs(rad / orad - 1.0)) <= RTOL

@@ -48,5 +48,7 @@ def test_team_matches_thread_and_oracle(N):
 def test_kernel_api_validates():
     L = _lib.lib()
     assert L.aerort_set_kernel(7, 0, 0) == 1003
-    assert L.aerort_set_kernel(8, 0, 2) == 1002
-    assert L.aerort_get_kernel(16, 0) == 1 and L.aerort_get_kernel(4, 0) == 0 and L.aerort_get_kernel(6, 1) == 1
+    assert L.aerort_set_kernel(8, 0, 3) == 1002
+    assert all(L.aerort_get_kernel(n, p) == _lib.KERNEL_AUTO for n in (4, 6, 8, 12, 16) for p in (0, 1))
+    assert L.aerort_set_kernel(8, 1, _lib.KERNEL_TEAM) == 0 and L.aerort_get_kernel(8, 1) == _lib.KERNEL_TEAM
+    assert L.aerort_set_kernel(8, 1, _lib.KERNEL_AUTO) == 0 and L.aerort_get_kernel(8, 1) == _lib.KERNEL_AUTO
