@@ -68,6 +68,7 @@ void Context::release() {
     p = Pad();
   }
   pad = nullptr;
+  last_mixed = nullptr;
   for (auto& b : stage) b.release();
   if (stream) cudaStreamDestroy(stream);
   stream = nullptr;
@@ -504,6 +505,7 @@ int dispatch_lambert_on_pad(Context& c, int precision, int nstreams, const RtOpt
     return set_error(AERORT_RC_ARG, "precision must be AERORT_PREC_FP64 or AERORT_PREC_MIXED");
   const int nsolve = in.nobs * in.nch;
   Pad& p = *c.pad;
+  c.last_mixed = c.pad;
   if (int rc = p.redo.ensure(sizeof(int) * ((size_t)nsolve + 1))) return rc;
   if (int rc = p.counter.ensure(4 * sizeof(int))) return rc;
   int* count = (int*)p.counter.p + 2;
@@ -613,10 +615,10 @@ extern "C" int aerort_refined_count(void* stream, int* count) {
   Context& c = ctx();
   std::lock_guard<std::mutex> lk(c.mu);
   *count = 0;
-  Pad* p = c.find((cudaStream_t)stream);
+  Pad* p = stream ? c.find((cudaStream_t)stream) : c.last_mixed;
   if (!p || !p->counter.p || p->counter.bytes < 4 * sizeof(int)) return AERORT_OK;
-  CUDA_TRY(cudaMemcpyAsync(count, (int*)p->counter.p + 2, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
-  CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  CUDA_TRY(cudaMemcpyAsync(count, (int*)p->counter.p + 2, sizeof(int), cudaMemcpyDeviceToHost, p->owner));
+  CUDA_TRY(cudaStreamSynchronize(p->owner));
   return AERORT_OK;
 }
 

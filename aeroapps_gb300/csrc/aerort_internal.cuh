@@ -81,7 +81,8 @@ struct Context {
   int device = -1, num_sms = 0;
   cudaStream_t stream = nullptr;
   Pad pads[kPads];
-  Pad* pad = nullptr;  // the pad of the call in progress (set by bind)
+  Pad* pad = nullptr;         // the pad of the call in progress (set by bind)
+  Pad* last_mixed = nullptr;  // the pad of the last mixed-method call
   unsigned long tick = 0;
   DevBuf stage[24];
   Schedule sched[2][5];  // [precision][stream index]

@@ -196,9 +196,11 @@ int aerort_vlidort_scalar_lambert_ws_dev(aerort_workspace* ws, int precision, in
                                          const double* sensor_zenith, double MISSING, double* radiance_VL,
                                          double* reflectance_VL, int* nfourier, int* status, void* stream);
 
-/* Number of solves the last mixed call through the library's batched entry
- * points re-solved in FP64 (synchronises `stream`).  No counterpart in the
- * reference. */
+/* Number of solves that the last mixed call enqueued on `stream` through the
+ * library's batched entry points re-solved in FP64; with stream = NULL, the
+ * last mixed call on any stream (this is how to ask after the host-pointer
+ * entry points, which run on the library's own stream).  Synchronises the
+ * stream of that call.  No counterpart in the reference. */
 int aerort_refined_count(void* stream, int* count);
 
 /* Launch schedule of the RT kernel per (stream count, precision): threads per
