@@ -1,0 +1,209 @@
+// Rayleigh optical thickness and depolarisation on the device: the
+// reference's VLIDORT_ROT_CALC (geo_vlidort/VLIDORT_ROT.F90:19-86), i.e.
+// VLIDORT_Rayleigh, A(), coef_depol and F_air
+// (RTSI/VLIDORT2p8p3/VLIDORT_ScatMod.F90:145-283) for every pixel and channel.
+//
+// Bit-identical to the reference arithmetic: every operation is an explicitly
+// rounded FP64 intrinsic (no FMA contraction) in the Fortran evaluation order;
+// the reference's default-REAL literals enter as the nearest float, and its
+// all-literal subexpressions are evaluated in single precision.
+//
+// Layout: one block per (pixel, channel) column.  Its threads compute the
+// volume scattering coefficient at the km+1 edges once each (two FP64
+// divisions per edge) into shared memory, then the km layer values
+// (trapezoid in height).  The per-channel cross section A(lambda) is computed
+// once per block.  Reads pe/he/te (3 x (km+1) doubles per pixel, shared by the
+// channels through L2), writes km doubles per column: HBM-bound at large
+// batches.
+#include "aerort_internal.cuh"
+
+namespace aerort_internal {
+namespace {
+
+#define LIT(x) ((double)(x##f))  // a default-REAL literal widened to REAL*8
+
+__host__ __device__ inline double dm(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+__host__ __device__ inline double da(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+__host__ __device__ inline double ds(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dsub_rn(a, b);
+#else
+  return a - b;
+#endif
+}
+__host__ __device__ inline double dd(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __ddiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// F_air (ScatMod.F90:267-283): King factor of the air mixture; c = CO2 ratio.
+__host__ __device__ inline double king_factor(double xx2, double c) {
+  const double d1 = da(LIT(1.034), dm(LIT(3.17E-4), xx2));
+  const double d2 = da(da(LIT(1.096), dm(LIT(1.385E-3), xx2)), dm(dm(LIT(1.448E-4), xx2), xx2));
+  const double d3 = 1.0, d4 = LIT(1.15);
+  const double c100 = dm(c, LIT(100.0));
+  const double num = da(da(da(dm(LIT(78.084), d1), dm(LIT(20.946), d2)), dm(LIT(0.934), d3)), dm(c100, d4));
+  const float lit_sum = (78.084f + 20.946f) + 0.934f;  // REAL*4 in the reference
+  return dd(num, da((double)lit_sum, c100));
+}
+
+__host__ __device__ inline double co2_ratio() { return (double)(360.0f * 1e-6f); }  // `360.0*1e-6`, REAL*4
+
+// Ns = (Av/22.4141)*(273.15/Ts)*(1.0/1000) [molecules/cm^3]
+__host__ __device__ inline double ns_standard() {
+  return dm(dm(dd(LIT(6.0221367e23), LIT(22.4141)), dd(LIT(273.15), LIT(288.15))), (double)(1.0f / 1000.0f));
+}
+
+// A(X): Rayleigh cross section [cm^2/molecule] at X micron (ScatMod.F90:211-247).
+__host__ __device__ inline double rayleigh_cross_section(double x) {
+  const double pi = (double)3.14159274101257324f;  // 4.*atan(1.0) in REAL*4
+  const double xx = dd(1.0, x);
+  const double xx2 = dm(xx, xx);
+  const double cm = dd(x, LIT(10000.0));
+  const double pi3 = dm(dm(pi, pi), pi);
+  double ri = da(da(LIT(8060.51), dd(LIT(2480990.0), ds(LIT(132.274), xx2))), dd(LIT(17455.7), ds(LIT(39.32957), xx2)));
+  ri = da(dm(ri, LIT(1e-8)), 1.0);
+  const double c = co2_ratio();
+  ri = da(dm(ds(ri, 1.0), da(1.0, dm(LIT(0.54), ds(c, LIT(0.0003))))), 1.0);
+  const double ri2 = dm(ri, ri);
+  const double ns = ns_standard();
+  const double num = dm(dm(dm(24.0, pi3), king_factor(xx2, c)), dm(ds(ri2, 1.0), ds(ri2, 1.0)));
+  double den = dm(ns, ns);
+  den = dm(den, cm);
+  den = dm(den, cm);
+  den = dm(den, cm);
+  den = dm(den, cm);
+  den = dm(den, da(ri2, 2.0));
+  den = dm(den, da(ri2, 2.0));
+  return dd(num, den);
+}
+
+// coef_depol (ScatMod.F90:251-265), x in micron.
+__host__ __device__ inline double depolarisation(double x) {
+  const double xx = dd(1.0, x);
+  const double xx2 = dm(xx, xx);
+  const double c = co2_ratio();
+  const double f = king_factor(xx2, c);
+  return dd(dm(6.0, ds(f, 1.0)), da(dm(7.0, f), 3.0));
+}
+
+__global__ void k_rot_calc(int km, int nch, int nobs, const double* __restrict__ channels,
+                           const double* __restrict__ pe, const double* __restrict__ he,
+                           const double* __restrict__ te, double* __restrict__ rot, double* __restrict__ depol) {
+  extern __shared__ double vol[];  // km + 1 edge values of the current column
+  __shared__ double a_ns;
+  const double ps = LIT(1013.25), ts = LIT(288.15);
+  for (long col = blockIdx.x; col < (long)nobs * nch; col += gridDim.x) {
+    const int j = (int)(col % nobs), i = (int)(col / nobs);
+    const double wmicron = dm(channels[i], LIT(1.E-3));
+    if (threadIdx.x == 0) {
+      a_ns = dm(rayleigh_cross_section(wmicron), ns_standard());
+      if (j == 0) depol[i] = depolarisation(wmicron);
+    }
+    __syncthreads();
+    const double* p = pe + (long)(km + 1) * j;
+    const double* t = te + (long)(km + 1) * j;
+    const double* z = he + (long)(km + 1) * j;
+    for (int k = threadIdx.x; k <= km; k += blockDim.x)
+      vol[k] = dm(dm(dm(a_ns, dd(dm(p[k], LIT(1.E-2)), ps)), dd(ts, t[k])), LIT(1.E5));
+    __syncthreads();
+    double* out = rot + (long)km * (j + (long)nobs * i);
+    for (int k = threadIdx.x; k < km; k += blockDim.x) {
+      const double difz = ds(dm(z[k], LIT(1.E-3)), dm(z[k + 1], LIT(1.E-3)));
+      out[k] = dd(dm(difz, da(vol[k], vol[k + 1])), 2.0);
+    }
+    __syncthreads();
+  }
+}
+
+int rot_checks(int km, int nch, int nobs) {
+  if (km <= 0 || nch <= 0 || nobs < 0) return set_error(AERORT_RC_ARG, "rot_calc: bad sizes");
+  if ((size_t)(km + 1) * sizeof(double) > 200 * 1024) return set_error(AERORT_RC_NLAYERS, "rot_calc: km too large");
+  return 0;
+}
+
+int launch_rot(int km, int nch, int nobs, const double* channels, const double* pe, const double* he,
+               const double* te, double* rot, double* depol, cudaStream_t s, int num_sms) {
+  if (nobs == 0) return 0;
+  const size_t smem = (size_t)(km + 1) * sizeof(double);
+  if (smem > 48 * 1024)
+    CUDA_TRY(cudaFuncSetAttribute(k_rot_calc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  long blocks = (long)nobs * nch;
+  const long cap = (long)num_sms * 16;
+  if (blocks > cap) blocks = cap;
+  k_rot_calc<<<(unsigned)blocks, 128, smem, s>>>(km, nch, nobs, channels, pe, he, te, rot, depol);
+  CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+}  // namespace
+}  // namespace aerort_internal
+
+using namespace aerort_internal;
+
+extern "C" int aerort_vlidort_rot_calc_dev(int km, int nch, int nobs, const double* channels, const double* pe,
+                                           const double* he, const double* te, double* ROT, double* depol,
+                                           void* stream) {
+  if (int rc = rot_checks(km, nch, nobs)) return rc;
+  if (!channels || !pe || !he || !te || !ROT || !depol) return set_error(AERORT_RC_ARG, "rot_calc_dev: null array");
+  Context& c = ctx();
+  int num_sms = 0;
+  {
+    std::lock_guard<std::mutex> lk(c.mu);
+    if (int rc = c.setup()) return rc;
+    num_sms = c.num_sms;
+  }
+  return launch_rot(km, nch, nobs, channels, pe, he, te, ROT, depol, (cudaStream_t)stream, num_sms);
+}
+
+extern "C" int aerort_vlidort_rot_calc(int km, int nch, int nobs, const double* channels, const double* pe,
+                                       const double* he, const double* te, double MISSING, int verbose, double* ROT,
+                                       double* depol) {
+  (void)MISSING;  // VLIDORT_Rayleigh cannot fail, so no layer is ever set to MISSING
+  (void)verbose;
+  if (int rc = rot_checks(km, nch, nobs)) return rc;
+  if (!channels || !pe || !he || !te || !ROT || !depol) return set_error(AERORT_RC_ARG, "rot_calc: null array");
+  Context& c = ctx();
+  std::lock_guard<std::mutex> lk(c.mu);
+  if (int rc = c.setup()) return rc;
+  cudaStream_t s = c.stream;
+  const size_t ne = (size_t)(km + 1) * nobs, nr = (size_t)km * nobs * nch;
+  // staging buffers 16..20 are this entry point's
+  if (int rc = c.stage[16].ensure(8 * (size_t)nch)) return rc;
+  if (int rc = c.stage[17].ensure(8 * ne + 8)) return rc;
+  if (int rc = c.stage[18].ensure(8 * ne + 8)) return rc;
+  if (int rc = c.stage[19].ensure(8 * ne + 8)) return rc;
+  if (int rc = c.stage[20].ensure(8 * (nr + nch) + 8)) return rc;
+  double* dch = (double*)c.stage[16].p;
+  double* dpe = (double*)c.stage[17].p;
+  double* dhe = (double*)c.stage[18].p;
+  double* dte = (double*)c.stage[19].p;
+  double* drot = (double*)c.stage[20].p;
+  double* ddep = drot + nr;
+  CUDA_TRY(cudaMemcpyAsync(dch, channels, 8 * (size_t)nch, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(dpe, pe, 8 * ne, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(dhe, he, 8 * ne, cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(dte, te, 8 * ne, cudaMemcpyHostToDevice, s));
+  if (int rc = launch_rot(km, nch, nobs, dch, dpe, dhe, dte, drot, ddep, s, c.num_sms)) return rc;
+  if (nobs > 0) {
+    CUDA_TRY(cudaMemcpyAsync(ROT, drot, 8 * nr, cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(depol, ddep, 8 * (size_t)nch, cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_TRY(cudaStreamSynchronize(s));
+  return AERORT_OK;
+}

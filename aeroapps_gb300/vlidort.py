@@ -91,3 +91,18 @@ def vlidort_scalar_lambert_batch(km, nch, nobs, nstreams, nMom, nlay, ROT, depol
         raise RuntimeError("aerort_vlidort_scalar_lambert_batch rc=%d: %s" % (rc, _lib.last_error()))
     return rad, refl, rc, nf, st
 
+
+
+def rot_calc(channels, pe, he, te, MISSING, verbose=0):
+    """f2py-style ROT_CALC (leo_vlidort/VLIDORT_POLAR_py.F90:9-41): pe, he, te
+    (km+1, nobs) in Pa, m, K; returns (ROT(km, nobs, nch), depol(nch), rc)."""
+    pe, he, te = _f64(pe), _f64(he), _f64(te)
+    ch = np.ascontiguousarray(channels, np.float64)
+    km, nobs, nch = pe.shape[0] - 1, pe.shape[1], ch.size
+    rot = np.zeros((km, nobs, nch), order="F")
+    depol = np.zeros(nch)
+    L = _lib.lib()
+    rc = L.aerort_vlidort_rot_calc(km, nch, nobs, _lib.ptr(ch, _lib.P_d), _lib.ptr(pe, _lib.P_d),
+                                   _lib.ptr(he, _lib.P_d), _lib.ptr(te, _lib.P_d), float(MISSING), int(verbose),
+                                   _lib.ptr(rot, _lib.P_d), _lib.ptr(depol, _lib.P_d))
+    return rot, depol, rc

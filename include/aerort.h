@@ -172,6 +172,20 @@ int aerort_vlidort_scalar_lambert_mixed_batch(int km, int nch, int nobs, int nst
                                               double MISSING, double* radiance_VL, double* reflectance_VL,
                                               int* nfourier, int* status);
 
+/* Rayleigh optical thickness ROT(km,nobs,nch) and depolarisation ratio
+ * depol(nch) from the edge profiles pe (Pa), he (m), te (K), each
+ * (km+1,nobs), at channels(nch) nm.  Replaces VLIDORT_ROT_CALC
+ * (geo_vlidort/VLIDORT_ROT.F90:19-86, with VLIDORT_Rayleigh / coef_depol /
+ * F_air of RTSI/VLIDORT2p8p3/VLIDORT_ScatMod.F90:145-283), same argument list
+ * with rc as the return value; bit-identical to the reference arithmetic.
+ * MISSING and verbose are accepted for the drop-in and unused (the reference
+ * calculator cannot fail).  _dev: every array on the device, enqueued on
+ * `stream`. */
+int aerort_vlidort_rot_calc(int km, int nch, int nobs, const double* channels, const double* pe, const double* he,
+                            const double* te, double MISSING, int verbose, double* ROT, double* depol);
+int aerort_vlidort_rot_calc_dev(int km, int nch, int nobs, const double* channels, const double* pe,
+                                const double* he, const double* te, double* ROT, double* depol, void* stream);
+
 /* Caller-owned RT workspace (device scratch for one launch at a time).  No
  * counterpart in the reference.  aerort_workspace_create allocates `bytes` of
  * device memory once; launches through aerort_vlidort_scalar_lambert_ws_dev

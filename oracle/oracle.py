@@ -33,6 +33,9 @@ def lib():
         _lib.oracle_scalar_lambert.restype = ctypes.c_int
         _lib.oracle_get_aop_vector.restype = ctypes.c_int
         _lib.oracle_set_asymtx_tol.restype = None
+        _lib.oracle_rot_calc.restype = ctypes.c_int
+        _lib.oracle_coef_depol.restype = ctypes.c_double
+        _lib.oracle_coef_depol.argtypes = [ctypes.c_double]
     return _lib
 
 
@@ -119,3 +122,15 @@ def get_aop_vector(tableset, km, nobs, nch, nq, channels_nm, q_table, q_bin, qm,
                                      _p(qm, P_f), _p(rh, P_f), nMom, nPol, _p(tau, P_f), _p(ssa, P_f), _p(g, P_f),
                                      _p(pmom, P_f))
     return tau, ssa, g, pmom, rc
+
+
+def rot_calc(channels, pe, he, te):
+    """VLIDORT_ROT_CALC restated (rot_oracle.c): pe, he, te (km+1, nobs) -> ROT (km, nobs, nch), depol (nch), rc."""
+    pe, he, te = (np.asfortranarray(a, np.float64) for a in (pe, he, te))
+    ch = np.ascontiguousarray(channels, np.float64)
+    km, nobs, nch = pe.shape[0] - 1, pe.shape[1], ch.size
+    rot = np.zeros((km, nobs, nch), order="F")
+    depol = np.zeros(nch)
+    rc = lib().oracle_rot_calc(km, nch, nobs, _p(ch, P_d), _p(pe, P_d), _p(he, P_d), _p(te, P_d), _p(rot, P_d),
+                               _p(depol, P_d))
+    return rot, depol, rc
