@@ -179,6 +179,43 @@ RT_HD void apply_reflector_sym(int n, T* A, const T* v, T beta) {
 // sigma[a] = |G e_a| (the singular values, with the relative accuracy of a
 // column-graded G) and the columns of V are the right singular vectors, i.e.
 // the eigenvectors of G^T G.  Returns false if the sweep budget is exhausted.
+// 1/sqrt(x): the hardware reciprocal square root on the device.
+template <typename T>
+RT_HD T rsqrt_t(T x) {
+#ifdef __CUDA_ARCH__
+  if constexpr (sizeof(T) == sizeof(float)) return rsqrtf(x);
+  else return rsqrt(x);
+#else
+  return (T)1 / sqrt(x);
+#endif
+}
+
+// One Hestenes-Jacobi rotation of column pair (p, q) with squared norms al, be
+// and inner product ga.  Rotate when ga^2 > tol^2 al be (the pair is not yet
+// orthogonal to tol); the return value says whether ga^2 > tol al be (the
+// sweep does not count as the converged one).  tan(theta) comes from one
+// square root and one division, t = sign(d) 2 ga / (|d| + sqrt(d^2 + 4 ga^2))
+// with d = be - al (the smaller root of t^2 + 2 t d / (2 ga) - 1 = 0), and
+// cos(theta) from a reciprocal square root.
+template <typename T>
+struct Rotation {
+  T cs, sn;
+  bool rotate, unconverged;
+  RT_HD Rotation(T al, T be, T ga, T tol) {
+    const T ab = al * be, g2 = ga * ga;
+    rotate = g2 > tol * tol * ab;
+    unconverged = g2 > tol * ab;
+    cs = (T)1;
+    sn = (T)0;
+    if (rotate) {
+      const T d = be - al, two_ga = (T)2 * ga;
+      const T t = (d < (T)0 ? -two_ga : two_ga) / (fabs(d) + sqrt(d * d + two_ga * two_ga));
+      cs = rsqrt_t((T)1 + t * t);
+      sn = cs * t;
+    }
+  }
+};
+
 template <int NS, typename T>
 RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
   for (int j = 0; j < n; ++j)
@@ -186,10 +223,10 @@ RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
   const T tol = Eps<T>::v * (T)n;
   bool done = false;
   for (int sweep = 0; sweep < 30 && !done; ++sweep) {
-    // converged when no pair rotated, or when the largest normalised
-    // off-diagonal of this sweep was below sqrt(tol): Jacobi converges
+    // converged when no pair rotated, or when every normalised off-diagonal
+    // of this sweep, |ga| / sqrt(al be), was below sqrt(tol): Jacobi converges
     // quadratically, so the sweep that follows would not rotate
-    T off = 0;
+    bool unconverged = false;
     for (int p = 0; p + 1 < n; ++p)
       for (int q = p + 1; q < n; ++q) {
         T al = 0, be = 0, ga = 0;
@@ -197,12 +234,10 @@ RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
           const T gp = G[i + NS * p], gq = G[i + NS * q];
           al += gp * gp; be += gq * gq; ga += gp * gq;
         }
-        const T nb = sqrt(al * be);
-        if (!(fabs(ga) > tol * nb)) continue;
-        if (fabs(ga) > off * nb) off = fabs(ga) / nb;
-        const T zeta = (be - al) / ((T)2 * ga);
-        const T t = copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
-        const T cs = (T)1 / sqrt((T)1 + t * t), sn = cs * t;
+        const Rotation<T> rot(al, be, ga, tol);
+        if (!rot.rotate) continue;
+        unconverged = unconverged || rot.unconverged;
+        const T cs = rot.cs, sn = rot.sn;
         for (int i = 0; i < n; ++i) {
           const T gp = G[i + NS * p], gq = G[i + NS * q];
           G[i + NS * p] = cs * gp - sn * gq;
@@ -212,7 +247,7 @@ RT_HD bool jacobi_svd(int n, T* G, T* V, T* sigma) {
           V[i + NS * q] = sn * vp + cs * vq;
         }
       }
-    done = off * off <= tol;
+    done = !unconverged;
   }
   for (int a = 0; a < n; ++a) {
     T s = 0;

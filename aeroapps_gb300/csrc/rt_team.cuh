@@ -72,30 +72,43 @@ RT_HD bool team_any(const Team& tm, bool pred, int* flag) {
 #endif
 }
 
-// Index of the largest v over the lanes, the smallest index among equals (the
-// first maximum of a serial scan); every lane gets it.  v < 0 marks a lane
-// without a candidate.
+// Lane holding the largest v, the lowest lane among equals (the first maximum
+// of a serial scan when the candidates sit on lanes in index order); every
+// lane gets it and *vmax.  v >= 0 on lanes with a candidate, v < 0 elsewhere.
+// On the device, non-negative floats order as their bit patterns, so the
+// maximum is one warp reduction (two for FP64: high word, then low word).
 template <typename T>
-RT_HD int team_argmax(const Team& tm, T v, int idx, T* red, int* ired, T* vmax) {
+RT_HD int team_argmax_lane(const Team& tm, T v, T* red, T* vmax) {
 #ifdef __CUDA_ARCH__
-  (void)red; (void)ired;
-  for (int o = 1; o < kTeam; o <<= 1) {
-    T ov = __shfl_xor_sync(0xffffffffu, v, o);
-    int oi = __shfl_xor_sync(0xffffffffu, idx, o);
-    if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+  (void)red;
+  const unsigned full = 0xffffffffu;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    const unsigned key = (v >= (T)0) ? __float_as_uint(v) : 0u;
+    const unsigned mx = __reduce_max_sync(full, key);
+    const int src = __ffs(__ballot_sync(full, key == mx)) - 1;
+    *vmax = __uint_as_float(mx);
+    return src;
+  } else {
+    const unsigned hi = (v >= (T)0) ? (unsigned)__double2hiint(v) : 0u;
+    const unsigned lo = (v >= (T)0) ? (unsigned)__double2loint(v) : 0u;
+    const unsigned mh = __reduce_max_sync(full, hi);
+    const unsigned cand = __ballot_sync(full, hi == mh);
+    unsigned ml = 0;
+    if (cand & (1u << tm.lane)) ml = __reduce_max_sync(cand, lo);
+    ml = __shfl_sync(full, ml, __ffs(cand) - 1);
+    const int src = __ffs(__ballot_sync(full, hi == mh && lo == ml)) - 1;
+    *vmax = __hiloint2double((int)mh, (int)ml);
+    return src;
   }
-  *vmax = v;
-  return idx;
 #else
   red[tm.lane] = v;
-  ired[tm.lane] = idx;
   tm.sync();
   T bv = red[0];
-  int bi = ired[0];
+  int bi = 0;
   for (int k = 1; k < kTeam; ++k)
-    if (red[k] > bv || (red[k] == bv && ired[k] < bi)) { bv = red[k]; bi = ired[k]; }
+    if (red[k] > bv) { bv = red[k]; bi = k; }
   tm.sync();
-  *vmax = bv;
+  *vmax = bv < (T)0 ? (T)0 : bv;
   return bi;
 #endif
 }
@@ -143,36 +156,43 @@ struct SweepLayout {
 };
 
 // ---------------------------------------------------------------------------------- dense steps
-// Cholesky A = L L^T (lower triangle, leading dimension LDA), right-looking.
-// Returns false (on every lane) if a pivot is not positive.
+// Cholesky A = L L^T (lower triangle, leading dimension LDA, n <= 32),
+// right-looking; lane r owns row r of the trailing update (the column below
+// the pivot is a shared-memory broadcast).  Returns false (on every lane) if a
+// pivot is not positive.
 template <int LDA, typename T>
 RT_HD bool team_cholesky(const Team& tm, int n, T* A) {
+  const int r = tm.lane;
   for (int j = 0; j < n; ++j) {
     const T d = A[j + LDA * j];
     if (!(d > (T)0)) return false;
     const T ljj = sqrt(d), inv = (T)1 / ljj;
     tm.sync();
-    if (tm.lane == 0) A[j + LDA * j] = ljj;
-    for (int i = j + 1 + tm.lane; i < n; i += kTeam) A[i + LDA * j] *= inv;
+    if (r == 0) A[j + LDA * j] = ljj;
+    if (r > j && r < n) A[r + LDA * j] *= inv;
     tm.sync();
-    const int m2 = n - j - 1;
-    for (int e = tm.lane; e < m2 * m2; e += kTeam) {
-      const int i = j + 1 + e / m2, k = j + 1 + e % m2;
-      if (k <= i) A[i + LDA * k] -= A[i + LDA * j] * A[k + LDA * j];
+    if (r > j && r < n) {
+      const T lrj = A[r + LDA * j];
+      for (int k = j + 1; k <= r; ++k) A[r + LDA * k] -= lrj * A[k + LDA * j];
     }
     tm.sync();
   }
   return true;
 }
 
-// In-place LU with partial pivoting of the n x n matrix A and solution of nrhs
-// right-hand sides B (leading dimension LDA for both); pivots as lu_solve.
+// In-place LU with partial pivoting of the n x n matrix A (n <= 32) and
+// solution of nrhs right-hand sides B (leading dimension LDA for both); pivots
+// and per-element arithmetic as lu_solve.  Lane r owns row r in the
+// elimination and the back substitution: its multiplier stays in a register,
+// the pivot row is a shared-memory broadcast, and the rows of a column are
+// consecutive words (no bank conflicts).
 template <int LDA, typename T>
 RT_HD bool team_lu_solve(const Team& tm, int n, T* A, T* B, int nrhs, T* red, int* ired) {
+  (void)ired;
+  const int r = tm.lane;
   for (int k = 0; k < n; ++k) {
-    const int i = k + tm.lane;
     T vmax;
-    const int piv = team_argmax(tm, (i < n) ? fabs(A[i + LDA * k]) : (T)-1, i, red, ired, &vmax);
+    const int piv = team_argmax_lane(tm, (r >= k && r < n) ? fabs(A[r + LDA * k]) : (T)-1, red, &vmax);
     if (vmax == (T)0) return false;
     if (piv != k) {
       for (int j = tm.lane; j < n + nrhs; j += kTeam) {
@@ -183,28 +203,22 @@ RT_HD bool team_lu_solve(const Team& tm, int n, T* A, T* B, int nrhs, T* red, in
       }
       tm.sync();
     }
-    const T inv = (T)1 / A[k + LDA * k];
-    const int m2 = n - k - 1;
-    // multipliers, then the trailing update of A and B (each element once per k)
-    for (int e = tm.lane; e < m2; e += kTeam) A[k + 1 + e + LDA * k] *= inv;
-    tm.sync();
-    const int cols = m2 + nrhs;
-    for (int e = tm.lane; e < m2 * cols; e += kTeam) {
-      const int r = k + 1 + e % m2, cj = e / m2;
-      const T fm = A[r + LDA * k];
-      if (cj < m2) A[r + LDA * (k + 1 + cj)] -= fm * A[k + LDA * (k + 1 + cj)];
-      else B[r + LDA * (cj - m2)] -= fm * B[k + LDA * (cj - m2)];
+    if (r > k && r < n) {
+      const T inv = (T)1 / A[k + LDA * k];
+      const T fm = A[r + LDA * k] * inv;
+      A[r + LDA * k] = fm;
+      for (int j = k + 1; j < n; ++j) A[r + LDA * j] -= fm * A[k + LDA * j];
+      for (int j = 0; j < nrhs; ++j) B[r + LDA * j] -= fm * B[k + LDA * j];
     }
     tm.sync();
   }
-  // back substitution, right-looking over rows
   for (int i = n - 1; i >= 0; --i) {
     const T inv = (T)1 / A[i + LDA * i];
     for (int j = tm.lane; j < nrhs; j += kTeam) B[i + LDA * j] *= inv;
     tm.sync();
-    for (int e = tm.lane; e < i * nrhs; e += kTeam) {
-      const int r = e % i, j = e / i;
-      B[r + LDA * j] -= A[r + LDA * i] * B[i + LDA * j];
+    if (r < i) {
+      const T a = A[r + LDA * i];
+      for (int j = 0; j < nrhs; ++j) B[r + LDA * j] -= a * B[i + LDA * j];
     }
     tm.sync();
   }
@@ -227,7 +241,7 @@ RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int*
   const T tol = Eps<T>::v * (T)n;
   bool done = false;
   for (int sweep = 0; sweep < 30 && !done; ++sweep) {
-    T off = 0;  // largest normalised off-diagonal rotated in this sweep (see jacobi_svd)
+    bool unconverged = false;  // see jacobi_svd
     for (int round = 0; round < n - 1; ++round) {
       int p = 0, q = 0;
       if (act) {
@@ -244,12 +258,10 @@ RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int*
       al = group_sum<LPP>(tm, al, red);
       be = group_sum<LPP>(tm, be, red);
       ga = group_sum<LPP>(tm, ga, red);
-      const T nb = sqrt(al * be);
-      if (act && fabs(ga) > tol * nb) {
-        if (fabs(ga) > off * nb) off = fabs(ga) / nb;
-        const T zeta = (be - al) / ((T)2 * ga);
-        const T t = copysign((T)1, zeta) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
-        const T cs = (T)1 / sqrt((T)1 + t * t), sn = cs * t;
+      const Rotation<T> rot(al, be, ga, tol);
+      if (act && rot.rotate) {
+        unconverged = unconverged || rot.unconverged;
+        const T cs = rot.cs, sn = rot.sn;
         for (int i = sub; i < n; i += LPP) {
           const T gp = G[i + LD * p], gq = G[i + LD * q];
           G[i + LD * p] = cs * gp - sn * gq;
@@ -261,7 +273,7 @@ RT_HD bool team_jacobi(const Team& tm, int n, T* G, T* V, T* sigma, T* red, int*
       }
       tm.sync();
     }
-    done = !team_any(tm, off * off > tol, flag);
+    done = !team_any(tm, unconverged, flag);
   }
   if (tm.lane < n) {
     T s = 0;
@@ -315,18 +327,45 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
   T* G = M.work + 3 * NS * LD;
   T* V = M.work + 4 * NS * LD;
   const T dtau = M.lsc[0], om1 = M.lsc[1];
-  // Sp (even l-m) and Sm (odd l-m) contractions of omega*beta_l P_l(mu_i) P_l(mu_j)
-  for (int e = tm.lane; e < N * N; e += kTeam) {
-    const int i = e % N, j = e / N;
-    T se = 0, so = 0;
-    for (int l = m; l <= NM; ++l) {
-      const T t = M.og[l] * M.piq[i][l] * M.piq[j][l];
-      if (((l - m) & 1) == 0) se += t; else so += t;
+  // Sp (even l-m) and Sm (odd l-m) contractions of omega*beta_l P_l(mu_i) P_l(mu_j),
+  // symmetric: the lower triangle only (Sp mirrored; Bs is read below its
+  // diagonal only).  Element e of the folded triangle: row pairs (r, N-1-r)
+  // hold N+1 elements together (N even).
+  // Each lane keeps its U elements' sums in registers (U independent chains).
+  {
+    constexpr int NE = (NS / 2) * (NS + 1), U = (NE + kTeam - 1) / kTeam;
+    int ii[U], jj[U];
+    T se[U], so[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = tm.lane + kTeam * u, r = e / (N + 1), cc = e % (N + 1);
+      ii[u] = (cc <= r) ? r : N - 1 - r;
+      jj[u] = (cc <= r) ? cc : cc - r - 1;
+      se[u] = 0;
+      so[u] = 0;
     }
-    Sp[i + LD * j] = se;
-    T b = -c.sqw[i] * c.sqw[j] * so;
-    if (i == j) b += (T)1;
-    Bs[i + LD * j] = b;
+    for (int l = m; l <= NM; ++l) {
+      const T og = M.og[l];
+      const bool even = ((l - m) & 1) == 0;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (tm.lane + kTeam * u < NE) {
+          const T t = og * M.piq[ii[u]][l] * M.piq[jj[u]][l];
+          if (even) se[u] += t; else so[u] += t;
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (tm.lane + kTeam * u < NE) {
+        const int i = ii[u], j = jj[u];
+        Sp[i + LD * j] = se[u];
+        Sp[j + LD * i] = se[u];
+        T b = -c.sqw[i] * c.sqw[j] * so[u];
+        if (i == j) b += (T)1;
+        Bs[i + LD * j] = b;
+      }
+    }
   }
   tm.sync();
   if (!team_cholesky<LD>(tm, N, Bs)) return RT_EIGEN_FAIL;
@@ -645,20 +684,44 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
       for (int i = tm.lane; i < N; i += kTeam) { M.f[i] = R[i + LK * N]; sw[swl.f + i + NS * (long)n] = M.f[i]; }
       tm.sync();
     } else {
-      for (int e = tm.lane; e < N * N; e += kTeam) {
-        const int i = e % N, j = e / N;
-        T gt = M.Q[prev][i + LD * j], gb = M.P[prev][i + LD * j];
-        for (int k = 0; k < N; ++k) {
-          const T tf = M.t[prev][k] * M.F[k + LD * j];
-          gt += M.P[prev][i + LD * k] * tf;
-          gb += M.Q[prev][i + LD * k] * tf;
+      {
+        // U elements per lane, their 2U sums in registers (independent chains)
+        constexpr int NE = NS * NS, U = (NE + kTeam - 1) / kTeam;
+        T gt[U], gb[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int e = tm.lane + kTeam * u;
+          if (e < NE) {
+            gt[u] = M.Q[prev][e % N + LD * (e / N)];
+            gb[u] = M.P[prev][e % N + LD * (e / N)];
+          }
         }
-        K[i + LK * j] = gt;
-        K[N + i + LK * j] = gb;
-        K[i + LK * (N + j)] = -M.P[cur][i + LD * j];
-        K[N + i + LK * (N + j)] = -M.Q[cur][i + LD * j];
-        R[i + LK * j] = M.Q[cur][i + LD * j] * M.t[cur][j];
-        R[N + i + LK * j] = M.P[cur][i + LD * j] * M.t[cur][j];
+        for (int k = 0; k < N; ++k) {
+          const T tk = M.t[prev][k];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int e = tm.lane + kTeam * u;
+            if (e < NE) {
+              const int i = e % N, j = e / N;
+              const T tf = tk * M.F[k + LD * j];
+              gt[u] += M.P[prev][i + LD * k] * tf;
+              gb[u] += M.Q[prev][i + LD * k] * tf;
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int e = tm.lane + kTeam * u;
+          if (e < NE) {
+            const int i = e % N, j = e / N;
+            K[i + LK * j] = gt[u];
+            K[N + i + LK * j] = gb[u];
+            K[i + LK * (N + j)] = -M.P[cur][i + LD * j];
+            K[N + i + LK * (N + j)] = -M.Q[cur][i + LD * j];
+            R[i + LK * j] = M.Q[cur][i + LD * j] * M.t[cur][j];
+            R[N + i + LK * j] = M.P[cur][i + LD * j] * M.t[cur][j];
+          }
+        }
       }
       for (int i = tm.lane; i < N; i += kTeam) {
         T gt = 0, gb = 0;
