@@ -8,13 +8,13 @@
 // the reference's default-REAL literals enter as the nearest float, and its
 // all-literal subexpressions are evaluated in single precision.
 //
-// Layout: one block per (pixel, channel) column.  Its threads compute the
-// volume scattering coefficient at the km+1 edges once each (two FP64
-// divisions per edge) into shared memory, then the km layer values
-// (trapezoid in height).  The per-channel cross section A(lambda) is computed
-// once per block.  Reads pe/he/te (3 x (km+1) doubles per pixel, shared by the
-// channels through L2), writes km doubles per column: HBM-bound at large
-// batches.
+// Layout: a 2-D grid, y = channel.  A block computes the channel's cross
+// section A(lambda) once, then walks groups of pixels: the volume scattering
+// coefficient at each of the km+1 edges once (two FP64 divisions per edge,
+// into shared memory), then the km layer values (trapezoid in height).
+// Reads pe/he/te (3 x (km+1) doubles per pixel and channel; the channels'
+// re-reads of a pixel mostly hit L2), writes km doubles per pixel and channel:
+// HBM-bound at large batches.
 #include "aerort_internal.cuh"
 
 namespace aerort_internal {
@@ -102,30 +102,31 @@ __host__ __device__ inline double depolarisation(double x) {
   return dd(dm(6.0, ds(f, 1.0)), da(dm(7.0, f), 3.0));
 }
 
+// grid (x: pixel groups, y: channel); each block iteration takes cpb pixels
+// whose (km+1)-edge profiles are contiguous, so thread t reads edge word t of
+// the group (coalesced) and writes layer word t.
 __global__ void k_rot_calc(int km, int nch, int nobs, const double* __restrict__ channels,
                            const double* __restrict__ pe, const double* __restrict__ he,
                            const double* __restrict__ te, double* __restrict__ rot, double* __restrict__ depol) {
-  extern __shared__ double vol[];  // km + 1 edge values of the current column
-  __shared__ double a_ns;
+  extern __shared__ double vol[];  // cpb x (km + 1) edge values of the current pixel group
   const double ps = LIT(1013.25), ts = LIT(288.15);
-  for (long col = blockIdx.x; col < (long)nobs * nch; col += gridDim.x) {
-    const int j = (int)(col % nobs), i = (int)(col / nobs);
-    const double wmicron = dm(channels[i], LIT(1.E-3));
-    if (threadIdx.x == 0) {
-      a_ns = dm(rayleigh_cross_section(wmicron), ns_standard());
-      if (j == 0) depol[i] = depolarisation(wmicron);
-    }
+  const int i = blockIdx.y, ne = km + 1;
+  const int cpb = blockDim.x / ne > 0 ? blockDim.x / ne : 1;
+  const double wmicron = dm(channels[i], LIT(1.E-3));
+  const double a_ns = dm(rayleigh_cross_section(wmicron), ns_standard());
+  if (blockIdx.x == 0 && threadIdx.x == 0) depol[i] = depolarisation(wmicron);
+  for (long j0 = (long)blockIdx.x * cpb; j0 < nobs; j0 += (long)gridDim.x * cpb) {
+    const long nj = (nobs - j0 < cpb) ? nobs - j0 : cpb;
+    const long base = (long)ne * j0;
+    for (int t = threadIdx.x; t < nj * ne; t += blockDim.x)
+      vol[t] = dm(dm(dm(a_ns, dd(dm(pe[base + t], LIT(1.E-2)), ps)), dd(ts, te[base + t])), LIT(1.E5));
     __syncthreads();
-    const double* p = pe + (long)(km + 1) * j;
-    const double* t = te + (long)(km + 1) * j;
-    const double* z = he + (long)(km + 1) * j;
-    for (int k = threadIdx.x; k <= km; k += blockDim.x)
-      vol[k] = dm(dm(dm(a_ns, dd(dm(p[k], LIT(1.E-2)), ps)), dd(ts, t[k])), LIT(1.E5));
-    __syncthreads();
-    double* out = rot + (long)km * (j + (long)nobs * i);
-    for (int k = threadIdx.x; k < km; k += blockDim.x) {
+    double* out = rot + (long)km * (j0 + (long)nobs * i);
+    for (int t = threadIdx.x; t < nj * km; t += blockDim.x) {
+      const int c = t / km, k = t - c * km;
+      const double* z = he + base + (long)ne * c;
       const double difz = ds(dm(z[k], LIT(1.E-3)), dm(z[k + 1], LIT(1.E-3)));
-      out[k] = dd(dm(difz, da(vol[k], vol[k + 1])), 2.0);
+      out[t] = dd(dm(difz, da(vol[ne * c + k], vol[ne * c + k + 1])), 2.0);
     }
     __syncthreads();
   }
@@ -134,19 +135,24 @@ __global__ void k_rot_calc(int km, int nch, int nobs, const double* __restrict__
 int rot_checks(int km, int nch, int nobs) {
   if (km <= 0 || nch <= 0 || nobs < 0) return set_error(AERORT_RC_ARG, "rot_calc: bad sizes");
   if ((size_t)(km + 1) * sizeof(double) > 200 * 1024) return set_error(AERORT_RC_NLAYERS, "rot_calc: km too large");
+  if (nch > 65535) return set_error(AERORT_RC_ARG, "rot_calc: nch > 65535");
   return 0;
 }
 
 int launch_rot(int km, int nch, int nobs, const double* channels, const double* pe, const double* he,
                const double* te, double* rot, double* depol, cudaStream_t s, int num_sms) {
   if (nobs == 0) return 0;
-  const size_t smem = (size_t)(km + 1) * sizeof(double);
+  constexpr int kThreads = 256;
+  const int ne = km + 1, cpb = kThreads / ne > 0 ? kThreads / ne : 1;
+  const size_t smem = (size_t)cpb * ne * sizeof(double);
   if (smem > 48 * 1024)
     CUDA_TRY(cudaFuncSetAttribute(k_rot_calc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  long blocks = (long)nobs * nch;
-  const long cap = (long)num_sms * 16;
-  if (blocks > cap) blocks = cap;
-  k_rot_calc<<<(unsigned)blocks, 128, smem, s>>>(km, nch, nobs, channels, pe, he, te, rot, depol);
+  long bx = (nobs + cpb - 1) / cpb;
+  long cap = (long)num_sms * 16 / nch;  // about 16 resident blocks per SM over all channels
+  if (cap < 1) cap = 1;
+  if (bx > cap) bx = cap;
+  k_rot_calc<<<dim3((unsigned)bx, (unsigned)nch), kThreads, smem, s>>>(km, nch, nobs, channels, pe, he, te, rot,
+                                                                       depol);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }

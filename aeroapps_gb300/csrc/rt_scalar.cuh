@@ -179,11 +179,13 @@ RT_HD void apply_reflector_sym(int n, T* A, const T* v, T beta) {
 // sigma[a] = |G e_a| (the singular values, with the relative accuracy of a
 // column-graded G) and the columns of V are the right singular vectors, i.e.
 // the eigenvectors of G^T G.  Returns false if the sweep budget is exhausted.
-// 1/sqrt(x): the hardware reciprocal square root on the device.
+// 1/sqrt(x), correctly rounded in FP32 on the device (the approximate
+// hardware rsqrtf lets cs^2 + sn^2 drift from 1 by a few ulp per rotation,
+// which the hundreds of rotations of one eigen-solve accumulate).
 template <typename T>
 RT_HD T rsqrt_t(T x) {
 #ifdef __CUDA_ARCH__
-  if constexpr (sizeof(T) == sizeof(float)) return rsqrtf(x);
+  if constexpr (sizeof(T) == sizeof(float)) return __frsqrt_rn(x);
   else return rsqrt(x);
 #else
   return (T)1 / sqrt(x);

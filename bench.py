@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--cols", type=int, default=8192, help="columns per step per GPU (x4 wavelengths = solves)")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 solve")
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--cpu-cols", type=int, default=0, help="CPU-baseline sample columns (0 = auto)")
+    ap.add_argument("--cpu-cols", type=int, default=0, help="CPU-baseline sample columns (0 = 2048, or 512 per step "
+                    "of --impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate [requests/s]")
@@ -241,7 +242,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    batch = make_batch(max(args.cpu_cols or 64, 8), seed=20261204)
+    batch = make_batch(max(args.cpu_cols or 512, 8), seed=20261204)  # about 2-5 s per step on 8-16 cores
     ncols = batch["ncol"]
     times = []
     for i in range(args.warmup + args.steps):
@@ -491,6 +492,50 @@ def main():
         e2e_val = solves / ((time.perf_counter() - t) / args.e2e_steps)
         assert np.isfinite(got)
 
+    # ---------------------------------------------------------------- Rayleigh optical thickness kernel
+    # VLIDORT_ROT_CALC on the device for the whole batch (km = 72 edges profiles):
+    # algorithmic bytes = pe, he, te read once per pixel + ROT written per pixel
+    # and channel (+ depol); HBM-bound, against the measured copy bandwidth
+    rot_line = None
+    if rank == 0:
+        # the 262,144 columns of the batching configuration: this batch's edge
+        # profiles tiled (Fortran (km+1, columns) = C (columns, km+1))
+        kmb = batch["km"]
+        ncr = 262144
+        tile = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float64).T)).cuda().repeat(
+            (ncr + my_cols - 1) // my_cols, 1)[:ncr].contiguous()
+        dpe, dhe, dte = (tile(batch[k]) for k in ("pe", "he", "te"))
+        dch = dev(np.array(CHANNELS), np.float64)
+        drot = torch.empty(kmb * ncr * nch, dtype=torch.float64, device="cuda")
+        ddep = torch.empty(nch, dtype=torch.float64, device="cuda")
+        call = lambda: L.aerort_vlidort_rot_calc_dev(kmb, nch, ncr, P(dch), P(dpe), P(dhe), P(dte), P(drot),
+                                                     P(ddep), stream)
+        for _ in range(3):
+            assert call() == 0, _lib.last_error()
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > L2: each launch reads from HBM
+        reps, ms_rot = 20, 0.0
+        for _ in range(reps):
+            flush.zero_()
+            r0, r1 = ev(), ev()
+            r0.record()
+            call()
+            r1.record()
+            torch.cuda.synchronize()
+            ms_rot += r0.elapsed_time(r1) / reps
+        del flush, dpe, dhe, dte, drot
+        alg = 3 * (kmb + 1) * 8 * ncr + kmb * ncr * nch * 8 + nch * 8
+        peak = None
+        try:
+            peak = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")))["hbm_gbs"]
+            src = "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy), of measured"
+        except (OSError, ValueError, KeyError):
+            peak, src = 6800.0, "fallback 6.8 TB/s, of fallback"
+        ach = alg / (ms_rot * 1e-3) / 1e9
+        rot_line = {"kernel": "k_rot_calc (VLIDORT_ROT_CALC)", "bound": "hbm", "ms_per_launch": ms_rot,
+                    "algorithmic_bytes": alg, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                    "peak_source": src, "columns": ncr, "wavelengths": nch, "layers": kmb,
+                    "note": "L2 flushed (512 MB write) before each timed launch"}
+
     # ---------------------------------------------------------------- serving
     serving = None
     if not args.no_serve and rank == 0 and args.serve_requests > 0:
@@ -539,7 +584,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(batch, args.cpu_cols or 32)
+        cpu = cpu_baseline(batch, min(args.cpu_cols or 2048, my_cols))  # about 10 s on a 16-core host
     # inside the timed mixed steps, per stream group: the AOP kernel, then for the FP32 pass and for the FP64
     # re-solve of its list each a scheduler init, the nadir flag and the RT kernel
     launches = 7 * len(groups) * args.steps
@@ -561,7 +606,7 @@ def main():
                 "path": "pinned host inputs -> device copies, aerort_get_aop_vector_dev + "
                         "aerort_vlidort_scalar_lambert_mixed_batch_dev per stream group (%s), device -> pinned host "
                         "outputs, host read" % ("one CUDA stream per group" if side else "one stream")},
-        "serving": serving, "gpu_launches": launches, "clocks": clk,
+        "serving": serving, "gpu_launches": launches, "clocks": clk, "rot_calc": rot_line,
     }
     if rank == 0:
         print(json.dumps(line))
