@@ -8,13 +8,12 @@
 // the reference's default-REAL literals enter as the nearest float, and its
 // all-literal subexpressions are evaluated in single precision.
 //
-// Layout: a 2-D grid, y = channel.  A block computes the channel's cross
-// section A(lambda) once, then walks groups of pixels: the volume scattering
-// coefficient at each of the km+1 edges once (two FP64 divisions per edge,
-// into shared memory), then the km layer values (trapezoid in height).
-// Reads pe/he/te (3 x (km+1) doubles per pixel and channel; the channels'
-// re-reads of a pixel mostly hit L2), writes km doubles per pixel and channel:
-// HBM-bound at large batches.
+// Layout: blocks walk groups of pixels; per group the channel-independent
+// edge quotients and layer height differences go to shared memory once, then
+// every channel's km layer values are written.  Reads pe/he/te once (3 x
+// (km+1) doubles per pixel), writes km doubles per pixel and channel.  On
+// GB300 the FP64 divisions (two per edge) and multiplications set the pace
+// rather than HBM.
 #include "aerort_internal.cuh"
 
 namespace aerort_internal {
@@ -102,31 +101,54 @@ __host__ __device__ inline double depolarisation(double x) {
   return dd(dm(6.0, ds(f, 1.0)), da(dm(7.0, f), 3.0));
 }
 
-// grid (x: pixel groups, y: channel); each block iteration takes cpb pixels
-// whose (km+1)-edge profiles are contiguous, so thread t reads edge word t of
-// the group (coalesced) and writes layer word t.
+// Each block iteration takes cpb pixels, whose (km+1)-edge profiles are
+// contiguous: thread t reads edge word t of the group (coalesced).  The two
+// divisions of an edge, (p/Ps) and (Ts/T), and the height difference of a
+// layer do not depend on the channel, so they are formed once per pixel; per
+// channel only the products with A(lambda) Ns remain.  The reference's
+// evaluation order ((A Ns) (p/Ps)) (Ts/T) 1e5 allows exactly this split.
+// Division by 2 is the exact product with 0.5.
 __global__ void k_rot_calc(int km, int nch, int nobs, const double* __restrict__ channels,
                            const double* __restrict__ pe, const double* __restrict__ he,
                            const double* __restrict__ te, double* __restrict__ rot, double* __restrict__ depol) {
-  extern __shared__ double vol[];  // cpb x (km + 1) edge values of the current pixel group
+  // shared: A(lambda) Ns per channel; cpb x (km+1) p/Ps and Ts/T; cpb x km layer height differences
+  extern __shared__ double sm[];
   const double ps = LIT(1013.25), ts = LIT(288.15);
-  const int i = blockIdx.y, ne = km + 1;
+  const int ne = km + 1;
   const int cpb = blockDim.x / ne > 0 ? blockDim.x / ne : 1;
-  const double wmicron = dm(channels[i], LIT(1.E-3));
-  const double a_ns = dm(rayleigh_cross_section(wmicron), ns_standard());
-  if (blockIdx.x == 0 && threadIdx.x == 0) depol[i] = depolarisation(wmicron);
+  double* ans = sm;
+  double* qp = sm + nch;
+  double* qt = qp + cpb * ne;
+  double* dz = qt + cpb * ne;
+  for (int i = threadIdx.x; i < nch; i += blockDim.x) {
+    const double wmicron = dm(channels[i], LIT(1.E-3));
+    ans[i] = dm(rayleigh_cross_section(wmicron), ns_standard());
+    if (blockIdx.x == 0) depol[i] = depolarisation(wmicron);
+  }
+  __syncthreads();
   for (long j0 = (long)blockIdx.x * cpb; j0 < nobs; j0 += (long)gridDim.x * cpb) {
     const long nj = (nobs - j0 < cpb) ? nobs - j0 : cpb;
     const long base = (long)ne * j0;
-    for (int t = threadIdx.x; t < nj * ne; t += blockDim.x)
-      vol[t] = dm(dm(dm(a_ns, dd(dm(pe[base + t], LIT(1.E-2)), ps)), dd(ts, te[base + t])), LIT(1.E5));
-    __syncthreads();
-    double* out = rot + (long)km * (j0 + (long)nobs * i);
+    for (int t = threadIdx.x; t < nj * ne; t += blockDim.x) {
+      qp[t] = dd(dm(pe[base + t], LIT(1.E-2)), ps);
+      qt[t] = dd(ts, te[base + t]);
+    }
     for (int t = threadIdx.x; t < nj * km; t += blockDim.x) {
       const int c = t / km, k = t - c * km;
       const double* z = he + base + (long)ne * c;
-      const double difz = ds(dm(z[k], LIT(1.E-3)), dm(z[k + 1], LIT(1.E-3)));
-      out[t] = dd(dm(difz, da(vol[ne * c + k], vol[ne * c + k + 1])), 2.0);
+      dz[t] = ds(dm(z[k], LIT(1.E-3)), dm(z[k + 1], LIT(1.E-3)));
+    }
+    __syncthreads();
+    for (int i = 0; i < nch; ++i) {
+      const double a_ns = ans[i];
+      double* out = rot + (long)km * (j0 + (long)nobs * i);
+      for (int t = threadIdx.x; t < nj * km; t += blockDim.x) {
+        const int c = t / km, k = t - c * km;
+        const int e = ne * c + k;
+        const double v0 = dm(dm(dm(a_ns, qp[e]), qt[e]), LIT(1.E5));
+        const double v1 = dm(dm(dm(a_ns, qp[e + 1]), qt[e + 1]), LIT(1.E5));
+        out[t] = dm(dm(dz[t], da(v0, v1)), 0.5);
+      }
     }
     __syncthreads();
   }
@@ -134,8 +156,8 @@ __global__ void k_rot_calc(int km, int nch, int nobs, const double* __restrict__
 
 int rot_checks(int km, int nch, int nobs) {
   if (km <= 0 || nch <= 0 || nobs < 0) return set_error(AERORT_RC_ARG, "rot_calc: bad sizes");
-  if ((size_t)(km + 1) * sizeof(double) > 200 * 1024) return set_error(AERORT_RC_NLAYERS, "rot_calc: km too large");
-  if (nch > 65535) return set_error(AERORT_RC_ARG, "rot_calc: nch > 65535");
+  if (((size_t)3 * (km + 1) + nch) * sizeof(double) > 200 * 1024)
+    return set_error(AERORT_RC_NLAYERS, "rot_calc: km or nch too large");
   return 0;
 }
 
@@ -144,15 +166,13 @@ int launch_rot(int km, int nch, int nobs, const double* channels, const double* 
   if (nobs == 0) return 0;
   constexpr int kThreads = 256;
   const int ne = km + 1, cpb = kThreads / ne > 0 ? kThreads / ne : 1;
-  const size_t smem = (size_t)cpb * ne * sizeof(double);
+  const size_t smem = ((size_t)cpb * (3 * ne) + nch) * sizeof(double);
   if (smem > 48 * 1024)
     CUDA_TRY(cudaFuncSetAttribute(k_rot_calc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  long bx = (nobs + cpb - 1) / cpb;
-  long cap = (long)num_sms * 16 / nch;  // about 16 resident blocks per SM over all channels
-  if (cap < 1) cap = 1;
-  if (bx > cap) bx = cap;
-  k_rot_calc<<<dim3((unsigned)bx, (unsigned)nch), kThreads, smem, s>>>(km, nch, nobs, channels, pe, he, te, rot,
-                                                                       depol);
+  long blocks = (nobs + cpb - 1) / cpb;
+  const long cap = (long)num_sms * 8;  // about 8 resident 256-thread blocks per SM
+  if (blocks > cap) blocks = cap;
+  k_rot_calc<<<(unsigned)blocks, kThreads, smem, s>>>(km, nch, nobs, channels, pe, he, te, rot, depol);
   CUDA_TRY(cudaGetLastError());
   return 0;
 }

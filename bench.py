@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--cols", type=int, default=8192, help="columns per step per GPU (x4 wavelengths = solves)")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 solve")
     ap.add_argument("--e2e-steps", type=int, default=1)
-    ap.add_argument("--cpu-cols", type=int, default=0, help="CPU-baseline sample columns (0 = 2048, or 512 per step "
+    ap.add_argument("--cpu-cols", type=int, default=0, help="CPU-baseline sample columns (0 = 4096, or 512 per step "
                     "of --impl reference)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=32)
@@ -380,6 +380,12 @@ def main():
                 tuned["%s N%d" % ("mixed" if prec else "fp64", d["N"])] = (
                     "team" if r["kernel"] == _lib.KERNEL_TEAM else "thread", r["threads"], r["blocks_per_sm"])
 
+    # Concurrent groups: launch the costliest (most streams) first, so that the
+    # cheap groups fill its tail rather than the reverse.  (Capping each
+    # group's resident blocks to a cost-proportional share of the SMs was
+    # measured slower: SMs freed by a group that finishes early stay idle.)
+    groups.sort(key=lambda d: -d["N"])
+
     # ---------------------------------------------------------------- mixed (headline)
     for _ in range(args.warmup):
         step(_lib.PREC_MIXED)
@@ -584,7 +590,7 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(batch, min(args.cpu_cols or 2048, my_cols))  # about 10 s on a 16-core host
+        cpu = cpu_baseline(batch, min(args.cpu_cols or 4096, my_cols))  # about 10 s on a 16-core host
     # inside the timed mixed steps, per stream group: the AOP kernel, then for the FP32 pass and for the FP64
     # re-solve of its list each a scheduler init, the nadir flag and the RT kernel
     launches = 7 * len(groups) * args.steps
@@ -596,7 +602,8 @@ def main():
                    "columns_per_step": args.cols, "solves_per_step": solves, "wavelengths": list(CHANNELS),
                    "l2": "inputs larger than L2 (optics + scratch of a step: hundreds of MB)",
                    "failed_solves": bad, "tuned_schedules": tuned or None, "launch": graph_note,
-                   "groups": "concurrent, one CUDA stream per stream count" if side else "serial, one CUDA stream"},
+                   "groups": "concurrent, one CUDA stream per stream count, most streams first" if side
+                   else "serial, one CUDA stream"},
         "accuracy": {"max_rel_err_vs_fp64": float(err.max()), "median_rel_err_vs_fp64": float(np.median(err)),
                      "radiances_compared": int(err.size), "bar": 1e-4},
         "plain_fp64": {"value": plain_value, "unit": "radiances/s", "ms_per_step": ms_plain,
