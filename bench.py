@@ -380,11 +380,12 @@ def main():
                 tuned["%s N%d" % ("mixed" if prec else "fp64", d["N"])] = (
                     "team" if r["kernel"] == _lib.KERNEL_TEAM else "thread", r["threads"], r["blocks_per_sm"])
 
-    # Concurrent groups: launch the costliest (most streams) first, so that the
-    # cheap groups fill its tail rather than the reverse.  (Capping each
-    # group's resident blocks to a cost-proportional share of the SMs was
-    # measured slower: SMs freed by a group that finishes early stay idle.)
-    groups.sort(key=lambda d: -d["N"])
+    # Concurrent groups are launched in stream-count order; each group's
+    # persistent kernel takes the SMs it can get, and the next groups' blocks
+    # fill them as it drains.  (Measured on GB300: capping each group's resident
+    # blocks to a cost-proportional share of the SMs was 25% slower, since SMs
+    # freed by a group that finishes early stay idle; launching the costliest
+    # group first was no faster.)
 
     # ---------------------------------------------------------------- mixed (headline)
     for _ in range(args.warmup):
@@ -538,6 +539,9 @@ def main():
             peak, src = 6800.0, "fallback 6.8 TB/s, of fallback"
         ach = alg / (ms_rot * 1e-3) / 1e9
         rot_line = {"kernel": "k_rot_calc (VLIDORT_ROT_CALC)", "bound": "hbm", "ms_per_launch": ms_rot,
+                    "limiter": "FP64 issue: two correctly rounded FP64 divisions per layer edge and pixel (bit "
+                               "identity with the reference rules out reciprocal products); GB300 runs FP64 at "
+                               "about 1 TFLOP/s",
                     "algorithmic_bytes": alg, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                     "peak_source": src, "columns": ncr, "wavelengths": nch, "layers": kmb,
                     "note": "L2 flushed (512 MB write) before each timed launch"}
@@ -602,8 +606,7 @@ def main():
                    "columns_per_step": args.cols, "solves_per_step": solves, "wavelengths": list(CHANNELS),
                    "l2": "inputs larger than L2 (optics + scratch of a step: hundreds of MB)",
                    "failed_solves": bad, "tuned_schedules": tuned or None, "launch": graph_note,
-                   "groups": "concurrent, one CUDA stream per stream count, most streams first" if side
-                   else "serial, one CUDA stream"},
+                   "groups": "concurrent, one CUDA stream per stream count" if side else "serial, one CUDA stream"},
         "accuracy": {"max_rel_err_vs_fp64": float(err.max()), "median_rel_err_vs_fp64": float(np.median(err)),
                      "radiances_compared": int(err.size), "bar": 1e-4},
         "plain_fp64": {"value": plain_value, "unit": "radiances/s", "ms_per_step": ms_plain,
