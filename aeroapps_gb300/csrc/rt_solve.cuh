@@ -1065,10 +1065,13 @@ struct SetupRecord {
 };
 
 // Fourier-series context in the working precision from a set-up record.
+// sqrt(1 - x^2) of a cosine, formed in FP64 (exactly 0 at x = 1).
+RT_HD double quad_sine(double x) { return (x == 1.0) ? 0.0 : sqrt(1.0 - x * x); }
+
 template <int NS, typename T>
 RT_HD void make_ctx(const SetupRecord& r, const double* qx, const double* qw, SolveCtx<NS, T>& c) {
   c.L = r.L; c.NM = r.NM; c.cutoff = r.cutoff; c.msmode = r.msmode; c.refl_directbeam = r.refl_directbeam;
-  auto sine = [](double x) { return (x == 1.0) ? 0.0 : sqrt(1.0 - x * x); };
+  auto sine = quad_sine;
   for (int q = 0; q < NS; ++q) {
     c.qx[q] = (T)qx[q]; c.qw[q] = (T)qw[q]; c.sqw[q] = (T)sqrt(qw[q]); c.pimm_q[q] = 0;
     c.sin_q[q] = (T)sine(qx[q]);

@@ -135,6 +135,7 @@ struct TeamMem {
   T t[2][NS], wt[2][2 * NS], wb[2][2 * NS];
   T F[NS * LD], f[NS];               // L = F M + f of the current interface
   T Vp[NS * LD];                     // previous layer's Jacobi rotations (warm start)
+  T cqx[NS], cqw[NS], csqw[NS], csin[NS];  // quadrature cosines, weights, sqrt(weights), sines
   int vp_valid;
   T red[kTeam];
   int ired[kTeam];
@@ -300,7 +301,7 @@ RT_HD void team_legendre(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T
   const int i = tm.lane;
   if (i < NS + 2) {
     T x, s, *pim, *out;
-    if (i < NS) { x = c.qx[i]; s = c.sin_q[i]; pim = &M.pimq[i]; out = M.piq[i]; }
+    if (i < NS) { x = M.cqx[i]; s = M.csin[i]; pim = &M.pimq[i]; out = M.piq[i]; }
     else if (i == NS) { x = c.mu_u; s = c.sin_u; pim = &M.pimu; out = M.piu; }
     else { x = c.cos_sza; s = c.sin_0; pim = &M.pim0; out = M.pi0; }
     for (int l = 0; l < m && l <= NM; ++l) out[l] = 0;
@@ -361,7 +362,7 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
         const int i = ii[u], j = jj[u];
         Sp[i + LD * j] = se[u];
         Sp[j + LD * i] = se[u];
-        T b = -c.sqw[i] * c.sqw[j] * so[u];
+        T b = -M.csqw[i] * M.csqw[j] * so[u];
         if (i == j) b += (T)1;
         Bs[i + LD * j] = b;
       }
@@ -372,12 +373,12 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
   // R = M^-1 Lb
   for (int e = tm.lane; e < N * N; e += kTeam) {
     const int i = e % N, j = e / N;
-    if (i >= j) Bs[i + LD * j] /= c.qx[i];
+    if (i >= j) Bs[i + LD * j] /= M.cqx[i];
   }
   // As = I - W^1/2 Sp W^1/2 (full)
   for (int e = tm.lane; e < N * N; e += kTeam) {
     const int i = e % N, j = e / N;
-    T a = -c.sqw[i] * Sp[i + LD * j] * c.sqw[j];
+    T a = -M.csqw[i] * Sp[i + LD * j] * M.csqw[j];
     if (i == j) a += (T)1;
     H[i + LD * j] = a;
   }
@@ -385,15 +386,15 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
   if (m == 0) {
     // exact split of the conservative mode (see layer_eigen): Q As Q, reflector v
     T ns = 0;
-    for (int i = 0; i < N; ++i) ns += c.sqw[i] * c.sqw[i];
+    for (int i = 0; i < N; ++i) ns += M.csqw[i] * M.csqw[i];
     ns = sqrt(ns);
     T vv = 0;
     for (int i = 0; i < N; ++i) {
-      const T vi = c.sqw[i] + (i == 0 ? ns : (T)0);
+      const T vi = M.csqw[i] + (i == 0 ? ns : (T)0);
       vv += vi * vi;
     }
     const T beta = (T)2 / vv;
-    if (tm.lane < N) M.rv[tm.lane] = c.sqw[tm.lane] + (tm.lane == 0 ? ns : (T)0);
+    if (tm.lane < N) M.rv[tm.lane] = M.csqw[tm.lane] + (tm.lane == 0 ? ns : (T)0);
     if (tm.lane == 0) M.rbeta = beta;
     tm.sync();
     // p = beta A v ; w = p - (beta/2)(p.v) v ; A -= v w^T + w v^T
@@ -498,18 +499,18 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
       for (int i = 0; i < N; ++i) {
         T s = 0;
         for (int j = 0; j <= i; ++j) s += Bs[i + LD * j] * V[j + LD * a];
-        x[i] = s / c.sqw[i];
+        x[i] = s / M.csqw[i];
         nrm += x[i] * x[i];
       }
       nrm = (T)1 / sqrt(nrm);
       T nr = 0;
       for (int i = 0; i < N; ++i) {
         x[i] *= nrm;
-        const T dif = g[i] / (c.qx[i] * c.sqw[i]) * nrm;
+        const T dif = g[i] / (M.cqx[i] * M.csqw[i]) * nrm;
         g[i] = dif;  // keep dif for the user-angle solutions
         M.P[cur][i + LD * a] = (T)0.5 * (x[i] + dif);
         M.Q[cur][i + LD * a] = (T)0.5 * (x[i] - dif);
-        nr += c.qx[i] * c.qw[i] * x[i] * dif;
+        nr += M.cqx[i] * M.cqw[i] * x[i] * dif;
       }
       M.norm[a] = nr;
       const T help = k * dtau;
@@ -518,7 +519,7 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
       for (int l = m; l <= NM; ++l) {
         const bool even = ((l - m) & 1) == 0;
         T sps = 0;
-        for (int j = 0; j < N; ++j) sps += c.qw[j] * M.piq[j][l] * (even ? x[j] : g[j]);
+        for (int j = 0; j < N; ++j) sps += M.cqw[j] * M.piq[j][l] * (even ? x[j] : g[j]);
         const T h = (T)0.5 * M.og[l] * sps;
         dn += (even ? M.piu[l] : -M.piu[l]) * h;
         up += M.piu[l] * h;
@@ -597,8 +598,8 @@ RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<
       }
       T s1 = 0, s2 = 0;
       for (int i = 0; i < N; ++i) {
-        s1 += c.qw[i] * (M.dpi[i] * M.P[cur][i + LD * a] + M.dmi[i] * M.Q[cur][i + LD * a]);
-        s2 += c.qw[i] * (M.dmi[i] * M.P[cur][i + LD * a] + M.dpi[i] * M.Q[cur][i + LD * a]);
+        s1 += M.cqw[i] * (M.dpi[i] * M.P[cur][i + LD * a] + M.dmi[i] * M.Q[cur][i + LD * a]);
+        s2 += M.cqw[i] * (M.dmi[i] * M.P[cur][i + LD * a] + M.dpi[i] * M.Q[cur][i + LD * a]);
       }
       const T at = s1 / M.norm[a], bt = s2 / M.norm[a];
       M.gdn[a] = cf * at;
@@ -760,14 +761,14 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
     const int k = tm.lane;
     T sp = 0, sm = 0;
     for (int j = 0; j < N; ++j) {
-      sp += c.qx[j] * c.qw[j] * M.P[bl][j + LD * k];
-      sm += c.qx[j] * c.qw[j] * M.Q[bl][j + LD * k];
+      sp += M.cqx[j] * M.cqw[j] * M.P[bl][j + LD * k];
+      sm += M.cqx[j] * M.cqw[j] * M.Q[bl][j + LD * k];
     }
     M.dpi[k] = sp * kmult;   // r2p
     M.dmi[k] = sm * kmult;   // r2m
   }
   T r2b = 0;
-  for (int j = 0; j < N; ++j) r2b += c.qx[j] * c.qw[j] * M.wb[bl][j];
+  for (int j = 0; j < N; ++j) r2b += M.cqx[j] * M.cqw[j] * M.wb[bl][j];
   r2b *= kmult;
   tm.sync();
   for (int e = tm.lane; e < N * N; e += kTeam) {
@@ -803,7 +804,7 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
       const int i = tm.lane;
       T h = M.wb[bl][i];
       for (int k = 0; k < N; ++k) h += Lc[k] * M.P[bl][i + LD * k] * M.t[bl][k] + Mc[k] * M.Q[bl][i + LD * k];
-      M.red[i] = c.qx[i] * c.qw[i] * h;
+      M.red[i] = M.cqx[i] * M.cqw[i] * h;
     }
     tm.sync();
     T s = 0;
@@ -856,7 +857,14 @@ RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOption
                                int* nfourier, int* status, const Worklist& wl = Worklist(), int sidx = 0) {
   SolveCtx<NS, T> c;
   make_ctx<NS, T>(r, qx, qw, c);
-  if (tm.lane < NS) M.pimq[tm.lane] = 0;
+  if (tm.lane < NS) {
+    const int q = tm.lane;  // the quadrature arrays of make_ctx, in shared memory for lane-indexed access
+    M.cqx[q] = (T)qx[q];
+    M.cqw[q] = (T)qw[q];
+    M.csqw[q] = (T)sqrt(qw[q]);
+    M.csin[q] = (T)quad_sine(qx[q]);
+    M.pimq[q] = 0;
+  }
   if (tm.lane == 0) { M.pimu = 0; M.pim0 = 0; }
   tm.sync();
   const SweepLayout<NS> swl(r.L);

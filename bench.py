@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cols", type=int, default=8192, help="columns per step per GPU (x4 wavelengths = solves)")
+    ap.add_argument("--cols", type=int, default=16384, help="columns per step per GPU (x4 wavelengths = solves)")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed steps of the plain FP64 solve")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-cols", type=int, default=0, help="CPU-baseline sample columns (0 = 4096, or 512 per step "
