@@ -2,10 +2,9 @@
 
 A request is a swath of columns (each with its own stream count and layer
 count) at 1-8 wavelengths.  The server keeps the Mie tables resident on the
-device and owns a fixed set of slots.  Each slot has, per stream-count group,
-a CUDA stream and a caller-owned RT workspace (aerort_workspace), so that
-slots, and the groups of one request, run concurrently without sharing
-scratch.  A request is admitted as soon as a slot is free and
+device and owns a fixed set of slots.  Each slot has a CUDA stream and a
+caller-owned RT workspace (aerort_workspace), so that slots run concurrently
+without sharing scratch.  A request is admitted as soon as a slot is free and
 its device-memory estimate fits both the configured HBM budget (the device
 memory the server may hold for requests in flight) and the free device memory
 the driver reports.  Requests that arrive while others are on the GPU are
@@ -13,14 +12,15 @@ admitted as slots free up, and their kernels overlap on the device.  A request
 completes when the event recorded after its last device->host copy fires;
 latency is completion minus arrival.
 
-Per request, for every stream-count group of its columns, on the slot's
-stream for that group: host->device copy of the column inputs (pinned),
-VLIDORT_getAOPvector (aerort_get_aop_vector_dev, FP32), the RT solve
-(aerort_vlidort_scalar_lambert_ws_dev, mixed or FP64), device->host copy of
-radiance / reflectance / Fourier count / status; the slot's main stream then
-joins the group streams.  Every solve's result depends on its own inputs only
-(whichever thread or warp runs it), so a request's result is the same alone
-and in the mix.
+Per request, for every stream-count group of its columns, on the slot's stream:
+host->device copy of the column inputs (pinned), VLIDORT_getAOPvector
+(aerort_get_aop_vector_dev, FP32), the RT solve (aerort_vlidort_scalar_lambert_ws_dev,
+mixed or FP64), device->host copy of radiance / reflectance / Fourier count /
+status.  Every solve's result depends on its own inputs only (whichever thread
+or warp runs it), so a request's result is the same alone and in the mix.
+(One stream and workspace per stream-count group in each slot, so that a
+request's groups run concurrently, was measured on GB300: same latency at half
+capacity, 35% lower offline throughput.)
 """
 import collections
 import ctypes
@@ -122,23 +122,15 @@ class Server:
         # each slot's workspace holds 1/nslots of the threads the GPU keeps resident
         frac = slot_fraction if slot_fraction is not None else 1.0 / nslots
         threads = max(64, int(props.multi_processor_count * 256 * frac) // 64 * 64)
-        # per stream-count group, sized for 72-layer columns of that group
-        self.ws_group_bytes = [self.L.aerort_workspace_bytes_per_thread(72, n, self.prec) * threads
-                               for n in STREAMS]
-        self.ws_bytes = sum(self.ws_group_bytes)
+        per_thread = self.L.aerort_workspace_bytes_per_thread(72, 16, self.prec)
+        self.ws_bytes = per_thread * threads
         self.slots = []
         for _ in range(nslots):
-            # one CUDA stream and one workspace per stream-count group, so that
-            # the groups of a request run concurrently
-            wss = []
-            for nbytes in self.ws_group_bytes:
-                ws = ctypes.c_void_p()
-                rc = self.L.aerort_workspace_create(nbytes, ctypes.byref(ws))
-                if rc != 0:
-                    raise RuntimeError("workspace_create rc=%d: %s" % (rc, _lib.last_error()))
-                wss.append(ws)
-            self.slots.append({"stream": torch.cuda.Stream(), "sub": [torch.cuda.Stream() for _ in STREAMS],
-                               "ws": wss, "busy": None})
+            ws = ctypes.c_void_p()
+            rc = self.L.aerort_workspace_create(self.ws_bytes, ctypes.byref(ws))
+            if rc != 0:
+                raise RuntimeError("workspace_create rc=%d: %s" % (rc, _lib.last_error()))
+            self.slots.append({"stream": torch.cuda.Stream(), "ws": ws, "busy": None})
         self.queue = collections.deque()
         self.lock = threading.Lock()
         self.inflight_bytes = 0
@@ -151,10 +143,7 @@ class Server:
     def close(self):
         for s in self.slots:
             s["stream"].synchronize()
-            for ss in s["sub"]:
-                ss.synchronize()
-            for ws in s["ws"]:
-                self.L.aerort_workspace_destroy(ws)
+            self.L.aerort_workspace_destroy(s["ws"])
         self.slots = []
         self.chem.destroy()
 
@@ -171,15 +160,12 @@ class Server:
         ch32 = np.array(sw.channels, np.float32)
         keep = []
         outs = []
-        main = slot["stream"]
-        for gi, N in enumerate(STREAMS):
-            idx = np.nonzero(sw.nstreams == N)[0]
-            if len(idx) == 0:
-                continue
-            sub = slot["sub"][gi]
-            sub.wait_stream(main)
-            with torch.cuda.stream(sub):
-                st = sub.cuda_stream
+        with torch.cuda.stream(slot["stream"]):
+            st = slot["stream"].cuda_stream
+            for N in STREAMS:
+                idx = np.nonzero(sw.nstreams == N)[0]
+                if len(idx) == 0:
+                    continue
                 g = _group(sw.cols, idx)
                 km, n = g["km"], g["ncol"]
 
@@ -207,8 +193,8 @@ class Server:
                 nf = torch.empty(n * nch, dtype=torch.int32, device="cuda")
                 sts = torch.empty_like(nf)
                 rc = L.aerort_vlidort_scalar_lambert_ws_dev(
-                    slot["ws"][gi], self.prec, km, nch, n, N, 0, 2 * N, nl.data_ptr(), rot.data_ptr(),
-                    depol.data_ptr(), None, None, None, tau.data_ptr(), ssa.data_ptr(), pm.data_ptr(), he.data_ptr(), alb.data_ptr(),
+                    slot["ws"], self.prec, km, nch, n, N, 0, 2 * N, nl.data_ptr(), rot.data_ptr(), depol.data_ptr(),
+                    None, None, None, tau.data_ptr(), ssa.data_ptr(), pm.data_ptr(), he.data_ptr(), alb.data_ptr(),
                     sza.data_ptr(), raa.data_ptr(), vza.data_ptr(), MISSING, rad.data_ptr(), refl.data_ptr(),
                     nf.data_ptr(), sts.data_ptr(), st)
                 if rc != 0:
@@ -223,9 +209,8 @@ class Server:
                 hst.copy_(sts, non_blocking=True)
                 keep += [qm, rh, rot, depol, he, alb, sza, raa, vza, nl, tau, ssa, gg, pm, rad, refl, nf, sts]
                 outs.append((idx, hrad, hrefl, hnf, hst, n))
-            main.wait_stream(sub)
-        ev = torch.cuda.Event()
-        ev.record(main)
+            ev = torch.cuda.Event()
+            ev.record(slot["stream"])
         return ev, keep, outs
 
     def _finish(self, sw, outs):
