@@ -48,7 +48,7 @@ int stream_index(int nstreams);  // 0..4 for 4, 6, 8, 12, 16; -1 otherwise
 // from this many warps of 32 solves per SM on ([precision][stream index
 // 0..4 = 4, 6, 8, 12, 16]; 0 = never).  The FP64 re-solve of a mixed launch's
 // short refinement list always takes the team kernel.
-constexpr int kThreadMinWarpsPerSm[2][5] = {{2, 3, 3, 0, 0}, {4, 0, 4, 0, 0}};
+constexpr int kThreadMinWarpsPerSm[2][5] = {{2, 3, 3, 0, 0}, {2, 0, 4, 0, 0}};
 inline int resolve_kernel(int kernel, int precision, int si, long nsolve, int num_sms, bool list) {
   if (list) return 1;
   if (kernel == 0 || kernel == 1) return kernel;
