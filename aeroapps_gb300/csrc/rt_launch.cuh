@@ -64,7 +64,7 @@ constexpr int kGrabShare = 4;
 template <int NS, typename T, int WPB>
 // FP32: at most 170 registers, so that 6 two-warp blocks (12 warps) fit an SM
 // as the FP32 shared-memory working set allows.
-__global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? 6 : 1) k_scalar_lambert_team(RtOptions opt, LambertInputs in, Quad q,
+__global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 12 ? 8 : 6) : 1) k_scalar_lambert_team(RtOptions opt, LambertInputs in, Quad q,
                                                                    void* scratch, long nthreads, T* sweep,
                                                                    long sweep_per_warp, int nsolve, int chunk,
                                                                    int* counter, double* rad, double* refl, int* nf,
