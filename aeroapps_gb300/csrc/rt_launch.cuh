@@ -62,9 +62,11 @@ inline int team_chunk(int nsolve, long resident_blocks, int wpb, long* nblocks) 
 // one TeamMem per warp in dynamic shared memory.
 constexpr int kGrabShare = 4;
 template <int NS, typename T, int WPB>
-// FP32: at most 170 registers, so that 6 two-warp blocks (12 warps) fit an SM
-// as the FP32 shared-memory working set allows.
-__global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 12 ? 8 : 6) : 1) k_scalar_lambert_team(RtOptions opt, LambertInputs in, Quad q,
+// FP32: a register cap so that the resident warps are limited by the
+// shared-memory working set rather than by registers: 8 two-warp blocks (16
+// warps, <= 128 registers) up to 8 streams, 6 blocks (12 warps, <= 170
+// registers) above, where 128 registers would spill (measured on GB300).
+__global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 8 ? 8 : 6) : 1) k_scalar_lambert_team(RtOptions opt, LambertInputs in, Quad q,
                                                                    void* scratch, long nthreads, T* sweep,
                                                                    long sweep_per_warp, int nsolve, int chunk,
                                                                    int* counter, double* rad, double* refl, int* nf,
