@@ -113,22 +113,28 @@ RT_HD int team_argmax_lane(const Team& tm, T v, T* red, T* vmax) {
 #endif
 }
 
-// Shared-memory working set of one team.  Matrices are column-major with a
-// padded leading dimension (LD = N + 1, LK = 2N + 1) so that lanes working on
-// different columns hit different banks.
+// Shared-memory working set of one team.  The layer matrices are
+// column-major with a padded leading dimension (LD = N + 1) so that lanes
+// working on different columns hit different banks.  The interface systems
+// are row-major, [A | pad | B] per row with a row stride of LR words: a lane
+// owns a row in the elimination and moves it 16 bytes at a time; LR is an
+// odd number of 16-byte units, so 8 lanes' 16-byte accesses at the same
+// column fall in 8 different bank groups.
 template <int NS, typename T>
 struct TeamMem {
   static constexpr int LD = NS + 1;
-  static constexpr int LK = 2 * NS + 1;
-  // eigen phase: Sp, Bs, H, G, V (N x LD each); interface: K (2N x LK), R (LK x (N+1))
-  static constexpr int NWORK = (5 * NS * LD > LK * (3 * NS + 1)) ? 5 * NS * LD : LK * (3 * NS + 1);
+  static constexpr int V = 16 / (int)sizeof(T);                  // words per 16 bytes
+  static constexpr int LRQ = (3 * NS + 1 + V - 1) / V;           // 16-byte units for 2N + (N + 1) columns
+  static constexpr int LR = (LRQ % 2 == 1 ? LRQ : LRQ + 1) * V;  // row stride of the interface systems
+  // eigen phase: Sp, Bs, H, G, V (N x LD each); interface: 2N rows of LR
+  static constexpr int NWORK = (5 * NS * LD > 2 * NS * LR) ? 5 * NS * LD : 2 * NS * LR;
   T piq[NS][2 * NS + 1];             // P~_l^m at the quadrature cosines (row padded against bank conflicts)
   T piu[2 * NS], pi0[2 * NS];        // at the user and solar cosines
   T pimq[NS], pimu, pim0;            // P~_m^m carried across terms
   T lra[2 * NS], lrb[2 * NS], lr1;   // Legendre recurrence coefficients of term m
   T og[2 * NS];                      // omega * beta_l of the current layer
   T lsc[8];                          // dtau, 1 - omega, tuser, secbar, itrans, tmubar, emult, lnz
-  T work[NWORK];                     // eigen phase: Sp Bs H G V | interface: K R
+  alignas(16) T work[NWORK];         // eigen phase: Sp Bs H G V | interface system
   T kv[NS], norm[NS], uhd[NS], uhu[NS], hm1[NS], hm2[NS], gup[NS], gdn[NS], dpi[NS], dmi[NS], rv[NS];
   T rbeta;
   T P[2][NS * LD], Q[2][NS * LD];    // layer solutions (prev / cur)
@@ -181,45 +187,70 @@ RT_HD bool team_cholesky(const Team& tm, int n, T* A) {
   return true;
 }
 
-// In-place LU with partial pivoting of the n x n matrix A (n <= 32) and
-// solution of nrhs right-hand sides B (leading dimension LDA for both); pivots
-// and per-element arithmetic as lu_solve.  Lane r owns row r in the
-// elimination and the back substitution: its multiplier stays in a register,
-// the pivot row is a shared-memory broadcast, and the rows of a column are
-// consecutive words (no bank conflicts).
-template <int LDA, typename T>
-RT_HD bool team_lu_solve(const Team& tm, int n, T* A, T* B, int nrhs, T* red, int* ired) {
-  (void)ired;
-  const int r = tm.lane;
+// y[0..V) -= a x[0..V) for the 16 bytes at y and x (both 16-byte aligned).
+template <typename T>
+RT_HD void axpy16(T* y, const T* x, T a) {
+#ifdef __CUDA_ARCH__
+  if constexpr (sizeof(T) == sizeof(float)) {
+    const float4 xv = *reinterpret_cast<const float4*>(x);
+    float4 yv = *reinterpret_cast<float4*>(y);
+    yv.x -= a * xv.x; yv.y -= a * xv.y; yv.z -= a * xv.z; yv.w -= a * xv.w;
+    *reinterpret_cast<float4*>(y) = yv;
+  } else {
+    const double2 xv = *reinterpret_cast<const double2*>(x);
+    double2 yv = *reinterpret_cast<double2*>(y);
+    yv.x -= a * xv.x; yv.y -= a * xv.y;
+    *reinterpret_cast<double2*>(y) = yv;
+  }
+#else
+  for (int v = 0; v < 16 / (int)sizeof(T); ++v) y[v] -= a * x[v];
+#endif
+}
+
+// First column of the right-hand sides of an n-row interface system.
+RT_HD int rhs_col(int n) { return (n + 3) & ~3; }
+
+// Solution of A X = B by Gaussian elimination with partial pivoting, n <= 32
+// rows.  Row r of the system is S[r * LR ...]: A in columns 0..n-1, B in
+// columns rhs_col(n).. (nrhs of them); X overwrites B.  Pivots and the
+// arithmetic on every element of U and B as lu_solve.  Lane r owns row r: its
+// multiplier stays in a register and the pivot row is a broadcast.  A row is
+// updated 16 bytes at a time from the 16-byte boundary at or below the pivot
+// column; the entries this also touches (the eliminated column, the padding)
+// are not read again, since the solve needs no L.
+template <int LR, typename T>
+RT_HD bool team_lu_solve(const Team& tm, int n, T* S, int nrhs, T* red) {
+  constexpr int V = 16 / (int)sizeof(T);
+  const int r = tm.lane, nb = rhs_col(n), ncol = nb + nrhs;
+  T* row = S + LR * r;
   for (int k = 0; k < n; ++k) {
     T vmax;
-    const int piv = team_argmax_lane(tm, (r >= k && r < n) ? fabs(A[r + LDA * k]) : (T)-1, red, &vmax);
+    const int piv = team_argmax_lane(tm, (r >= k && r < n) ? fabs(row[k]) : (T)-1, red, &vmax);
     if (vmax == (T)0) return false;
     if (piv != k) {
-      for (int j = tm.lane; j < n + nrhs; j += kTeam) {
-        T* X = (j < n) ? A + LDA * j : B + LDA * (j - n);
-        const T tmp = X[k];
-        X[k] = X[piv];
-        X[piv] = tmp;
+      for (int j = tm.lane; j < ncol; j += kTeam) {
+        const T tmp = S[LR * k + j];
+        S[LR * k + j] = S[LR * piv + j];
+        S[LR * piv + j] = tmp;
       }
       tm.sync();
     }
     if (r > k && r < n) {
-      const T inv = (T)1 / A[k + LDA * k];
-      const T fm = A[r + LDA * k] * inv;
-      A[r + LDA * k] = fm;
-      for (int j = k + 1; j < n; ++j) A[r + LDA * j] -= fm * A[k + LDA * j];
-      for (int j = 0; j < nrhs; ++j) B[r + LDA * j] -= fm * B[k + LDA * j];
+      const T* rk = S + LR * k;
+      const T inv = (T)1 / rk[k];
+      const T fm = row[k] * inv;
+      for (int j = (k + 1) & ~(V - 1); j < ncol; j += V) axpy16(row + j, rk + j, fm);
     }
     tm.sync();
   }
   for (int i = n - 1; i >= 0; --i) {
-    const T inv = (T)1 / A[i + LDA * i];
-    for (int j = tm.lane; j < nrhs; j += kTeam) B[i + LDA * j] *= inv;
+    T* ri = S + LR * i;
+    const T inv = (T)1 / ri[i];
+    for (int j = tm.lane; j < nrhs; j += kTeam) ri[nb + j] *= inv;
     tm.sync();
     if (r < i) {
-      const T a = A[r + LDA * i];
-      for (int j = 0; j < nrhs; ++j) B[r + LDA * j] -= a * B[i + LDA * j];
+      const T a = row[i];
+      for (int j = nb; j < ncol; j += V) axpy16(row + j, ri + j, a);
     }
     tm.sync();
   }
@@ -639,7 +670,7 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
                             const ScratchT<T>& W, const ScratchLayout<NS>& lay, T* sw, const SweepLayout<NS>& swl,
                             T* out) {
   constexpr int LD = TeamMem<NS, T>::LD;
-  constexpr int LK = TeamMem<NS, T>::LK;
+  constexpr int LR = TeamMem<NS, T>::LR;
   const int N = NS, NM = c.NM, L = c.L;
   const bool incl_surface = (m == 0) && (c.albedo != (T)0);
   const T surface_factor = (m == 0) ? (T)2 : (T)1;
@@ -652,8 +683,7 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
     direct_beam = x0 * c.trans_solar_beam * c.albedo;
   }
   team_legendre<NS, T>(tm, M, c, m);
-  T* K = M.work;
-  T* R = M.work + 2 * NS * LK;
+  T* K = M.work;  // interface systems, row-major (team_lu_solve)
   int cur = 1, prev = 0;
   if (tm.lane == 0) M.vp_valid = 0;
   tm.sync();
@@ -669,22 +699,24 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
     int st = team_layer_solution<NS, T>(tm, M, c, opt, m, n, lsc, cur, sw, swl);
     if (st != RT_OK) return st;
     if (n == 0) {
+      const int nb = rhs_col(N);
       for (int e = tm.lane; e < N * N; e += kTeam) {
-        const int i = e % N, j = e / N;
-        K[i + LK * j] = M.P[cur][i + LD * j];
-        R[i + LK * j] = -M.Q[cur][i + LD * j] * M.t[cur][j];
+        const int j = e % N, i = e / N;
+        K[LR * i + j] = M.P[cur][i + LD * j];
+        K[LR * i + nb + j] = -M.Q[cur][i + LD * j] * M.t[cur][j];
       }
-      for (int i = tm.lane; i < N; i += kTeam) R[i + LK * N] = -M.wt[cur][i];
+      for (int i = tm.lane; i < N; i += kTeam) K[LR * i + nb + N] = -M.wt[cur][i];
       tm.sync();
-      if (!team_lu_solve<LK>(tm, N, K, R, N + 1, M.red, M.ired)) return RT_BVP_SINGULAR;
+      if (!team_lu_solve<LR>(tm, N, K, N + 1, M.red)) return RT_BVP_SINGULAR;
       for (int e = tm.lane; e < N * N; e += kTeam) {
         const int i = e % N, j = e / N;
-        M.F[i + LD * j] = R[i + LK * j];
-        sw[swl.F + i + NS * j + (long)NS * NS * n] = R[i + LK * j];
+        M.F[i + LD * j] = K[LR * i + nb + j];
+        sw[swl.F + i + NS * j + (long)NS * NS * n] = K[LR * i + nb + j];
       }
-      for (int i = tm.lane; i < N; i += kTeam) { M.f[i] = R[i + LK * N]; sw[swl.f + i + NS * (long)n] = M.f[i]; }
+      for (int i = tm.lane; i < N; i += kTeam) { M.f[i] = K[LR * i + nb + N]; sw[swl.f + i + NS * (long)n] = M.f[i]; }
       tm.sync();
     } else {
+      const int nb = rhs_col(2 * N);
       {
         // U elements per lane, their 2U sums in registers (independent chains)
         constexpr int NE = NS * NS, U = (NE + kTeam - 1) / kTeam;
@@ -693,8 +725,9 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
         for (int u = 0; u < U; ++u) {
           const int e = tm.lane + kTeam * u;
           if (e < NE) {
-            gt[u] = M.Q[prev][e % N + LD * (e / N)];
-            gb[u] = M.P[prev][e % N + LD * (e / N)];
+            const int j = e % N, i = e / N;
+            gt[u] = M.Q[prev][i + LD * j];
+            gb[u] = M.P[prev][i + LD * j];
           }
         }
         for (int k = 0; k < N; ++k) {
@@ -703,7 +736,7 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
           for (int u = 0; u < U; ++u) {
             const int e = tm.lane + kTeam * u;
             if (e < NE) {
-              const int i = e % N, j = e / N;
+              const int j = e % N, i = e / N;
               const T tf = tk * M.F[k + LD * j];
               gt[u] += M.P[prev][i + LD * k] * tf;
               gb[u] += M.Q[prev][i + LD * k] * tf;
@@ -714,13 +747,13 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
         for (int u = 0; u < U; ++u) {
           const int e = tm.lane + kTeam * u;
           if (e < NE) {
-            const int i = e % N, j = e / N;
-            K[i + LK * j] = gt[u];
-            K[N + i + LK * j] = gb[u];
-            K[i + LK * (N + j)] = -M.P[cur][i + LD * j];
-            K[N + i + LK * (N + j)] = -M.Q[cur][i + LD * j];
-            R[i + LK * j] = M.Q[cur][i + LD * j] * M.t[cur][j];
-            R[N + i + LK * j] = M.P[cur][i + LD * j] * M.t[cur][j];
+            const int j = e % N, i = e / N;
+            K[LR * i + j] = gt[u];
+            K[LR * (N + i) + j] = gb[u];
+            K[LR * i + N + j] = -M.P[cur][i + LD * j];
+            K[LR * (N + i) + N + j] = -M.Q[cur][i + LD * j];
+            K[LR * i + nb + j] = M.Q[cur][i + LD * j] * M.t[cur][j];
+            K[LR * (N + i) + nb + j] = M.P[cur][i + LD * j] * M.t[cur][j];
           }
         }
       }
@@ -731,22 +764,22 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
           gt += M.P[prev][i + LD * k] * tf;
           gb += M.Q[prev][i + LD * k] * tf;
         }
-        R[i + LK * N] = M.wt[cur][i] - M.wb[prev][i] - gt;
-        R[N + i + LK * N] = M.wt[cur][N + i] - M.wb[prev][N + i] - gb;
+        K[LR * i + nb + N] = M.wt[cur][i] - M.wb[prev][i] - gt;
+        K[LR * (N + i) + nb + N] = M.wt[cur][N + i] - M.wb[prev][N + i] - gb;
       }
       tm.sync();
-      if (!team_lu_solve<LK>(tm, 2 * N, K, R, N + 1, M.red, M.ired)) return RT_BVP_SINGULAR;
+      if (!team_lu_solve<LR>(tm, 2 * N, K, N + 1, M.red)) return RT_BVP_SINGULAR;
       const long oC = swl.C + (long)NS * NS * (n - 1), oc = swl.c + (long)NS * (n - 1);
       const long oF = swl.F + (long)NS * NS * n, of = swl.f + (long)NS * n;
       for (int e = tm.lane; e < N * N; e += kTeam) {
         const int i = e % N, j = e / N;
-        sw[oC + i + NS * j] = R[i + LK * j];
-        M.F[i + LD * j] = R[N + i + LK * j];
-        sw[oF + i + NS * j] = R[N + i + LK * j];
+        sw[oC + i + NS * j] = K[LR * i + nb + j];
+        M.F[i + LD * j] = K[LR * (N + i) + nb + j];
+        sw[oF + i + NS * j] = K[LR * (N + i) + nb + j];
       }
       for (int i = tm.lane; i < N; i += kTeam) {
-        sw[oc + i] = R[i + LK * N];
-        M.f[i] = R[N + i + LK * N];
+        sw[oc + i] = K[LR * i + nb + N];
+        M.f[i] = K[LR * (N + i) + nb + N];
         sw[of + i] = M.f[i];
       }
       tm.sync();
@@ -771,25 +804,26 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
   for (int j = 0; j < N; ++j) r2b += M.cqx[j] * M.cqw[j] * M.wb[bl][j];
   r2b *= kmult;
   tm.sync();
+  const int nbc = rhs_col(N);
   for (int e = tm.lane; e < N * N; e += kTeam) {
-    const int i = e % N, j = e / N;
+    const int j = e % N, i = e / N;
     T s = M.P[bl][i + LD * j] - M.dmi[j];
     for (int k = 0; k < N; ++k) s += (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.F[k + LD * j];
-    K[i + LK * j] = s;
+    K[LR * i + j] = s;
   }
   if (tm.lane < N) {
     const int i = tm.lane;
     T s = -M.wb[bl][N + i] + r2b + (localbeam ? direct_beam : (T)0);
     for (int k = 0; k < N; ++k) s -= (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.f[k];
-    R[i] = s;
+    K[LR * i + nbc] = s;
   }
   tm.sync();
-  if (!team_lu_solve<LK>(tm, N, K, R, 1, M.red, M.ired)) return RT_BVP_SINGULAR;
-  // Mc in R[0..N), Lc in M.gup, Mn in M.gdn
+  if (!team_lu_solve<LR>(tm, N, K, 1, M.red)) return RT_BVP_SINGULAR;
+  // Mc in the solved right-hand side, Lc in M.gup, Mn in M.gdn
   T* Mc = M.hm1;
   T* Lc = M.gup;
   T* Mn = M.gdn;
-  if (tm.lane < N) Mc[tm.lane] = R[tm.lane];
+  if (tm.lane < N) Mc[tm.lane] = K[LR * tm.lane + nbc];
   tm.sync();
   if (tm.lane < N) {
     const int i = tm.lane;
