@@ -56,6 +56,13 @@ RT_HD T group_sum(const Team& tm, T v, T* red) {
 #endif
 }
 
+// Whether the team splits its per-row and per-eigenvector sums (particular
+// solution, user-angle solutions) across both half-warps, two lanes per row.
+// Measured on GB300: faster in FP64 (4%) and for the 16-stream FP32 kernel
+// (6%), slower for the 12-stream FP32 kernel (17%).
+template <int NS, typename T>
+constexpr bool kTeamSplitSums = sizeof(T) == sizeof(double) || NS >= 16;
+
 // v of this lane plus v of lane + h (lanes < h get the sum of the pair; the
 // others keep their own v).  Every lane must call it.
 template <typename T>
@@ -562,14 +569,28 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
       M.norm[a] = nr;
       const T help = k * dtau;
       M.t[cur][a] = help > (T)kMaxTau ? (T)0 : exp(-help);
-      for (int i = 0; i < N; ++i) Sp[i + LD * a] = x[i];  // Sp is free: x for the user solutions
+      if constexpr (!kTeamSplitSums<NS, T>) {
+        T dn = 0, up = 0;
+        for (int l = m; l <= NM; ++l) {
+          const bool even = ((l - m) & 1) == 0;
+          T sps = 0;
+          for (int j = 0; j < N; ++j) sps += M.cqw[j] * M.piq[j][l] * (even ? x[j] : g[j]);
+          const T h = (T)0.5 * M.og[l] * sps;
+          dn += (even ? M.piu[l] : -M.piu[l]) * h;
+          up += M.piu[l] * h;
+        }
+        M.uhd[a] = dn;
+        M.uhu[a] = up;
+      } else {
+        for (int i = 0; i < N; ++i) Sp[i + LD * a] = x[i];  // Sp is free: x for the user solutions
+      }
     }
   }
   if (team_any(tm, fail != 0, &M.flag)) return RT_EIGEN_FAIL;
-  tm.sync();
-  // user-angle solutions: lanes a and a + N share eigenvector a, each summing
-  // half of the moments (x in Sp, dif in G)
-  {
+  if constexpr (kTeamSplitSums<NS, T>) {
+    tm.sync();
+    // user-angle solutions: lanes a and a + N share eigenvector a, each summing
+    // half of the moments (x in Sp, dif in G)
     const int ea = tm.lane % N, half = tm.lane / N;
     const int nl = NM - m + 1, l0 = m + (half == 0 ? 0 : (nl + 1) / 2), l1 = (half == 0) ? m + (nl + 1) / 2 : NM + 1;
     T dn = 0, up = 0;
@@ -629,25 +650,41 @@ RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<
   if (active) {
     const T F1 = (T)(opt.flux_factor / kPI4);
     const T secbar = M.lsc[3], cnst = M.lsc[4], wdel = M.lsc[5], emult = M.lsc[6];
-    // dpi/dmi: lanes i and i + N over quadrature row i, each half of the moments
     const int hq = tm.lane % N, half = tm.lane / N;
-    {
-      const int nl = NM - m + 1, l0 = m + (half == 0 ? 0 : (nl + 1) / 2), l1 = (half == 0) ? m + (nl + 1) / 2 : NM + 1;
-      T sp = 0, sm = 0;
-      if (half < 2)
-        for (int l = l0; l < l1; ++l) {
-          const T t = M.piq[hq][l] * (M.og[l] * M.pi0[l]);
+    if constexpr (!kTeamSplitSums<NS, T>) {
+      // dpi/dmi: lanes over quadrature rows
+      if (tm.lane < N) {
+        const int i = tm.lane;
+        T sp = 0, sm = 0;
+        for (int l = m; l <= NM; ++l) {
+          const T t = M.piq[i][l] * (M.og[l] * M.pi0[l]);
           sp += t;
           sm += (((l - m) & 1) ? -t : t);
         }
-      sp = pair_sum(tm, sp, N, M.red);
-      sm = pair_sum(tm, sm, N, M.red);
-      if (tm.lane < N) {
-        M.dpi[hq] = F1 * sp;
-        M.dmi[hq] = F1 * sm;
+        M.dpi[i] = F1 * sp;
+        M.dmi[i] = F1 * sm;
       }
+      tm.sync();
+    } else {
+      // dpi/dmi: lanes i and i + N over quadrature row i, each half of the moments
+      {
+        const int nl = NM - m + 1, l0 = m + (half == 0 ? 0 : (nl + 1) / 2), l1 = (half == 0) ? m + (nl + 1) / 2 : NM + 1;
+        T sp = 0, sm = 0;
+        if (half < 2)
+          for (int l = l0; l < l1; ++l) {
+            const T t = M.piq[hq][l] * (M.og[l] * M.pi0[l]);
+            sp += t;
+            sm += (((l - m) & 1) ? -t : t);
+          }
+        sp = pair_sum(tm, sp, N, M.red);
+        sm = pair_sum(tm, sm, N, M.red);
+        if (tm.lane < N) {
+          M.dpi[hq] = F1 * sp;
+          M.dmi[hq] = F1 * sm;
+        }
+      }
+      tm.sync();
     }
-    tm.sync();
     T part = 0;
     if (a < N) {
       const T zdel = M.t[cur][a], kk = M.kv[a];
@@ -666,37 +703,62 @@ RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<
         else sd = (cnst * M.hm2[a] - emult) / gm;
         su = (itw * M.hm1[a] + emult) / gp;
       }
-      M.hm2[a] = cf;  // multipliers of eigenvector a, until at and bt are known
-      M.gdn[a] = df;
-      M.gup[a] = sd;
-      M.red[a] = su;
-    }
-    tm.sync();
-    // projections at, bt of the beam source on eigenvector hq: lanes hq and
-    // hq + N, each half of the quadrature rows
-    {
-      const int i0 = half == 0 ? 0 : N / 2, i1 = half == 0 ? N / 2 : N;
-      T s1 = 0, s2 = 0;
-      if (half < 2)
-        for (int i = i0; i < i1; ++i) {
-          s1 += M.cqw[i] * (M.dpi[i] * M.P[cur][i + LD * hq] + M.dmi[i] * M.Q[cur][i + LD * hq]);
-          s2 += M.cqw[i] * (M.dmi[i] * M.P[cur][i + LD * hq] + M.dpi[i] * M.Q[cur][i + LD * hq]);
+      if constexpr (!kTeamSplitSums<NS, T>) {
+        T s1 = 0, s2 = 0;
+        for (int i = 0; i < N; ++i) {
+          s1 += M.cqw[i] * (M.dpi[i] * M.P[cur][i + LD * a] + M.dmi[i] * M.Q[cur][i + LD * a]);
+          s2 += M.cqw[i] * (M.dmi[i] * M.P[cur][i + LD * a] + M.dpi[i] * M.Q[cur][i + LD * a]);
         }
-      s1 = pair_sum(tm, s1, N, M.red + kTeam);
-      s2 = pair_sum(tm, s2, N, M.red + kTeam);
-      if (a < N) {
-        const T cf = M.hm2[a], df = M.gdn[a], sd = M.gup[a], su = M.red[a];
         const T at = s1 / M.norm[a], bt = s2 / M.norm[a];
-        part = M.uhd[a] * sd * at + M.uhu[a] * su * bt;
         M.gdn[a] = cf * at;
         M.gup[a] = df * bt;
+        part = M.uhd[a] * sd * at + M.uhu[a] * su * bt;
+      } else {
+        M.hm2[a] = cf;  // multipliers of eigenvector a, until at and bt are known
+        M.gdn[a] = df;
+        M.gup[a] = sd;
+        M.red[a] = su;
+      }
+    }
+    if constexpr (kTeamSplitSums<NS, T>) {
+      tm.sync();
+      // projections at, bt of the beam source on eigenvector hq: lanes hq and
+      // hq + N, each half of the quadrature rows
+      {
+        const int i0 = half == 0 ? 0 : N / 2, i1 = half == 0 ? N / 2 : N;
+        T s1 = 0, s2 = 0;
+        if (half < 2)
+          for (int i = i0; i < i1; ++i) {
+            s1 += M.cqw[i] * (M.dpi[i] * M.P[cur][i + LD * hq] + M.dmi[i] * M.Q[cur][i + LD * hq]);
+            s2 += M.cqw[i] * (M.dmi[i] * M.P[cur][i + LD * hq] + M.dpi[i] * M.Q[cur][i + LD * hq]);
+          }
+        s1 = pair_sum(tm, s1, N, M.red + kTeam);
+        s2 = pair_sum(tm, s2, N, M.red + kTeam);
+        if (a < N) {
+          const T cf = M.hm2[a], df = M.gdn[a], sd = M.gup[a], su = M.red[a];
+          const T at = s1 / M.norm[a], bt = s2 / M.norm[a];
+          part = M.uhd[a] * sd * at + M.uhu[a] * su * bt;
+          M.gdn[a] = cf * at;
+          M.gup[a] = df * bt;
+        }
       }
     }
     tm.sync();
     M.red[tm.lane] = part;
     tm.sync();
     for (int k = 0; k < N; ++k) spart += M.red[k];
-    {
+    if constexpr (!kTeamSplitSums<NS, T>) {
+      if (tm.lane < N) {
+        const int i = tm.lane;
+        T wu1 = 0, wu2 = 0, wl1 = 0, wl2 = 0;
+        for (int k = 0; k < N; ++k) {
+          wu1 += M.gup[k] * M.Q[cur][i + LD * k]; wu2 += M.gup[k] * M.P[cur][i + LD * k];
+          wl1 += M.gdn[k] * M.P[cur][i + LD * k]; wl2 += M.gdn[k] * M.Q[cur][i + LD * k];
+        }
+        M.wt[cur][i] = wu1; M.wt[cur][N + i] = wu2;
+        M.wb[cur][i] = wl1; M.wb[cur][N + i] = wl2;
+      }
+    } else {
       // particular solution at the layer boundaries, row hq: lanes hq and hq + N, half of the eigenvectors each
       const int k0 = half == 0 ? 0 : N / 2, k1 = half == 0 ? N / 2 : N;
       T wu1 = 0, wu2 = 0, wl1 = 0, wl2 = 0;
