@@ -62,6 +62,7 @@ _SIGNATURES = {
     "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_probe_ffma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_last_error": (ctypes.c_char_p, []),
+    "aerort_launch_count": (ctypes.c_ulonglong, []),
     "aerort_version": (c_int, []),
     "aerort_release": (c_int, []),
     "aerort_miegen_lognormal": (c_int, [c_int, P_d, c_int, P_d, c_int, P_d, P_d, c_double, c_double, c_int, c_double,

@@ -8,6 +8,7 @@
 //                     warp-granular dynamic scheduling over a persistent grid
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -111,6 +112,9 @@ Context& ctx() {
   static Context c;
   return c;
 }
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
 int stream_index(int nstreams) {
   switch (nstreams) {
@@ -376,6 +380,7 @@ int aop_launch(aerort_mie* mie, int km, int nobs, int nch, int nq, const std::ve
   long nb = (total + bs - 1) / bs;
   k_aop<<<(unsigned)nb, bs, 0, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, tau, ssa, g, pmom);
   CUDA_TRY(cudaGetLastError());
+  count_launches(1);
   return 0;
 }
 }  // namespace
@@ -992,3 +997,7 @@ extern "C" int aerort_probe_dfma(int blocks, int threads, int iters, double* out
   return AERORT_OK;
 }
 
+
+extern "C" unsigned long long aerort_launch_count(void) {
+  return aerort_internal::g_launches.load(std::memory_order_relaxed);
+}

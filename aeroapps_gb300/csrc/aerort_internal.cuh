@@ -14,6 +14,9 @@ namespace aerort_internal {
 
 int set_error(int rc, const std::string& msg);
 
+// Kernel launches made by the library since it was loaded (aerort_launch_count).
+void count_launches(int n);
+
 #define CUDA_TRY(expr)                                                                                   \
   do {                                                                                                   \
     cudaError_t e_ = (expr);                                                                             \

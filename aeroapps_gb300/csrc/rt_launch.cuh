@@ -118,6 +118,55 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 
   }
 }
 
+// Two-pass team solve (library scratch, whole batches): k_team_setup runs the
+// set-up of every solve of a slice, one thread per solve and all lanes busy;
+// k_team_series then runs the Fourier series, each warp taking one solve at a
+// time in index order.  Against the fused kernel this removes the set-up from
+// the team kernel (one or two busy lanes per grab there) and its code from
+// the team kernel's instruction footprint.  Per-solve scratch (set-up record
+// and layer arrays, element-major / solve-minor) for at most kSetupSlice
+// solves at once.
+constexpr int kSetupSlice = 1 << 17;
+
+template <int NS, typename T>
+__global__ void __launch_bounds__(32) k_team_setup(RtOptions opt, LambertInputs in, Quad q, void* scratch, int base,
+                                                   int count, double* rad, double* refl, int* nf, int* st,
+                                                   unsigned char* live) {
+  const ScratchLayout<NS> lay(in.km, false);
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < count; s += gridDim.x * blockDim.x) {
+    const SolveScratch<T> S = make_scratch<NS, T>(scratch, s, count, in.km, false);
+    SetupRecord r;
+    const bool ok = solve_setup<NS, T>(opt, in, base + s, q.tu, q.wu, S, rad, refl, nf, st, r);
+    if (ok) r.store(S.D, lay.rec);
+    live[s] = ok ? 1 : 0;
+  }
+}
+
+template <int NS, typename T, int WPB>
+__global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 8 ? 8 : 6) : 1)
+    k_team_series(RtOptions opt, LambertInputs in, Quad q, void* scratch, int base, int count, T* sweep,
+                  long sweep_per_warp, int* counter, const unsigned char* live, double* rad, double* refl, int* nf,
+                  int* st, Worklist wl) {
+  extern __shared__ __align__(16) unsigned char team_smem[];
+  const int lane = threadIdx.x & 31;
+  TeamMem<NS, T>& M = reinterpret_cast<TeamMem<NS, T>*>(team_smem)[threadIdx.x >> 5];
+  const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  T* sw = sweep + warp * sweep_per_warp;
+  const ScratchLayout<NS> lay(in.km, false);
+  const Team tm{lane, nullptr, nullptr};
+  for (;;) {
+    int s = 0;
+    if (lane == 0) s = atomicAdd(counter, 1);
+    s = __shfl_sync(0xffffffffu, s, 0);
+    if (s >= count) break;
+    if (!live[s]) continue;
+    const SolveScratch<T> S = make_scratch<NS, T>(scratch, s, count, in.km, false);
+    SetupRecord r;
+    r.load(S.D, lay.rec);
+    team_fourier_series<NS, T>(tm, M, opt, in, r, q.qx, q.qw, S.W, lay, sw, rad, refl, nf, st, wl, base + s);
+  }
+}
+
 template <int NS, typename T>
 int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
                                int* nf, int* st, cudaStream_t s, const Worklist& wl) {
@@ -130,6 +179,47 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
   const int bs = 32 * WPB;
   const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
+  if (!wl.in_list) {
+    CUDA_TRY(cudaFuncSetAttribute(k_team_series<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_team_series<NS, T, WPB>, bs, smem));
+    if (per_sm < 1) return set_error(AERORT_RC_CUDA, "team kernel does not fit on an SM");
+    const Schedule& sc = c.sched[sizeof(T) == sizeof(float) ? 1 : 0][stream_index(NS)];
+    if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
+    const int slice = nsolve < kSetupSlice ? nsolve : kSetupSlice;
+    long nblocks = (long)per_sm * c.num_sms;
+    if (nblocks > (slice + WPB - 1) / WPB) nblocks = (slice + WPB - 1) / WPB;
+    const ScratchLayout<NS> lay(in.km, false);
+    const SweepLayout<NS> swl(in.km);
+    auto up256 = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t live_off = up256((size_t)lay.template bytes<T>() * slice);
+    const size_t sweep_off = live_off + up256((size_t)slice);
+    const size_t sweep_bytes = sizeof(T) * (size_t)swl.total * (size_t)(nblocks * WPB);
+    if (int rc = c.pad->scratch.ensure(sweep_off + sweep_bytes)) return rc;
+    if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
+    char* base_p = (char*)c.pad->scratch.p;
+    int* counter = (int*)c.pad->counter.p;
+    int* first = counter + 1;
+    k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
+    k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo,
+                                                         in.missing, first);
+    CUDA_TRY(cudaGetLastError());
+    count_launches(2);
+    LambertInputs in2 = in;
+    in2.nadir_first = first;
+    for (int b0 = 0; b0 < nsolve; b0 += slice) {
+      const int cnt = nsolve - b0 < slice ? nsolve - b0 : slice;
+      if (b0 > 0) CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+      k_team_setup<NS, T><<<(unsigned)((cnt + 31) / 32), 32, 0, s>>>(opt, in2, q, base_p, b0, cnt, rad, refl, nf, st,
+                                                                     (unsigned char*)(base_p + live_off));
+      k_team_series<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(
+          opt, in2, q, base_p, b0, cnt, (T*)(base_p + sweep_off), swl.total, counter,
+          (const unsigned char*)(base_p + live_off), rad, refl, nf, st, wl);
+      CUDA_TRY(cudaGetLastError());
+      count_launches(2);
+    }
+    return 0;
+  }
   CUDA_TRY(cudaFuncSetAttribute(k_scalar_lambert_team<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
   int per_sm = 0;
@@ -164,6 +254,7 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
                                                                         sweep, swl.total, nsolve, chunk, counter, rad,
                                                                         refl, nf, st, wl);
   CUDA_TRY(cudaGetLastError());
+  count_launches(3);
   return 0;
 }
 
@@ -200,6 +291,7 @@ int launch_scalar_lambert(Context& c, const RtOptions& opt, const LambertInputs&
   k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, c.pad->scratch.p, nthreads, nsolve, counter,
                                                            rad, refl, nf, st, wl);
   CUDA_TRY(cudaGetLastError());
+  count_launches(3);
   return 0;
 }
 
@@ -253,6 +345,7 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
         opt, in2, q, arena, nthreads, (T*)((char*)arena + sweep_off), swl.total, nsolve, chunk, counter, rad, refl,
         nf, st, wl);
     CUDA_TRY(cudaGetLastError());
+    count_launches(3);
     return 0;
   }
   const int bs = sc.threads;
@@ -283,6 +376,7 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
   k_scalar_lambert<NS, T><<<(unsigned)nblocks, bs, 0, s>>>(opt, in2, q, arena, nthreads, nsolve, counter, rad, refl,
                                                            nf, st, wl);
   CUDA_TRY(cudaGetLastError());
+  count_launches(3);
   return 0;
 }
 

@@ -174,6 +174,7 @@ int launch_rot(int km, int nch, int nobs, const double* channels, const double* 
   if (blocks > cap) blocks = cap;
   k_rot_calc<<<(unsigned)blocks, kThreads, smem, s>>>(km, nch, nobs, channels, pe, he, te, rot, depol);
   CUDA_TRY(cudaGetLastError());
+  count_launches(1);
   return 0;
 }
 

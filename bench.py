@@ -409,6 +409,7 @@ def main():
     t0, t1 = ev(), ev()
     rt_m = []
     torch.cuda.synchronize()
+    lc0 = L.aerort_launch_count()
     t0.record()
     for _ in range(args.steps):
         if graph is not None:
@@ -418,9 +419,12 @@ def main():
     t1.record()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    if graph is not None:  # per-kernel times from one eager step
+    launches = L.aerort_launch_count() - lc0  # the library's kernel launches in the timed region
+    if graph is not None:  # per-kernel times from one eager step; a replay launches that step's kernels
+        lc0 = L.aerort_launch_count()
         step(_lib.PREC_MIXED, rt_m)
         torch.cuda.synchronize()
+        launches = (L.aerort_launch_count() - lc0) * args.steps
     ms = t0.elapsed_time(t1) / args.steps
     if world > 1:
         tt = torch.tensor([ms], device="cuda")
@@ -595,9 +599,6 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(batch, min(args.cpu_cols or 4096, my_cols))  # about 10 s on a 16-core host
-    # inside the timed mixed steps, per stream group: the AOP kernel, then for the FP32 pass and for the FP64
-    # re-solve of its list each a scheduler init, the nadir flag and the RT kernel
-    launches = 7 * len(groups) * args.steps
     line = {
         "metric": METRIC, "value": value, "unit": "radiances/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

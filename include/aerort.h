@@ -284,6 +284,9 @@ int aerort_probe_dfma(int blocks, int threads, int iters, double* out_dev, void*
 /* Same with FP32 FMA chains (the FP32 pipe rate that bounds the mixed solve). */
 int aerort_probe_ffma(int blocks, int threads, int iters, float* out_dev, void* stream);
 
+/* Number of kernels the library has launched since it was loaded (all entry
+ * points, all streams); a diagnostic for launch accounting. */
+unsigned long long aerort_launch_count(void);
 const char* aerort_last_error(void);  /* last error message of the calling thread */
 int aerort_version(void);             /* 100 * major + minor */
 /* Release the library's cached device buffers and streams (optional). */

@@ -1,9 +1,9 @@
 """Batched entry points on several CUDA streams at once (the library keeps one
 scratch pad per caller stream, up to 8, and hands a pad to a new stream only
 after the device has finished with it), the automatic kernel choice on a large
-batch, and empty batches.  Bar: results bitwise identical to the same solves
-run alone on one stream; the automatic choice within 1e-12 (FP64) of the other
-kernel."""
+batch, a team-kernel batch larger than one set-up slice, and empty batches.
+Bar: results bitwise identical to the same solves run alone on one stream;
+the two kernels within 1e-12 (FP64) of each other."""
 import numpy as np
 import pytest
 
@@ -123,3 +123,29 @@ def test_empty_batch(precision):
     c["ncol"] = 0
     assert _launch(L, c, t, out, 8, torch.cuda.current_stream().cuda_stream, precision) == 0
     torch.cuda.synchronize()
+
+
+@pytest.mark.gpu
+def test_team_kernel_batch_larger_than_one_setup_slice():
+    # more solves than the two-pass team path sets up at once (2^17): the second
+    # slice must give the same results as the thread kernel does for it
+    import torch
+    L = _lib.lib()
+    N = 4
+    ncol = (1 << 17) // CH + 4000
+    c, t, out = _device_case(torch, N, ncol, seed=21, km=20)
+    s0 = torch.cuda.current_stream().cuda_stream
+    res = {}
+    for kern in (_lib.KERNEL_TEAM, _lib.KERNEL_THREAD):
+        assert L.aerort_set_kernel(N, _lib.PREC_FP64, kern) == 0
+        try:
+            assert _launch(L, c, t, out, N, s0, _lib.PREC_FP64) == 0, _lib.last_error()
+            torch.cuda.synchronize()
+        finally:
+            L.aerort_set_kernel(N, _lib.PREC_FP64, _lib.KERNEL_AUTO)
+        res[kern] = {k: v.cpu().numpy().copy() for k, v in out.items()}
+    a, b = res[_lib.KERNEL_TEAM], res[_lib.KERNEL_THREAD]
+    assert np.array_equal(a["st"], b["st"]) and np.array_equal(a["nf"], b["nf"])
+    ok = b["rad"] != MISSING
+    assert ok.sum() > (1 << 17)
+    assert np.max(np.abs(a["rad"][ok] / b["rad"][ok] - 1.0)) <= 1e-12
