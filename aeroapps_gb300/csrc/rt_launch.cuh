@@ -167,6 +167,49 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 
   }
 }
 
+// Enqueue the two-pass team solve on storage at `base`: per-solve scratch for
+// `slice` solves, their live flags at live_off, the per-warp sweep regions at
+// sweep_off (nblocks x 2 warps); counter and first are two scheduling ints.
+template <int NS, typename T>
+int enqueue_team_two_pass(const RtOptions& opt, const LambertInputs& in, const Quad& q, char* base, size_t live_off,
+                          size_t sweep_off, long nblocks, int slice, int* counter, int* first, double* rad,
+                          double* refl, int* nf, int* st, cudaStream_t s, const Worklist& wl) {
+  constexpr int WPB = 2;
+  const int nsolve = in.nobs * in.nch;
+  const SweepLayout<NS> swl(in.km);
+  const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
+  k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
+                                                       first);
+  CUDA_TRY(cudaGetLastError());
+  count_launches(2);
+  LambertInputs in2 = in;
+  in2.nadir_first = first;
+  for (int b0 = 0; b0 < nsolve; b0 += slice) {
+    const int cnt = nsolve - b0 < slice ? nsolve - b0 : slice;
+    if (b0 > 0) CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+    k_team_setup<NS, T><<<(unsigned)((cnt + 31) / 32), 32, 0, s>>>(opt, in2, q, base, b0, cnt, rad, refl, nf, st,
+                                                                   (unsigned char*)(base + live_off));
+    k_team_series<NS, T, WPB><<<(unsigned)nblocks, 32 * WPB, smem, s>>>(
+        opt, in2, q, base, b0, cnt, (T*)(base + sweep_off), swl.total, counter,
+        (const unsigned char*)(base + live_off), rad, refl, nf, st, wl);
+    CUDA_TRY(cudaGetLastError());
+    count_launches(2);
+  }
+  return 0;
+}
+
+// Resident two-warp blocks of the series kernel per SM (sets its shared-memory attribute).
+template <int NS, typename T>
+int team_series_blocks_per_sm(int* per_sm) {
+  constexpr int WPB = 2;
+  const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
+  CUDA_TRY(cudaFuncSetAttribute(k_team_series<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_team_series<NS, T, WPB>, 32 * WPB, smem));
+  if (*per_sm < 1) return set_error(AERORT_RC_CUDA, "team kernel does not fit on an SM");
+  return 0;
+}
+
 template <int NS, typename T>
 int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
                                int* nf, int* st, cudaStream_t s, const Worklist& wl) {
@@ -180,10 +223,8 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   const int bs = 32 * WPB;
   const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
   if (!wl.in_list) {
-    CUDA_TRY(cudaFuncSetAttribute(k_team_series<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_team_series<NS, T, WPB>, bs, smem));
-    if (per_sm < 1) return set_error(AERORT_RC_CUDA, "team kernel does not fit on an SM");
+    if (int rc = team_series_blocks_per_sm<NS, T>(&per_sm)) return rc;
     const Schedule& sc = c.sched[sizeof(T) == sizeof(float) ? 1 : 0][stream_index(NS)];
     if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
     const int slice = nsolve < kSetupSlice ? nsolve : kSetupSlice;
@@ -197,28 +238,9 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
     const size_t sweep_bytes = sizeof(T) * (size_t)swl.total * (size_t)(nblocks * WPB);
     if (int rc = c.pad->scratch.ensure(sweep_off + sweep_bytes)) return rc;
     if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
-    char* base_p = (char*)c.pad->scratch.p;
     int* counter = (int*)c.pad->counter.p;
-    int* first = counter + 1;
-    k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
-    k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo,
-                                                         in.missing, first);
-    CUDA_TRY(cudaGetLastError());
-    count_launches(2);
-    LambertInputs in2 = in;
-    in2.nadir_first = first;
-    for (int b0 = 0; b0 < nsolve; b0 += slice) {
-      const int cnt = nsolve - b0 < slice ? nsolve - b0 : slice;
-      if (b0 > 0) CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
-      k_team_setup<NS, T><<<(unsigned)((cnt + 31) / 32), 32, 0, s>>>(opt, in2, q, base_p, b0, cnt, rad, refl, nf, st,
-                                                                     (unsigned char*)(base_p + live_off));
-      k_team_series<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(
-          opt, in2, q, base_p, b0, cnt, (T*)(base_p + sweep_off), swl.total, counter,
-          (const unsigned char*)(base_p + live_off), rad, refl, nf, st, wl);
-      CUDA_TRY(cudaGetLastError());
-      count_launches(2);
-    }
-    return 0;
+    return enqueue_team_two_pass<NS, T>(opt, in, q, (char*)c.pad->scratch.p, live_off, sweep_off, nblocks, slice,
+                                        counter, counter + 1, rad, refl, nf, st, s, wl);
   }
   CUDA_TRY(cudaFuncSetAttribute(k_scalar_lambert_team<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
@@ -306,8 +328,36 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
                                 int* st, cudaStream_t s, const Worklist& wl) {
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
+  if (sc.kernel == 1 && !wl.in_list) {
+    // two-pass team solve when the arena holds per-solve scratch for a slice of
+    // at least two solves per resident warp (or the whole batch)
+    constexpr int WPB = 2;
+    int per_sm = 0;
+    if (int rc = team_series_blocks_per_sm<NS, T>(&per_sm)) return rc;
+    if (sc.blocks_per_sm > 0 && sc.blocks_per_sm < per_sm) per_sm = sc.blocks_per_sm;
+    long nblocks = (long)per_sm * num_sms;
+    if (nblocks > ((long)nsolve + WPB - 1) / WPB) nblocks = ((long)nsolve + WPB - 1) / WPB;
+    const ScratchLayout<NS> lay(in.km, false);
+    const SweepLayout<NS> swl(in.km);
+    auto up256 = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t sweep_bytes = up256(sizeof(T) * (size_t)swl.total * (size_t)(nblocks * WPB));
+    const size_t per_solve = (size_t)lay.template bytes<T>() + 1;
+    long fit = arena_bytes > sweep_bytes + 1024 ? (long)((arena_bytes - sweep_bytes - 1024) / per_solve) : 0;
+    long slice = nsolve < kSetupSlice ? nsolve : kSetupSlice;
+    if (slice > fit) slice = fit;
+    if (slice >= nsolve || slice >= 2 * nblocks * WPB) {
+      Quad q;
+      std::memset(&q, 0, sizeof(q));
+      gauss_legendre01(NS, q.qx, q.qw);
+      if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
+      const size_t live_off = up256((size_t)lay.template bytes<T>() * slice);
+      const size_t sweep_off = live_off + up256((size_t)slice);
+      return enqueue_team_two_pass<NS, T>(opt, in, q, (char*)arena, live_off, sweep_off, nblocks, (int)slice, sched,
+                                          sched + 1, rad, refl, nf, st, s, wl);
+    }
+  }
   if (sc.kernel == 1) {
-    // team kernel: per warp 32 set-up scratches + one sweep region, all inside the arena
+    // fused team kernel: per warp 32 set-up scratches + one sweep region, all inside the arena
     constexpr int WPB = 2;
     const ScratchLayout<NS> tlay(in.km, false);
     const SweepLayout<NS> swl(in.km);
