@@ -167,7 +167,6 @@ struct TeamMem {
   T cqx[NS], cqw[NS], csqw[NS], csin[NS];  // quadrature cosines, weights, sqrt(weights), sines
   int vp_valid;
   T red[2 * kTeam];
-  int ired[kTeam];
   int flag;
 };
 
