@@ -142,8 +142,10 @@ __global__ void __launch_bounds__(32) k_team_setup(RtOptions opt, LambertInputs 
   }
 }
 
+// FP32 register caps as for the fused kernel; without the set-up code the
+// 12-stream series kernel also fits 128 registers (16 warps per SM, no spills).
 template <int NS, typename T, int WPB>
-__global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 8 ? 8 : 6) : 1)
+__global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 12 ? 8 : 6) : 1)
     k_team_series(RtOptions opt, LambertInputs in, Quad q, void* scratch, int base, int count, T* sweep,
                   long sweep_per_warp, int* counter, const unsigned char* live, double* rad, double* refl, int* nf,
                   int* st, Worklist wl) {
