@@ -17,3 +17,10 @@ def golden_solar():
     import json
     with open(os.path.join(ROOT, "tests", "golden", "solar_tester.json")) as f:
         return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def golden_obsgeo():
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "obsgeo_lpcs.json")) as f:
+        return json.load(f)
