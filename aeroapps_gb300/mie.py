@@ -4,9 +4,10 @@ Mirrors the reference interface of
   src/Shared/GMAO_Shared/Chem_Base/Chem_MieMod.F90      (Chem_MieCreate, Chem_MieQueryIdx,
                                                          Chem_MieQuery, Chem_MieDestroy)
   src/Components/rtms/geo_vlidort/VLIDORT_MieMod.F90    (VLIDORT_getAOPvector)
-with the tables held on the GPU.  Table data come from
-`generate_tables` (a Lorenz-Mie series over lognormal size distributions),
-since the GEOS optics_*.nc files are not part of this project.
+with the tables held on the GPU.  Table data come either from GEOS
+optics_*.nc files (`read_tables`: the netCDF read and the wavelength
+interpolation of Chem_MieTableRead, Chem_MieTableMod.F90:238-719) or from
+`generate_tables` (a Lorenz-Mie series over lognormal size distributions).
 """
 import ctypes
 import dataclasses
@@ -109,11 +110,135 @@ def generate_tables(channels_nm, nmom=64, nrh=NRH, nradii=160, use_cache=True):
     return MieTableSet((channels_nm * 1e-9).astype(np.float32), tabs)
 
 
-class ChemMie:
-    """Device-resident Chem_Mie object (Chem_MieMod.F90:41-47)."""
+_HDF5_MAGIC = b"\x89HDF\r\n\x1a\n"
+_FIELDS3 = ("lambda", "rh", "radius")
+_FIELDS5 = ("lambda", "rh", "radius", "nMom", "nPol")
 
-    def __init__(self, tableset):
+
+def read_optics_file(path):
+    """The arrays Chem_MieTableRead reads from one optics_*.nc file
+    (Chem_MieTableMod.F90:297-466): lambda [m], rh, and bext, bsca, g
+    (nlambda, nrh, nbin) and pmom (nlambda, nrh, nbin, nMom, nPol) as REAL*8,
+    axes ordered by dimension name whatever the file's declaration order
+    (pmom None when the file has none).  Values are taken as stored, without
+    scale/offset attributes, as nf_get_var_double does.
+
+    Reads netCDF classic and 64-bit-offset files; a netCDF-4 (HDF5) file is
+    refused with a message (convert it with `nccopy -k classic`, or read it
+    elsewhere and call `table_from_file_arrays`)."""
+    from scipy.io import netcdf_file
+    with open(path, "rb") as fh:
+        if fh.read(8) == _HDF5_MAGIC:
+            raise ValueError("%s is netCDF-4/HDF5; this reader takes netCDF classic files "
+                             "(convert with: nccopy -k classic)" % path)
+    out = {}
+    with netcdf_file(path, "r", mmap=False) as nc:
+        v = nc.variables
+
+        def arr(name, order):
+            var = v[name]
+            dims = tuple(var.dimensions)
+            if sorted(dims) != sorted(order):
+                raise ValueError("%s: variable %s has dimensions %s, expected %s" % (path, name, dims, order))
+            a = np.asarray(var.data, np.float64)
+            return np.asfortranarray(np.transpose(a, [dims.index(d) for d in order]))
+
+        out["lambda"] = np.asarray(v["lambda"].data, np.float64).ravel().copy()
+        out["rh"] = np.asarray(v["rh"].data, np.float64).ravel().copy()
+        for name in ("bext", "bsca", "g"):
+            out[name] = arr(name, _FIELDS3)
+        out["pmom"] = arr("pmom", _FIELDS5) if "pmom" in v else None
+    return out
+
+
+def table_from_file_arrays(name, lam, rh, bext, bsca, g, pmom, channels_m, nmom):
+    """Chem_MieTableRead's set-up of one table (Chem_MieTableMod.F90:557-601):
+    the file arrays (wavelength first, REAL*8) interpolated to channels_m [m]
+    with the reference's polint, through aerort_mie_table_interp.  Returns
+    (MieTable, number of channels outside the table's wavelength range)."""
+    f = lambda a: np.asfortranarray(a, np.float64)
+    lam = np.ascontiguousarray(lam, np.float64)
+    rh = np.ascontiguousarray(rh, np.float64)
+    bext, bsca, g = f(bext), f(bsca), f(g)
+    nlam, nrh, nbin = bext.shape
+    if pmom is None:
+        if nmom > 0:
+            raise ValueError("table %s has no pmom, %d moments requested" % (name, nmom))
+        pmom = np.zeros((nlam, nrh, nbin, 0, 1))
+    pmom = f(pmom)
+    nmom_table, npol = pmom.shape[3], pmom.shape[4]
+    ch = np.ascontiguousarray(channels_m, np.float32)
+    nch = len(ch)
+    orh = np.zeros(nrh, np.float32)
+    ob = [np.zeros((nrh, nch, nbin), np.float32, order="F") for _ in range(3)]
+    opm = np.zeros((nrh, nch, nbin, nmom, npol), np.float32, order="F")
+    nout = ctypes.c_int(0)
+    rc = _lib.lib().aerort_mie_table_interp(
+        nlam, _lib.ptr(lam, _lib.P_d), nrh, _lib.ptr(rh, _lib.P_d), nbin, nmom_table, npol,
+        _lib.ptr(bext, _lib.P_d), _lib.ptr(bsca, _lib.P_d), _lib.ptr(g, _lib.P_d),
+        _lib.ptr(pmom, _lib.P_d) if pmom.size else None, nch, _lib.ptr(ch, _lib.P_f), nmom,
+        _lib.ptr(orh, _lib.P_f), *[_lib.ptr(a, _lib.P_f) for a in ob], _lib.ptr(opm, _lib.P_f) if opm.size else None,
+        ctypes.byref(nout))
+    if rc != 0:
+        raise RuntimeError("aerort_mie_table_interp rc=%d for table %s (nmom %d, table has %d)"
+                           % (rc, name, nmom, nmom_table))
+    return MieTable(name, orh, ob[0], ob[1], ob[2], opm), nout.value
+
+
+def read_tables(files, channels_nm, nmom):
+    """Chem_MieCreate's table reads (Chem_MieMod.F90:326-339): one optics file
+    per species, {name: path} in table order, each interpolated to the
+    channels [nm].  Channels outside a table's wavelength range are allowed,
+    as in the reference, and reported through warnings.warn."""
+    import warnings
+    ch = (np.asarray(channels_nm, np.float64) * 1e-9).astype(np.float32)
+    tabs = []
+    for name, path in files.items():
+        a = read_optics_file(path)
+        t, nout = table_from_file_arrays(name, a["lambda"], a["rh"], a["bext"], a["bsca"], a["g"], a["pmom"], ch, nmom)
+        if nout:
+            warnings.warn("Mie table %s (%s): %d channel(s) outside its wavelength range %g..%g m"
+                          % (name, path, nout, a["lambda"][0], a["lambda"][-1]))
+        tabs.append(t)
+    return MieTableSet(ch, tabs)
+
+
+def registry_map(groups, tables):
+    """The tracer -> (table, bin) hash of Chem_MieCreate (Chem_MieMod.F90:345-399).
+
+    groups: {species: [tracer names in registry order]} with species among
+    du, ss, oc, brc, bc, su, ni; tables: the table names in table order.
+    du/ss/oc/brc/bc tracers take bins 1, 2, ... in registry order; for su only
+    the names beginning so4/SO4/sul/SUL, and for ni only no3/NO3, count, the
+    others keep no optics.  Returns {upper-case name: (table index, 0-based
+    bin)}; unmapped names are absent."""
+    out = {}
+    for sp, names in groups.items():
+        ti = tables.index(sp)
+        if sp in ("du", "ss", "oc", "brc", "bc"):
+            for b, n in enumerate(names):
+                out[n.strip().upper()] = (ti, b)
+        elif sp in ("su", "ni"):
+            keys = ("so4", "SO4", "sul", "SUL") if sp == "su" else ("no3", "NO3")
+            b = 0
+            for n in names:
+                if n.strip()[:3] in keys:
+                    out[n.strip().upper()] = (ti, b)
+                    b += 1
+        else:
+            raise ValueError("unknown species group %r" % sp)
+    return out
+
+
+class ChemMie:
+    """Device-resident Chem_Mie object (Chem_MieMod.F90:41-47).
+
+    registry: optional {upper-case tracer name: (table, bin)} as made by
+    registry_map; without it tracer names are <table name><bin, 3 digits>."""
+
+    def __init__(self, tableset, registry=None):
         self.tableset = tableset
+        self.registry = registry
         self.names = [t.name for t in tableset.tables]
         descs = (_lib.MieTableDesc * len(tableset.tables))()
         self._keep = []
@@ -136,8 +261,15 @@ class ChemMie:
         self.channels = ch
 
     def query_idx(self, vname):
-        """Chem_MieQueryIdx (Chem_MieMod.F90:720-777): tracer name -> (table, bin) or (-1, -1)."""
-        v = vname.strip().lower()
+        """Chem_MieQueryIdx (Chem_MieMod.F90:720-777): tracer name -> (table, bin) or (-1, -1).
+        Case-insensitive; a qualifier such as GOCART:: is dropped (:750-754)."""
+        v = vname.strip()
+        i = v.find("::")
+        if i >= 0:
+            v = v[i + 2:]
+        if self.registry is not None:
+            return self.registry.get(v.strip().upper(), (-1, -1))
+        v = v.strip().lower()
         for ti, t in enumerate(self.tableset.tables):
             for b in range(t.bext.shape[2]):
                 if v == "%s%03d" % (t.name, b + 1):

@@ -66,6 +66,28 @@ int aerort_mie_create(int ntables, const aerort_mie_table_desc* tables, int nch,
                       aerort_mie** out);
 int aerort_mie_destroy(aerort_mie* mie);
 
+/* Chem_MieTableRead after the netCDF read (Chem_MieTableMod.F90:557-627):
+ * brings one species table from its file wavelengths to the requested
+ * channels with the reference's polint (:671-717) — linear in wavelength,
+ * REAL*8 in, REAL*4 slope/offset/result; below the first table wavelength it
+ * extrapolates the first segment, above the last it holds the last value —
+ * and converts the RH grid to REAL*4.  Host code; no GPU needed.
+ * Inputs in file (Fortran) order, wavelength fastest:
+ *   lambda_table(nlam) [m], rh_table(nrh), bext/bsca/g_table(nlam,nrh,nbin),
+ *   pmom_table(nlam,nrh,nbin,nmom_table,npol) (may be NULL when nmom = 0).
+ * Outputs in the aerort_mie_table_desc order:
+ *   rh(nrh), bext/bsca/g(nrh,nch,nbin), pmom(nrh,nch,nbin,nmom,npol) (the
+ *   first nmom moments).
+ * channels_m(nch) [m] as Chem_Mie%channels.  nout (optional) receives the
+ * number of channels outside the table's wavelength range (the reference
+ * prints a warning for each interpolation there).
+ * rc: 0; 99 when nmom > nmom_table (Chem_MieTableMod.F90:331-335);
+ * AERORT_RC_ARG for bad sizes, NULL pointers or NaN wavelengths. */
+int aerort_mie_table_interp(int nlam, const double* lambda_table, int nrh, const double* rh_table, int nbin,
+                            int nmom_table, int npol, const double* bext_table, const double* bsca_table,
+                            const double* g_table, const double* pmom_table, int nch, const float* channels_m,
+                            int nmom, float* rh, float* bext, float* bsca, float* g, float* pmom, int* nout);
+
 /* VLIDORT_getAOPvector (geo_vlidort/VLIDORT_MieMod.F90:124-336) with
  * Chem_MieQuery (Chem_MieMod.F90:789-965) for every tracer.  The tracer names
  * vname(nq,16) of the reference are resolved by the caller (Chem_MieQueryIdx,

@@ -146,3 +146,56 @@ int oracle_get_aop_vector(int ntables, const OracleMieTable* tables, int km, int
   free(idxch);
   return 0;
 }
+
+/* polint of Chem_MieTableRead (Chem_MieTableMod.F90:671-717), as the
+ * reference declares it: x(n), y(n) REAL*8; xWant, slope, dx, yWant REAL*4.
+ * Returns 1 when the reference would print its out-of-range warning. */
+int oracle_mie_polint(const double* x, const double* y, int n, float xwant, float* ywant) {
+  int i = 0, warn = 0, j;
+  float slope, dx, sdx;
+  if ((double)xwant < x[0]) { warn = 1; i = 1; }
+  if ((double)xwant > x[n - 1]) { warn = 1; i = n; }
+  if (i == 0)
+    for (j = 1; j <= n; ++j)
+      if ((double)xwant >= x[j - 1]) i = j;
+  if (i == n)
+    slope = 0.0f;
+  else
+    slope = (float)((y[i] - y[i - 1]) / (x[i] - x[i - 1]));
+  dx = (float)((double)xwant - x[i - 1]);
+  sdx = slope * dx;
+  *ywant = (float)(y[i - 1] + (double)sdx);
+  return warn;
+}
+
+/* The interpolation loop of Chem_MieTableRead (Chem_MieTableMod.F90:575-601)
+ * for bext, bsca, g and the first nmom moments of pmom, with the table read
+ * as REAL*8 in file order (lambda fastest) and the result in Chem_MieTable
+ * order (rh fastest).  Returns the number of polint warnings. */
+int oracle_mie_table_interp(int nlam, const double* lam, int nrh, const double* rh_table, int nbin, int nmom_table,
+                            int npol, const double* bext_t, const double* bsca_t, const double* g_t,
+                            const double* pmom_t, int nch, const float* channels, int nmom, float* rh, float* bext,
+                            float* bsca, float* g, float* pmom) {
+  int warns = 0;
+  double* col = (double*)malloc(sizeof(double) * (size_t)nlam);
+  for (int i = 0; i < nrh; ++i) rh[i] = (float)rh_table[i];
+  for (int j = 0; j < nbin; ++j)
+    for (int i = 0; i < nrh; ++i)
+      for (int n = 0; n < nch; ++n) {
+        const long o = i + (long)nrh * (n + (long)nch * j);
+        const long t = (long)nlam * (i + (long)nrh * j);
+        warns += oracle_mie_polint(lam, bext_t + t, nlam, channels[n], &bext[o]);
+        warns += oracle_mie_polint(lam, bsca_t + t, nlam, channels[n], &bsca[o]);
+        warns += oracle_mie_polint(lam, g_t + t, nlam, channels[n], &g[o]);
+        for (int m = 0; m < nmom; ++m)
+          for (int p = 0; p < npol; ++p) {
+            /* gather the wavelength column of pmom_table(:, i, j, m, p) */
+            for (int l = 0; l < nlam; ++l)
+              col[l] = pmom_t[l + (long)nlam * (i + (long)nrh * (j + (long)nbin * (m + (long)nmom_table * p)))];
+            warns += oracle_mie_polint(lam, col, nlam, channels[n],
+                                       &pmom[i + (long)nrh * (n + (long)nch * (j + (long)nbin * (m + (long)nmom * p)))]);
+          }
+      }
+  free(col);
+  return warns;
+}

@@ -93,6 +93,27 @@ def rh_map(rh):
     return rhi, rha
 
 
+def mie_table_interp(lam, rh_table, bext, bsca, g, pmom, channels_m, nmom):
+    """Chem_MieTableRead's wavelength interpolation (Chem_MieTableMod.F90:575-601).
+
+    Table fields in file order, wavelength first: bext/bsca/g (nlam,nrh,nbin),
+    pmom (nlam,nrh,nbin,nmom_table,npol).  Returns (rh, bext, bsca, g, pmom,
+    warnings) in Chem_MieTable order, REAL*4."""
+    lam = np.ascontiguousarray(lam, np.float64)
+    rh_table = np.ascontiguousarray(rh_table, np.float64)
+    f = lambda a: np.asfortranarray(a, np.float64)
+    bext, bsca, g, pmom = f(bext), f(bsca), f(g), f(pmom)
+    ch = np.ascontiguousarray(channels_m, np.float32)
+    nlam, nrh, nbin, nmom_table, npol = pmom.shape
+    nch = len(ch)
+    out = [np.zeros(nrh, np.float32)] + [np.zeros((nrh, nch, nbin), np.float32, order="F") for _ in range(3)]
+    opm = np.zeros((nrh, nch, nbin, nmom, npol), np.float32, order="F")
+    warns = lib().oracle_mie_table_interp(nlam, _p(lam, P_d), nrh, _p(rh_table, P_d), nbin, nmom_table, npol,
+                                          _p(bext, P_d), _p(bsca, P_d), _p(g, P_d), _p(pmom, P_d), nch, _p(ch, P_f),
+                                          nmom, *[_p(a, P_f) for a in out], _p(opm, P_f))
+    return out[0], out[1], out[2], out[3], opm, warns
+
+
 def get_aop_vector(tableset, km, nobs, nch, nq, channels_nm, q_table, q_bin, qm, rh, nMom, nPol):
     """Oracle VLIDORT_getAOPvector on a mie.MieTableSet; returns (tau, ssa, g, pmom, rc)."""
     keep = []
