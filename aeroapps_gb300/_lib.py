@@ -49,6 +49,9 @@ _SIGNATURES = {
                                                       [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
     "aerort_vlidort_scalar_lambert_mixed_batch": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, P_i] + [P_d] * 10 +
                                                   [c_double, P_d, P_d, P_i, P_i]),
+    "aerort_get_edge_vars": (c_int, [c_int, c_int, P_f, P_f, ctypes.c_float, P_f, P_f, P_f]),
+    "aerort_get_edge_vars_dev": (c_int, [c_int, c_int, c_void_p, c_void_p, ctypes.c_float, c_void_p, c_void_p,
+                                         c_void_p, c_void_p]),
     "aerort_vlidort_rot_calc": (c_int, [c_int, c_int, c_int, P_d, P_d, P_d, P_d, c_double, c_int, P_d, P_d]),
     "aerort_vlidort_rot_calc_dev": (c_int, [c_int, c_int, c_int] + [c_void_p] * 7),
     "aerort_set_schedule": (c_int, [c_int, c_int, c_int, c_int]),

@@ -312,3 +312,20 @@ def get_aop_vector(mie, km, nobs, nch, nq, channels, vname, verbose, qm, rh, nMo
     if rc not in (0, 99, 666, 777):
         raise RuntimeError("aerort_get_aop_vector rc=%d: %s" % (rc, _lib.last_error()))
     return tau, ssa, g, pmom, rc
+
+
+def get_edge_vars(km, nobs, airdens, delp, ptop):
+    """getEdgeVars (MieObs_py.F90:27-83) on the GPU: edge pressure [Pa],
+    height above the surface [m] and temperature [K], each (km+1, nobs) REAL*4,
+    from airdens and delp (km, nobs) and the top pressure ptop [Pa].
+    Returns (pe, ze, te) like the f2py routine."""
+    rho = np.asfortranarray(airdens, np.float32)
+    dp = np.asfortranarray(delp, np.float32)
+    if rho.shape != (km, nobs) or dp.shape != (km, nobs):
+        raise ValueError("airdens and delp must be (km, nobs) = (%d, %d)" % (km, nobs))
+    pe, ze, te = [np.zeros((km + 1, nobs), np.float32, order="F") for _ in range(3)]
+    rc = _lib.lib().aerort_get_edge_vars(km, nobs, _lib.ptr(rho, _lib.P_f), _lib.ptr(dp, _lib.P_f), float(ptop),
+                                         _lib.ptr(pe, _lib.P_f), _lib.ptr(ze, _lib.P_f), _lib.ptr(te, _lib.P_f))
+    if rc != 0:
+        raise RuntimeError("aerort_get_edge_vars rc=%d: %s" % (rc, _lib.last_error()))
+    return pe, ze, te

@@ -194,6 +194,19 @@ int aerort_vlidort_scalar_lambert_mixed_batch(int km, int nch, int nobs, int nst
                                               double MISSING, double* radiance_VL, double* reflectance_VL,
                                               int* nfourier, int* status);
 
+/* Edge pressure pe (Pa), height above the surface ze (m) and temperature te
+ * (K), each (km+1,nobs), from layer air density airdens (kg m-3) and pressure
+ * thickness delp (Pa), each (km,nobs), and the top pressure ptop (Pa).
+ * Replaces getEdgeVars (Chem_Base/MieObs_py.F90:27-83), same argument list
+ * with rc as the return value.  FP32 like the reference: pe and ze
+ * bit-identical, te within a few units in the last place (logf/powf).
+ * rc: 0; AERORT_RC_ARG; AERORT_RC_NLAYERS when km > 318.  _dev: every array on
+ * the device, enqueued on `stream`. */
+int aerort_get_edge_vars(int km, int nobs, const float* airdens, const float* delp, float ptop, float* pe, float* ze,
+                         float* te);
+int aerort_get_edge_vars_dev(int km, int nobs, const float* airdens, const float* delp, float ptop, float* pe,
+                             float* ze, float* te, void* stream);
+
 /* Rayleigh optical thickness ROT(km,nobs,nch) and depolarisation ratio
  * depol(nch) from the edge profiles pe (Pa), he (m), te (K), each
  * (km+1,nobs), at channels(nch) nm.  Replaces VLIDORT_ROT_CALC

@@ -145,6 +145,16 @@ def get_aop_vector(tableset, km, nobs, nch, nq, channels_nm, q_table, q_bin, qm,
     return tau, ssa, g, pmom, rc
 
 
+def get_edge_vars(airdens, delp, ptop):
+    """getEdgeVars (MieObs_py.F90:27-83): (pe, ze, te), each (km+1, nobs), REAL*4."""
+    rho = np.asfortranarray(airdens, np.float32)
+    dp = np.asfortranarray(delp, np.float32)
+    km, nobs = rho.shape
+    out = [np.zeros((km + 1, nobs), np.float32, order="F") for _ in range(3)]
+    lib().oracle_get_edge_vars(km, nobs, _p(rho, P_f), _p(dp, P_f), ctypes.c_float(ptop), *[_p(a, P_f) for a in out])
+    return tuple(out)
+
+
 def rot_calc(channels, pe, he, te):
     """VLIDORT_ROT_CALC restated (rot_oracle.c): pe, he, te (km+1, nobs) -> ROT (km, nobs, nch), depol (nch), rc."""
     pe, he, te = (np.asfortranarray(a, np.float64) for a in (pe, he, te))
