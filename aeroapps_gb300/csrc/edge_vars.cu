@@ -13,14 +13,16 @@
 // Layout: one thread per column, one warp of 32 columns per block.  The 32
 // columns of a block are contiguous in the (km, nobs) inputs and in the
 // (km+1, nobs) outputs, so they move between HBM and shared memory as whole
-// coalesced chunks; each thread then walks its own column in shared memory
-// (odd column stride, so the 32 lanes hit 32 banks).
+// coalesced chunks, with several loads in flight per lane; each thread then
+// walks its own column in shared memory (odd column stride, so the 32 lanes
+// hit 32 banks).
 #include "aerort_internal.cuh"
 
 namespace aerort_internal {
 namespace {
 
 constexpr int kEdgeCols = 32;
+constexpr int kBatch = 9;  // loads in flight per lane and input (72-layer chunk: 2304 words = 8 x 9 x 32)
 constexpr float kGrav = 9.80616f;
 constexpr float kRgas = 287.0f;
 constexpr float kKappa = 2.0f / 7.0f;  // REAL parameter 2.0/7.0, a single-precision quotient
@@ -45,12 +47,29 @@ __global__ void __launch_bounds__(kEdgeCols) k_edge_vars(int km, int nobs, const
   const int lane = threadIdx.x;
   for (long c0 = (long)blockIdx.x * kEdgeCols; c0 < nobs; c0 += (long)gridDim.x * kEdgeCols) {
     const int nc = (int)min((long)kEdgeCols, (long)nobs - c0);
-    for (int j = 0; j < nc; ++j) {
-      const float* a = airdens + (c0 + j) * km;
-      const float* d = delp + (c0 + j) * km;
-      for (int k = lane; k < km; k += kEdgeCols) {
-        s_rho[j * ks + k] = a[k];
-        s_dp[j * ks + k] = d[k];
+    // the block's nc columns are one contiguous chunk of nc*km words per input:
+    // each lane issues kBatch loads of both inputs before it stores any
+    const int nin = nc * km;
+    const float* a = airdens + c0 * km;
+    const float* d = delp + c0 * km;
+    for (int base = lane; base < nin; base += kEdgeCols * kBatch) {
+      float va[kBatch], vd[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int i = base + u * kEdgeCols;
+        if (i < nin) {
+          va[u] = a[i];
+          vd[u] = d[i];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int i = base + u * kEdgeCols;
+        if (i < nin) {
+          const int j = i / km, k = i - j * km;
+          s_rho[j * ks + k] = va[u];
+          s_dp[j * ks + k] = vd[u];
+        }
       }
     }
     __syncwarp();
@@ -79,13 +98,14 @@ __global__ void __launch_bounds__(kEdgeCols) k_edge_vars(int km, int nobs, const
       T[km] = __fmul_rn(tm_prev, powf(__fdiv_rn(P[km], pm_prev), kKappa));  // dry adiabatic at the surface
     }
     __syncwarp();
-    for (int j = 0; j < nc; ++j) {
-      const long o = (c0 + j) * (km + 1);
-      for (int k = lane; k <= km; k += kEdgeCols) {
-        pe[o + k] = s_pe[j * es + k];
-        ze[o + k] = s_ze[j * es + k];
-        te[o + k] = s_te[j * es + k];
-      }
+    // outputs: one contiguous chunk of nc*(km+1) words each
+    const int ne = km + 1, nout = nc * ne;
+    const long o = c0 * ne;
+    for (int i = lane; i < nout; i += kEdgeCols) {
+      const int j = i / ne, k = i - j * ne;
+      pe[o + i] = s_pe[j * es + k];
+      ze[o + i] = s_ze[j * es + k];
+      te[o + i] = s_te[j * es + k];
     }
     __syncwarp();
   }

@@ -262,6 +262,88 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _hbm_peak():
+    try:
+        peak = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")))["hbm_gbs"]
+        return peak, "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy), of measured"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s, of fallback"
+
+
+def _time_flushed(torch, call, reps=20):
+    """Mean CUDA-event time [ms] of call() on the current stream, L2 flushed
+    (512 MB write) before each launch so that every launch reads from HBM."""
+    from aeroapps_gb300 import _lib
+    for _ in range(3):
+        assert call() == 0, _lib.last_error()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    ms = 0.0
+    for _ in range(reps):
+        flush.zero_()
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record()
+        call()
+        r1.record()
+        torch.cuda.synchronize()
+        ms += r0.elapsed_time(r1) / reps
+    return ms
+
+
+def front_end_rooflines(torch, L, batch, stream, ncr=262144):
+    """Rooflines of the two front-end kernels on the 262,144 columns of the
+    batching configuration (this batch's profiles tiled), against the measured
+    copy bandwidth:
+    - k_rot_calc (VLIDORT_ROT_CALC, FP64): algorithmic bytes = pe, he, te read
+      once per pixel + ROT written per pixel and channel (+ depol);
+    - k_edge_vars (getEdgeVars, FP32): airdens, delp read + pe, ze, te written."""
+    from aeroapps_gb300 import synth
+    P = lambda t: t.data_ptr()
+    kmb = batch["km"]
+    my_cols = batch["ncol"]
+    nch = len(CHANNELS)
+    peak, src = _hbm_peak()
+    # Fortran (k, columns) = C (columns, k), tiled to ncr columns
+    tile = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dt).T)).cuda().repeat(
+        (ncr + my_cols - 1) // my_cols, 1)[:ncr].contiguous()
+    dpe, dhe, dte = (tile(batch[k], np.float64) for k in ("pe", "he", "te"))
+    dch = torch.from_numpy(np.array(CHANNELS, np.float64)).cuda()
+    drot = torch.empty(kmb * ncr * nch, dtype=torch.float64, device="cuda")
+    ddep = torch.empty(nch, dtype=torch.float64, device="cuda")
+    ms_rot = _time_flushed(torch, lambda: L.aerort_vlidort_rot_calc_dev(kmb, nch, ncr, P(dch), P(dpe), P(dhe), P(dte),
+                                                                      P(drot), P(ddep), stream))
+    del dpe, dhe, dte, drot
+    alg = 3 * (kmb + 1) * 8 * ncr + kmb * ncr * nch * 8 + nch * 8
+    ach = alg / (ms_rot * 1e-3) / 1e9
+    rot_line = {"kernel": "k_rot_calc (VLIDORT_ROT_CALC)", "bound": "hbm", "ms_per_launch": ms_rot,
+                "limiter": "FP64 issue: two correctly rounded FP64 divisions per layer edge and pixel (bit "
+                           "identity with the reference rules out reciprocal products); GB300 runs FP64 at "
+                           "about 1 TFLOP/s",
+                "algorithmic_bytes": alg, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_source": src, "columns": ncr, "wavelengths": nch, "layers": kmb,
+                "note": "L2 flushed (512 MB write) before each timed launch"}
+    # layer air density and pressure thickness of full-height columns with km
+    # layers (the batch's shorter columns are padded with empty layers)
+    ue = synth.make_columns(min(my_cols, 4096), [550.0], seed=3, nlayers=kmb)
+    pe, te = ue["pe"], ue["te"]
+    pm = 0.5 * (pe[1:] + pe[:-1])
+    rho = pm / (synth.RGAS * 0.5 * (te[1:] + te[:-1]))
+    my_cols = ue["ncol"]
+    drho, ddp = tile(rho, np.float32), tile(np.diff(pe, axis=0), np.float32)
+    out = torch.empty(3 * (kmb + 1) * ncr, dtype=torch.float32, device="cuda")
+    ne = (kmb + 1) * ncr
+    ptop = float(pe[0, 0])
+    ms_edge = _time_flushed(torch, lambda: L.aerort_get_edge_vars_dev(kmb, ncr, P(drho), P(ddp), ptop, P(out),
+                                                                    P(out) + 4 * ne, P(out) + 8 * ne, stream))
+    del drho, ddp, out
+    alg = 2 * kmb * 4 * ncr + 3 * (kmb + 1) * 4 * ncr
+    ach = alg / (ms_edge * 1e-3) / 1e9
+    edge_line = {"kernel": "k_edge_vars (getEdgeVars)", "bound": "hbm", "ms_per_launch": ms_edge,
+                 "algorithmic_bytes": alg, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                 "peak_source": src, "columns": ncr, "layers": kmb,
+                 "note": "L2 flushed (512 MB write) before each timed launch"}
+    return rot_line, edge_line
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -503,52 +585,10 @@ def main():
         e2e_val = solves / ((time.perf_counter() - t) / args.e2e_steps)
         assert np.isfinite(got)
 
-    # ---------------------------------------------------------------- Rayleigh optical thickness kernel
-    # VLIDORT_ROT_CALC on the device for the whole batch (km = 72 edges profiles):
-    # algorithmic bytes = pe, he, te read once per pixel + ROT written per pixel
-    # and channel (+ depol); HBM-bound, against the measured copy bandwidth
-    rot_line = None
+    # ---------------------------------------------------------------- front end kernels (ROT, edge profiles)
+    rot_line = edge_line = None
     if rank == 0:
-        # the 262,144 columns of the batching configuration: this batch's edge
-        # profiles tiled (Fortran (km+1, columns) = C (columns, km+1))
-        kmb = batch["km"]
-        ncr = 262144
-        tile = lambda a: torch.from_numpy(np.ascontiguousarray(np.asarray(a, np.float64).T)).cuda().repeat(
-            (ncr + my_cols - 1) // my_cols, 1)[:ncr].contiguous()
-        dpe, dhe, dte = (tile(batch[k]) for k in ("pe", "he", "te"))
-        dch = dev(np.array(CHANNELS), np.float64)
-        drot = torch.empty(kmb * ncr * nch, dtype=torch.float64, device="cuda")
-        ddep = torch.empty(nch, dtype=torch.float64, device="cuda")
-        call = lambda: L.aerort_vlidort_rot_calc_dev(kmb, nch, ncr, P(dch), P(dpe), P(dhe), P(dte), P(drot),
-                                                     P(ddep), stream)
-        for _ in range(3):
-            assert call() == 0, _lib.last_error()
-        flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > L2: each launch reads from HBM
-        reps, ms_rot = 20, 0.0
-        for _ in range(reps):
-            flush.zero_()
-            r0, r1 = ev(), ev()
-            r0.record()
-            call()
-            r1.record()
-            torch.cuda.synchronize()
-            ms_rot += r0.elapsed_time(r1) / reps
-        del flush, dpe, dhe, dte, drot
-        alg = 3 * (kmb + 1) * 8 * ncr + kmb * ncr * nch * 8 + nch * 8
-        peak = None
-        try:
-            peak = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")))["hbm_gbs"]
-            src = "MEASURED_PEAKS.json hbm_gbs (STREAM-style copy), of measured"
-        except (OSError, ValueError, KeyError):
-            peak, src = 6800.0, "fallback 6.8 TB/s, of fallback"
-        ach = alg / (ms_rot * 1e-3) / 1e9
-        rot_line = {"kernel": "k_rot_calc (VLIDORT_ROT_CALC)", "bound": "hbm", "ms_per_launch": ms_rot,
-                    "limiter": "FP64 issue: two correctly rounded FP64 divisions per layer edge and pixel (bit "
-                               "identity with the reference rules out reciprocal products); GB300 runs FP64 at "
-                               "about 1 TFLOP/s",
-                    "algorithmic_bytes": alg, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                    "peak_source": src, "columns": ncr, "wavelengths": nch, "layers": kmb,
-                    "note": "L2 flushed (512 MB write) before each timed launch"}
+        rot_line, edge_line = front_end_rooflines(torch, L, batch, stream)
 
     # ---------------------------------------------------------------- serving
     serving = None
@@ -617,7 +657,7 @@ def main():
                 "path": "pinned host inputs -> device copies, aerort_get_aop_vector_dev + "
                         "aerort_vlidort_scalar_lambert_mixed_batch_dev per stream group (%s), device -> pinned host "
                         "outputs, host read" % ("one CUDA stream per group" if side else "one stream")},
-        "serving": serving, "gpu_launches": launches, "clocks": clk, "rot_calc": rot_line,
+        "serving": serving, "gpu_launches": launches, "clocks": clk, "rot_calc": rot_line, "edge_vars": edge_line,
     }
     if rank == 0:
         print(json.dumps(line))
