@@ -7,7 +7,7 @@ caller-owned RT workspace (aerort_workspace), so that slots run concurrently
 without sharing scratch.  A request is admitted as soon as a slot is free and
 its device-memory estimate fits both the configured HBM budget (the device
 memory the server may hold for requests in flight) and the free device memory
-the driver reports.  Requests that arrive while others are on the GPU are
+the CUDA driver reports.  Requests that arrive while others are on the GPU are
 admitted as slots free up, and their kernels overlap on the device.  A request
 completes when the event recorded after its last device->host copy fires;
 latency is completion minus arrival.
