@@ -29,6 +29,9 @@ _SIGNATURES = {
     "aerort_mie_destroy": (c_int, [c_void_p]),
     "aerort_mie_table_interp": (c_int, [c_int, P_d, c_int, P_d, c_int, c_int, c_int, P_d, P_d, P_d, P_d, c_int, P_f,
                                         c_int, P_f, P_f, P_f, P_f, P_f, P_i]),
+    "aerort_get_aop_scalar": (c_int, [c_void_p, c_int, c_int, c_int, c_int, P_f, P_i, P_i, P_f, P_f, P_f, P_f, P_f]),
+    "aerort_get_aop_scalar_dev": (c_int, [c_void_p, c_int, c_int, c_int, c_int, P_f, P_i, P_i, c_void_p, c_void_p,
+                                          c_void_p, c_void_p, c_void_p, c_void_p]),
     "aerort_get_aop_vector": (c_int, [c_void_p, c_int, c_int, c_int, c_int, P_f, P_i, P_i, P_f, P_f, c_int, c_int,
                                       P_f, P_f, P_f, P_f]),
     "aerort_get_aop_vector_dev": (c_int, [c_void_p, c_int, c_int, c_int, c_int, P_f, P_i, P_i, c_void_p, c_void_p,

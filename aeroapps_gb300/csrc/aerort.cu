@@ -433,6 +433,24 @@ extern "C" int aerort_get_aop_vector(aerort_mie* mie, int km, int nobs, int nch,
   return AERORT_OK;
 }
 
+// VLIDORT_getAOPscalar (VLIDORT_MieMod.F90:10-120): the vector routine without
+// phase-function moments; with no moments requested neither the 666 nor the
+// 777 check can fire, as in the reference, which has neither.
+extern "C" int aerort_get_aop_scalar_dev(aerort_mie* mie, int km, int nobs, int nch, int nq,
+                                         const float* channels_nm_host, const int* q_table_host,
+                                         const int* q_bin_host, const float* qm_dev, const float* rh_dev,
+                                         float* tau_dev, float* ssa_dev, float* g_dev, void* stream) {
+  return aerort_get_aop_vector_dev(mie, km, nobs, nch, nq, channels_nm_host, q_table_host, q_bin_host, qm_dev, rh_dev,
+                                   0, 1, tau_dev, ssa_dev, g_dev, nullptr, stream);
+}
+
+extern "C" int aerort_get_aop_scalar(aerort_mie* mie, int km, int nobs, int nch, int nq, const float* channels_nm,
+                                     const int* q_table, const int* q_bin, const float* qm, const float* rh,
+                                     float* tau, float* ssa, float* g) {
+  return aerort_get_aop_vector(mie, km, nobs, nch, nq, channels_nm, q_table, q_bin, qm, rh, 0, 1, tau, ssa, g,
+                               nullptr);
+}
+
 // =========================================================================================
 // Scalar radiative transfer
 // =========================================================================================

@@ -314,6 +314,28 @@ def get_aop_vector(mie, km, nobs, nch, nq, channels, vname, verbose, qm, rh, nMo
     return tau, ssa, g, pmom, rc
 
 
+def get_aop_scalar(mie, km, nobs, nch, nq, channels, vname, verbose, qm, rh):
+    """VLIDORT_getAOPscalar (VLIDORT_MieMod.F90:10-120).
+
+    Returns (tau, ssa, g, rc), each (km,nch,nobs), FP32, Fortran order."""
+    qtab = np.empty(nq, np.int32)
+    qbin = np.empty(nq, np.int32)
+    for iq in range(nq):
+        qtab[iq], qbin[iq] = mie.query_idx(vname[iq])
+    ch = np.ascontiguousarray(channels, np.float32)
+    qm = np.asfortranarray(qm, np.float32)
+    rh = np.asfortranarray(rh, np.float32)
+    tau = np.zeros((km, nch, nobs), np.float32, order="F")
+    ssa = np.zeros_like(tau)
+    g = np.zeros_like(tau)
+    rc = _lib.lib().aerort_get_aop_scalar(mie.handle, km, nobs, nch, nq, _lib.ptr(ch, _lib.P_f), _lib.ptr(qtab, _lib.P_i),
+                                          _lib.ptr(qbin, _lib.P_i), _lib.ptr(qm, _lib.P_f), _lib.ptr(rh, _lib.P_f),
+                                          _lib.ptr(tau, _lib.P_f), _lib.ptr(ssa, _lib.P_f), _lib.ptr(g, _lib.P_f))
+    if rc not in (0, 99):
+        raise RuntimeError("aerort_get_aop_scalar rc=%d: %s" % (rc, _lib.last_error()))
+    return tau, ssa, g, rc
+
+
 def get_edge_vars(km, nobs, airdens, delp, ptop):
     """getEdgeVars (MieObs_py.F90:27-83) on the GPU: edge pressure [Pa],
     height above the surface [m] and temperature [K], each (km+1, nobs) REAL*4,

@@ -104,6 +104,16 @@ int aerort_get_aop_vector_dev(aerort_mie* mie, int km, int nobs, int nch, int nq
                               const float* rh_dev, int nMom, int nPol, float* tau_dev, float* ssa_dev,
                               float* g_dev, float* pmom_dev, void* stream);
 
+/* VLIDORT_getAOPscalar (geo_vlidort/VLIDORT_MieMod.F90:10-120): tau, ssa, g
+ * (km,nch,nobs) without phase-function moments; otherwise as
+ * aerort_get_aop_vector (rc 0 or 99). */
+int aerort_get_aop_scalar(aerort_mie* mie, int km, int nobs, int nch, int nq, const float* channels_nm,
+                          const int* q_table, const int* q_bin, const float* qm, const float* rh, float* tau,
+                          float* ssa, float* g);
+int aerort_get_aop_scalar_dev(aerort_mie* mie, int km, int nobs, int nch, int nq, const float* channels_nm_host,
+                              const int* q_table_host, const int* q_bin_host, const float* qm_dev,
+                              const float* rh_dev, float* tau_dev, float* ssa_dev, float* g_dev, void* stream);
+
 /* ------------------------------------------------------------------------------------------
  * VLIDORT_Scalar_Lambert (geo_vlidort/VLIDORT_LAMBERT.F90:34-168): scalar TOA
  * radiance and reflectance for nobs pixels x nch channels, observation

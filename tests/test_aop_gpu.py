@@ -54,3 +54,20 @@ def test_rc_codes(tables):
     assert a([550.0], 64, 1) == 666
     assert a([550.0], 8, 2) == 777
     chem.destroy()
+
+
+@pytest.mark.gpu
+def test_aop_scalar_equals_vector_without_moments(tables):
+    # VLIDORT_getAOPscalar: tau, ssa, g of the vector routine, no moments and no 666/777 checks
+    cols = synth.make_columns(40, [470.0, 550.0, 670.0, 865.0], seed=61)
+    chem = mie.ChemMie(tables)
+    names = synth.tracer_names()
+    km, n = cols["km"], cols["ncol"]
+    ch = np.asarray([550.0, 865.0], np.float32)
+    sc = mie.get_aop_scalar(chem, km, n, 2, len(names), ch, names, 0, cols["qm"], cols["rh"])
+    vec = mie.get_aop_vector(chem, km, n, 2, len(names), ch, names, 0, cols["qm"], cols["rh"], 8, 1)
+    miss = mie.get_aop_scalar(chem, km, n, 1, len(names), np.float32([551.5]), names, 0, cols["qm"], cols["rh"])
+    chem.destroy()
+    assert sc[3] == 0 and vec[4] == 0 and miss[3] == 99
+    for a, b in zip(sc[:3], vec[:3]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
