@@ -208,12 +208,14 @@ def table_index(tabs):
     return qidx
 
 
-def cpu_baseline(batch, ncols_sample):
-    """The oracle (C++ restatement of the reference path, OpenMP over all host cores) on the first columns."""
+def cpu_baseline(batch, ncols_sample, threads=0):
+    """The oracle (C++ restatement of the reference path, OpenMP over all host
+    cores, or over `threads` of them) on the first columns."""
     from oracle import oracle
     from aeroapps_gb300 import mie, synth
     sub = subset(batch, np.arange(ncols_sample))
-    cores = os.cpu_count() or 1
+    cores = threads or os.cpu_count() or 1
+    oracle.set_threads(threads)
     tabs = mie.generate_tables(list(CHANNELS), nmom=32)
     qidx = table_index(tabs)
     qt, qb = zip(*[qidx[n] for n in synth.tracer_names()])
@@ -232,6 +234,7 @@ def cpu_baseline(batch, ncols_sample):
                               nlay=g["nlayers"])
         nsolve += n * nch
     dt = time.perf_counter() - t0
+    oracle.set_threads(0)
     return {"value": nsolve / dt, "unit": "radiances/s", "cores": cores, "kind": "port",
             "sample": "%d columns x %d wavelengths of the same batch (4-16 streams, 20-72 layers): C++ oracle restating "
                       "VLIDORT 2.8.3 + Chem_MieQuery (FP64), OpenMP over pixels, %d host threads; %.1f s"
@@ -639,6 +642,8 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(batch, min(args.cpu_cols or 4096, my_cols))  # about 10 s on a 16-core host
+        one = cpu_baseline(batch, min(128, my_cols), threads=1)  # about 5 s on one core
+        cpu["single_core"] = {"value": one["value"], "unit": one["unit"], "cores": 1, "sample": one["sample"]}
     line = {
         "metric": METRIC, "value": value, "unit": "radiances/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -80,6 +80,11 @@ def scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol
     return rad, refl, rc, nf, st
 
 
+def set_threads(n):
+    """Threads of the oracle's OpenMP loop over pixels (0: every host core)."""
+    lib().oracle_set_threads(int(n))
+
+
 def set_asymtx_tol(tol):
     """Tolerance of the oracle's ASYMTX in scalar_lambert (reference: 1e-12)."""
     lib().oracle_set_asymtx_tol(ctypes.c_double(tol))

@@ -17,6 +17,8 @@
 #include <vector>
 #include <algorithm>
 
+#include <omp.h>
+
 namespace {
 
 // vlidort_def/vlidort_pars.f90:386-444 (truncated DEG_TO_RAD is reproduced on purpose)
@@ -1368,6 +1370,9 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
 // that tolerance moves the reference algorithm from the converged solution.
 static double g_asymtx_tol = 1.0e-12;
 extern "C" void oracle_set_asymtx_tol(double tol) { g_asymtx_tol = tol; }
+
+// Threads of the OpenMP loop over pixels (n <= 0: every host core).
+extern "C" void oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
 
 extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* channels, int nstreams,
                                      int plane_parallel, int nMom, int nPol, const double* ROT,
