@@ -292,13 +292,15 @@ def _time_flushed(torch, call, reps=20):
     return ms
 
 
-def front_end_rooflines(torch, L, batch, stream, ncr=262144):
-    """Rooflines of the two front-end kernels on the 262,144 columns of the
+def front_end_rooflines(torch, L, batch, stream, ncr=262144, chem=None, qt=None, qb=None):
+    """Rooflines of the front-end kernels on the 262,144 columns of the
     batching configuration (this batch's profiles tiled), against the measured
     copy bandwidth:
     - k_rot_calc (VLIDORT_ROT_CALC, FP64): algorithmic bytes = pe, he, te read
       once per pixel + ROT written per pixel and channel (+ depol);
-    - k_edge_vars (getEdgeVars, FP32): airdens, delp read + pe, ze, te written."""
+    - k_edge_vars (getEdgeVars, FP32): airdens, delp read + pe, ze, te written;
+    - k_aop (VLIDORT_getAOPvector, FP32; when a Mie object is given): qm, rh
+      read + tau, ssa, g, pmom written, 72 layers, 4 channels, 16 moments."""
     from aeroapps_gb300 import synth
     P = lambda t: t.data_ptr()
     kmb = batch["km"]
@@ -344,7 +346,35 @@ def front_end_rooflines(torch, L, batch, stream, ncr=262144):
                  "algorithmic_bytes": alg, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                  "peak_source": src, "columns": ncr, "layers": kmb,
                  "note": "L2 flushed (512 MB write) before each timed launch"}
-    return rot_line, edge_line
+    aop_line = None
+    if chem is not None:
+        from aeroapps_gb300 import _lib
+        km, nq, nmom = 72, len(qt), 16
+        ua = synth.make_columns(min(batch["ncol"], 4096), list(CHANNELS), seed=5, nlayers=km)
+        reps = (ncr + ua["ncol"] - 1) // ua["ncol"]
+        # Fortran (km, nq, columns) = C (columns, nq, km)
+        dqm = torch.from_numpy(np.ascontiguousarray(np.asarray(ua["qm"], np.float32).T)).cuda().repeat(
+            reps, 1, 1)[:ncr].contiguous()
+        drh = torch.from_numpy(np.ascontiguousarray(np.asarray(ua["rh"], np.float32).T)).cuda().repeat(
+            reps, 1)[:ncr].contiguous()
+        no = km * nch * ncr
+        out = torch.empty(no * (3 + nmom), dtype=torch.float32, device="cuda")
+        ch32 = np.array(CHANNELS, np.float32)
+        qt32, qb32 = np.asarray(qt, np.int32), np.asarray(qb, np.int32)
+        ms_aop = _time_flushed(torch, lambda: L.aerort_get_aop_vector_dev(
+            chem.handle, km, ncr, nch, nq, _lib.ptr(ch32, _lib.P_f), _lib.ptr(qt32, _lib.P_i),
+            _lib.ptr(qb32, _lib.P_i), P(dqm), P(drh), nmom, 1, P(out), P(out) + 4 * no, P(out) + 8 * no,
+            P(out) + 12 * no, stream))
+        del dqm, drh, out
+        alg = (km * nq + km) * 4 * ncr + no * (3 + nmom) * 4
+        ach = alg / (ms_aop * 1e-3) / 1e9
+        aop_line = {"kernel": "k_aop (VLIDORT_getAOPvector + Chem_MieQuery)", "bound": "hbm",
+                    "ms_per_launch": ms_aop, "algorithmic_bytes": alg, "achieved": ach, "peak": peak, "unit": "GB/s",
+                    "frac": ach / peak, "peak_source": src, "columns": ncr, "layers": km, "tracers": nq,
+                    "wavelengths": nch, "moments": nmom,
+                    "note": "L2 flushed (512 MB write) before each timed launch; Mie-table reads (L2-resident) "
+                            "not counted"}
+    return rot_line, edge_line, aop_line
 
 
 def main():
@@ -589,9 +619,9 @@ def main():
         assert np.isfinite(got)
 
     # ---------------------------------------------------------------- front end kernels (ROT, edge profiles)
-    rot_line = edge_line = None
+    rot_line = edge_line = aop_line = None
     if rank == 0:
-        rot_line, edge_line = front_end_rooflines(torch, L, batch, stream)
+        rot_line, edge_line, aop_line = front_end_rooflines(torch, L, batch, stream, chem=chem, qt=qt, qb=qb)
 
     # ---------------------------------------------------------------- serving
     serving = None
@@ -662,7 +692,7 @@ def main():
                 "path": "pinned host inputs -> device copies, aerort_get_aop_vector_dev + "
                         "aerort_vlidort_scalar_lambert_mixed_batch_dev per stream group (%s), device -> pinned host "
                         "outputs, host read" % ("one CUDA stream per group" if side else "one stream")},
-        "serving": serving, "gpu_launches": launches, "clocks": clk, "rot_calc": rot_line, "edge_vars": edge_line,
+        "serving": serving, "gpu_launches": launches, "clocks": clk, "rot_calc": rot_line, "edge_vars": edge_line, "aop": aop_line,
     }
     if rank == 0:
         print(json.dumps(line))
