@@ -151,6 +151,27 @@ def read_optics_file(path):
     return out
 
 
+def get_mie_dims(path):
+    """getMieDims / Chem_MieTableGetDims (MieObs_py.F90:7-23,
+    Chem_MieTableMod.F90:733-800): (nCh, nRh, nBin, nMom, nPol, rc) of one
+    optics file.  A file without an nMom dimension has nMom = nPol = 0, as in
+    the reference.  rc is nonzero, with zero sizes, when the file or one of
+    the lambda/rh/radius dimensions cannot be read (netCDF-4 files included)."""
+    from scipy.io import netcdf_file
+    try:
+        with open(path, "rb") as fh:
+            if fh.read(8) == _HDF5_MAGIC:
+                return 0, 0, 0, 0, 0, 1
+        with netcdf_file(path, "r", mmap=False) as nc:
+            d = nc.dimensions
+            nch, nrh, nbin = int(d["lambda"]), int(d["rh"]), int(d["radius"])
+            nmom = int(d["nMom"]) if "nMom" in d else 0
+            npol = int(d["nPol"]) if "nMom" in d and "nPol" in d else 0
+        return nch, nrh, nbin, nmom, npol, 0
+    except (OSError, KeyError, TypeError, ValueError):
+        return 0, 0, 0, 0, 0, 1
+
+
 def table_from_file_arrays(name, lam, rh, bext, bsca, g, pmom, channels_m, nmom):
     """Chem_MieTableRead's set-up of one table (Chem_MieTableMod.F90:557-601):
     the file arrays (wavelength first, REAL*8) interpolated to channels_m [m]

@@ -147,6 +147,21 @@ def test_one_wavelength_table_and_moment_checks():
                                      P(zf), P(zf), None, None) == 1002
 
 
+def test_get_mie_dims(tmp_path):
+    t = _raw_table(11, nlam=7, nrh=5, nbin=3, nmom=10, npol=4)
+    path = os.path.join(tmp_path, "optics_dims.nc")
+    _write_nc(path, t)
+    assert mie.get_mie_dims(path) == (7, 5, 3, 10, 4, 0)
+    # a table without phase moments: nMom = nPol = 0
+    from scipy.io import netcdf_file
+    path2 = os.path.join(tmp_path, "optics_nomom.nc")
+    with netcdf_file(path2, "w") as nc:
+        for d, n in (("lambda", 2), ("rh", 3), ("radius", 1)):
+            nc.createDimension(d, n)
+    assert mie.get_mie_dims(path2) == (2, 3, 1, 0, 0, 0)
+    assert mie.get_mie_dims(os.path.join(tmp_path, "missing.nc"))[-1] != 0
+
+
 def test_netcdf4_file_is_refused_with_a_message(tmp_path):
     path = os.path.join(tmp_path, "optics_h5.nc")
     with open(path, "wb") as fh:
