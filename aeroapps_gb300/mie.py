@@ -206,13 +206,17 @@ def table_from_file_arrays(name, lam, rh, bext, bsca, g, pmom, channels_m, nmom)
     return MieTable(name, orh, ob[0], ob[1], ob[2], opm), nout.value
 
 
-def read_tables(files, channels_nm, nmom):
+def read_tables(files, channels_nm, nmom, channels_m=None):
     """Chem_MieCreate's table reads (Chem_MieMod.F90:326-339): one optics file
     per species, {name: path} in table order, each interpolated to the
-    channels [nm].  Channels outside a table's wavelength range are allowed,
-    as in the reference, and reported through warnings.warn."""
+    channels [nm] (or to channels_m [m], REAL*4, when given).  Channels outside
+    a table's wavelength range are allowed, as in the reference, and reported
+    through warnings.warn."""
     import warnings
-    ch = (np.asarray(channels_nm, np.float64) * 1e-9).astype(np.float32)
+    if channels_m is not None:
+        ch = np.ascontiguousarray(channels_m, np.float32)
+    else:
+        ch = (np.asarray(channels_nm, np.float64) * 1e-9).astype(np.float32)
     tabs = []
     for name, path in files.items():
         a = read_optics_file(path)
@@ -222,6 +226,56 @@ def read_tables(files, channels_nm, nmom):
                           % (name, path, nout, a["lambda"][0], a["lambda"][-1]))
         tabs.append(t)
     return MieTableSet(ch, tabs)
+
+
+# species of a Mie resource file, in Chem_MieCreate's table-read order (Chem_MieMod.F90:326-339)
+RC_SPECIES = ("du", "ss", "su", "oc", "bc", "ni", "brc")
+
+
+def read_mie_rc(rcfile):
+    """The Mie resource file of Chem_MieCreateFromRC (Chem_MieMod.F90:124-300):
+    n_channels, optional n_moments (default 0), r_channels [m] and
+    filename_optical_properties_<DU|SS|BC|OC|SU|NI|BRC>.  Lines are
+    `label: values`; `#` starts a comment.  Returns {"nch", "nmom",
+    "channels_m" (REAL*4), "files": {species: path}}; relative table paths
+    are taken from the resource file's directory.  Raises ValueError where the
+    reference stops (missing or unparsable entries)."""
+    entries = {}
+    with open(rcfile) as f:
+        for line in f:
+            line = line.split("#", 1)[0].strip()
+            if ":" not in line:
+                continue
+            label, rest = line.split(":", 1)
+            entries[label.strip()] = rest.split()
+
+    def need(label):
+        if label not in entries or not entries[label]:
+            raise ValueError("%s: could not find %s" % (rcfile, label))
+        return entries[label]
+
+    try:
+        nch = int(need("n_channels")[0])
+        nmom = int(entries["n_moments"][0]) if entries.get("n_moments") else 0
+        chans = need("r_channels")
+        if len(chans) < nch:
+            raise ValueError("%s: r_channels has %d values, n_channels is %d" % (rcfile, len(chans), nch))
+        ch = np.array([float(x.replace("d", "e").replace("D", "e")) for x in chans[:nch]], np.float32)
+    except (ValueError, IndexError) as e:
+        raise ValueError("%s: could not parse channels or moments (%s)" % (rcfile, e))
+    base = os.path.dirname(os.path.abspath(rcfile))
+    files = {}
+    for sp in RC_SPECIES:
+        path = need("filename_optical_properties_%s" % sp.upper())[0]
+        files[sp] = path if os.path.isabs(path) else os.path.join(base, path)
+    return {"nch": nch, "nmom": nmom, "channels_m": ch, "files": files}
+
+
+def tables_from_rc(rcfile):
+    """Every table of a Mie resource file, read and interpolated to its
+    channels with its moment count (Chem_MieCreateFromRC + Chem_MieTableRead)."""
+    rc = read_mie_rc(rcfile)
+    return read_tables(rc["files"], None, rc["nmom"], channels_m=rc["channels_m"])
 
 
 def registry_map(groups, tables):
@@ -280,6 +334,11 @@ class ChemMie:
             raise RuntimeError("aerort_mie_create rc=%d: %s" % (rc, _lib.last_error()))
         self.handle = h
         self.channels = ch
+
+    @classmethod
+    def from_rc(cls, rcfile, registry=None):
+        """Chem_MieCreate(rcfile) (Chem_MieMod.F90:124-411) on the device."""
+        return cls(tables_from_rc(rcfile), registry=registry)
 
     def query_idx(self, vname):
         """Chem_MieQueryIdx (Chem_MieMod.F90:720-777): tracer name -> (table, bin) or (-1, -1).

@@ -162,6 +162,43 @@ def test_get_mie_dims(tmp_path):
     assert mie.get_mie_dims(os.path.join(tmp_path, "missing.nc"))[-1] != 0
 
 
+def _write_rc(tmp_path, nmom=12, channels="4.70e-7 5.50d-7 6.70E-07"):
+    for k, sp in enumerate(mie.RC_SPECIES):
+        _write_nc(os.path.join(tmp_path, "optics_%s.nc" % sp.upper()), _raw_table(200 + k, nbin=4, nmom=24, npol=1))
+    rc = os.path.join(tmp_path, "Aod_test.rc")
+    with open(rc, "w") as f:
+        f.write("# Mie resource file\n")
+        f.write("n_channels: 3\n")
+        f.write("n_moments: %d   # phase-function moments\n" % nmom)
+        f.write("r_channels: %s\n" % channels)
+        for sp in mie.RC_SPECIES:
+            f.write("filename_optical_properties_%s: optics_%s.nc\n" % (sp.upper(), sp.upper()))
+    return rc
+
+
+def test_mie_resource_file(tmp_path):
+    rc = _write_rc(tmp_path)
+    r = mie.read_mie_rc(rc)
+    assert r["nch"] == 3 and r["nmom"] == 12
+    assert np.array_equal(r["channels_m"], np.array([4.70e-7, 5.50e-7, 6.70e-7], np.float32))
+    assert r["files"]["brc"] == os.path.join(tmp_path, "optics_BRC.nc")
+    ts = mie.tables_from_rc(rc)
+    assert [t.name for t in ts.tables] == list(mie.RC_SPECIES)
+    ref = mie.read_tables(r["files"], None, 12, channels_m=r["channels_m"])
+    for a, b in zip(ts.tables, ref.tables):
+        assert np.array_equal(a.pmom, b.pmom) and a.pmom.shape == (6, 3, 4, 12, 1)
+    # without n_moments the tables carry no moments
+    with open(rc) as f:
+        text = f.read()
+    with open(rc, "w") as f:
+        f.write("\n".join(l for l in text.splitlines() if not l.startswith("n_moments")) + "\n")
+    assert mie.tables_from_rc(rc).tables[0].pmom.shape[3] == 0
+    with open(rc, "w") as f:
+        f.write("n_channels: 2\nr_channels: 5.5e-7\n")
+    with pytest.raises(ValueError):
+        mie.read_mie_rc(rc)
+
+
 def test_netcdf4_file_is_refused_with_a_message(tmp_path):
     path = os.path.join(tmp_path, "optics_h5.nc")
     with open(path, "wb") as fh:
@@ -211,6 +248,24 @@ def test_aop_from_netcdf_tables_bit_identical_to_oracle(tmp_path):
     qt, qb = zip(*[chem.query_idx(x) for x in names])
     chem.destroy()
     want = oracle.get_aop_vector(tables, km, n, len(ch), len(names), ch, qt, qb, cols["qm"], cols["rh"], 16, 1)
+    assert got[4] == 0 and want[4] == 0
+    for a, b in zip(got[:4], want[:4]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_chem_mie_from_resource_file(tmp_path):
+    rc = _write_rc(tmp_path, nmom=16)
+    chem = mie.ChemMie.from_rc(rc)
+    cols = synth.make_columns(24, [470.0, 550.0, 670.0], seed=78)
+    names = synth.tracer_names()
+    km, n = cols["km"], cols["ncol"]
+    ch = np.asarray([470.0, 550.0, 670.0], np.float32)
+    got = mie.get_aop_vector(chem, km, n, 3, len(names), ch, names, 0, cols["qm"], cols["rh"], 16, 1)
+    qt, qb = zip(*[chem.query_idx(x) for x in names])
+    tables = chem.tableset
+    chem.destroy()
+    want = oracle.get_aop_vector(tables, km, n, 3, len(names), ch, qt, qb, cols["qm"], cols["rh"], 16, 1)
     assert got[4] == 0 and want[4] == 0
     for a, b in zip(got[:4], want[:4]):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
