@@ -278,6 +278,56 @@ def tables_from_rc(rcfile):
     return read_tables(rc["files"], None, rc["nmom"], channels_m=rc["channels_m"])
 
 
+def read_chem_registry(path):
+    """The aerosol part of Chem_RegistryCreate (Chem_RegistryMod.F90:185-552)
+    as Chem_MieCreate uses it: for each of du, ss, su, bc, oc, brc, ni with
+    `doing_XX: y...` and `nbins_XX` >= 1, the tracer names in registry order.
+    Names come from the first nbins lines of a `variable_table_XX::` block
+    (first token of each line) when there is one, else <species><bin, 3
+    digits>.  Returns {species: [names]} for registry_map."""
+    lines = []
+    with open(path) as f:
+        for line in f:
+            lines.append(line.split("#", 1)[0].rstrip("\n"))
+
+    def value(label):
+        for ln in lines:
+            t = ln.strip()
+            if t.startswith(label):
+                rest = t[len(label):].split()
+                return rest[0] if rest else None
+        return None
+
+    groups = {}
+    for sp in ("du", "ss", "su", "bc", "oc", "brc", "ni"):
+        doing = value("doing_%s:" % sp.upper())
+        if not doing or doing[0] not in "yY":
+            continue
+        nb = value("nbins_%s:" % sp.upper())
+        if nb is None:
+            raise ValueError("%s: cannot determine NBINS for %s" % (path, sp.upper()))
+        nbins = int(nb)
+        if nbins < 1:
+            continue
+        names = None
+        token = "variable_table_%s::" % sp.upper()
+        for i, ln in enumerate(lines):
+            if ln.strip().startswith(token):
+                names = []
+                for row in lines[i + 1:]:
+                    tok = row.split()
+                    if not tok:
+                        continue
+                    if tok[0] == "::" or len(names) == nbins:
+                        break
+                    names.append(tok[0])
+                if len(names) < nbins:
+                    raise ValueError("%s: not enough names in %s" % (path, token))
+                break
+        groups[sp] = names if names is not None else ["%s%03d" % (sp, b + 1) for b in range(nbins)]
+    return groups
+
+
 def registry_map(groups, tables):
     """The tracer -> (table, bin) hash of Chem_MieCreate (Chem_MieMod.F90:345-399).
 

@@ -199,6 +199,43 @@ def test_mie_resource_file(tmp_path):
         mie.read_mie_rc(rc)
 
 
+def test_chem_registry_names(tmp_path):
+    path = os.path.join(tmp_path, "Chem_MieRegistry.rc")
+    with open(path, "w") as f:
+        f.write("""doing_DU:  yes  # dust
+doing_SS:  no
+doing_SU:  Yes
+doing_BC:  yes
+doing_NI:  yes
+nbins_DU:   3
+nbins_SS:   5
+nbins_SU:   4
+nbins_BC:   2
+nbins_NI:   3
+variable_table_SU::
+DMS        kg/kg    Dimethylsulphide
+SO2        kg/kg    Sulphur dioxide
+SO4        kg/kg    Sulphate aerosol
+MSA        kg/kg    Methanesulphonic acid
+::
+variable_table_BC::
+BCphobic   kg/kg    Hydrophobic Black Carbon
+BCphilic   kg/kg    Hydrophilic Black Carbon
+::
+variable_table_NI::
+NH3        kg/kg    Ammonia
+NO3an1     kg/kg    Nitrate size bin 001
+NO3an2     kg/kg    Nitrate size bin 002
+::
+""")
+    groups = mie.read_chem_registry(path)
+    assert groups == {"du": ["du001", "du002", "du003"], "su": ["DMS", "SO2", "SO4", "MSA"],
+                      "bc": ["BCphobic", "BCphilic"], "ni": ["NH3", "NO3an1", "NO3an2"]}
+    reg = mie.registry_map(groups, list(mie.RC_SPECIES))
+    assert reg["DU003"] == (0, 2) and reg["SO4"] == (2, 0) and reg["BCPHILIC"] == (4, 1)
+    assert reg["NO3AN2"] == (5, 1) and "NH3" not in reg and "DMS" not in reg
+
+
 def test_netcdf4_file_is_refused_with_a_message(tmp_path):
     path = os.path.join(tmp_path, "optics_h5.nc")
     with open(path, "wb") as fh:
