@@ -6,6 +6,8 @@ import pytest
 from aeroapps_gb300 import mie, pipeline, synth
 from oracle import oracle
 
+MISSING = -1.0e15
+
 
 @pytest.mark.gpu
 def test_config0_slice_matches_oracle():
@@ -27,3 +29,44 @@ def test_config0_slice_matches_oracle():
     assert np.array_equal(nf, onf) and np.array_equal(st, ost)
     assert np.max(np.abs(rad / orad - 1)) < 1e-9
     assert np.max(np.abs(refl / orefl - 1)) < 1e-9
+
+
+def _model_fields(ncol, seed):
+    """Layer fields of the kind geo_vlidort reads (AIRDENS, DELP, RH, tracer
+    mixing ratios) for synthetic 72-layer columns, and their qm."""
+    c = synth.make_columns(ncol, [470.0, 550.0, 670.0], seed=seed)
+    pm = 0.5 * (c["pe"][1:] + c["pe"][:-1])
+    tm = 0.5 * (c["te"][1:] + c["te"][:-1])
+    airdens = np.asfortranarray(pm / (synth.RGAS * tm), np.float32)
+    delp = np.asfortranarray(np.diff(c["pe"], axis=0), np.float32)
+    return c, airdens, delp
+
+
+@pytest.mark.gpu
+def test_geo_chunk_matches_oracle_chain():
+    # the whole per-pixel chain from model fields, against the oracle running
+    # the same chain; te may differ by a few ulp (logf/powf), which moves ROT
+    # and the radiance by a few 1e-7 at most, hence the 1e-6 bar here
+    tabs = mie.generate_tables([470.0, 550.0, 670.0], nmom=32)
+    chem = mie.ChemMie(tabs)
+    c, airdens, delp = _model_fields(12, seed=33)
+    names = synth.tracer_names()
+    ch = np.array([470.0, 550.0, 670.0])
+    rad, refl, rc, prof = pipeline.geo_chunk(chem, ch, 8, airdens, delp, 1.0, c["qm"], c["rh"], names, c["albedo"],
+                                             c["sza"], c["raa"], c["vza"])
+    qt, qb = zip(*[chem.query_idx(x) for x in names])
+    chem.destroy()
+    assert rc == 0
+    pe, ze, te = oracle.get_edge_vars(airdens, delp, 1.0)
+    assert np.array_equal(prof["pe"], pe) and np.array_equal(prof["ze"], ze)
+    f64 = lambda a: np.asfortranarray(a, np.float64)
+    rot, depol, _ = oracle.rot_calc(ch, f64(pe), f64(ze), f64(te))
+    tau, ssa, g, pmom, orc = oracle.get_aop_vector(tabs, c["km"], 12, 3, len(names), ch.astype(np.float32), qt, qb,
+                                                   c["qm"], c["rh"], 16, 1)
+    assert orc == 0 and np.array_equal(prof["tau"], tau)
+    orad, orefl, orc2, _, _ = oracle.scalar_lambert(c["km"], 3, 12, ch, 8, 0, 16, 1, rot, depol, f64(tau), f64(ssa),
+                                                    f64(g), f64(pmom), f64(pe), f64(ze), f64(te), c["albedo"],
+                                                    c["sza"], c["raa"], c["vza"], MISSING)
+    ok = orad != MISSING
+    assert ok.all()
+    assert np.max(np.abs(rad / orad - 1.0)) <= 1e-6
