@@ -237,9 +237,11 @@ def read_mie_rc(rcfile):
     n_channels, optional n_moments (default 0), r_channels [m] and
     filename_optical_properties_<DU|SS|BC|OC|SU|NI|BRC>.  Lines are
     `label: values`; `#` starts a comment.  Returns {"nch", "nmom",
-    "channels_m" (REAL*4), "files": {species: path}}; relative table paths
-    are taken from the resource file's directory.  Raises ValueError where the
-    reference stops (missing or unparsable entries)."""
+    "channels_m" (REAL*4), "files": {species: path}}.  A relative table
+    path is opened from the working directory, as nf_open does in the
+    reference; when no such file is there, from the resource file's
+    directory.  Raises ValueError where the reference stops (missing or
+    unparsable entries)."""
     entries = {}
     with open(rcfile) as f:
         for line in f:
@@ -267,7 +269,9 @@ def read_mie_rc(rcfile):
     files = {}
     for sp in RC_SPECIES:
         path = need("filename_optical_properties_%s" % sp.upper())[0]
-        files[sp] = path if os.path.isabs(path) else os.path.join(base, path)
+        if not os.path.isabs(path):
+            path = os.path.abspath(path) if os.path.exists(path) else os.path.join(base, path)
+        files[sp] = path
     return {"nch": nch, "nmom": nmom, "channels_m": ch, "files": files}
 
 

@@ -181,7 +181,18 @@ def test_mie_resource_file(tmp_path):
     r = mie.read_mie_rc(rc)
     assert r["nch"] == 3 and r["nmom"] == 12
     assert np.array_equal(r["channels_m"], np.array([4.70e-7, 5.50e-7, 6.70e-7], np.float32))
-    assert r["files"]["brc"] == os.path.join(tmp_path, "optics_BRC.nc")
+    assert r["files"]["brc"] == os.path.join(tmp_path, "optics_BRC.nc")  # not in the working directory
+    # a table path that exists relative to the working directory is taken from there
+    sub = os.path.join(tmp_path, "run")
+    os.makedirs(sub)
+    cwd = os.getcwd()
+    try:
+        os.chdir(sub)
+        with open("optics_DU.nc", "w") as f:
+            f.write("")
+        assert mie.read_mie_rc(rc)["files"]["du"] == os.path.join(sub, "optics_DU.nc")
+    finally:
+        os.chdir(cwd)
     ts = mie.tables_from_rc(rc)
     assert [t.name for t in ts.tables] == list(mie.RC_SPECIES)
     ref = mie.read_tables(r["files"], None, 12, channels_m=r["channels_m"])
