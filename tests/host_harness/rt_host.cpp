@@ -28,12 +28,14 @@ static int run(const RtOptions& opt, const LambertInputs& in, double* rad, doubl
   for (int s = 0; s < in.nobs * in.nch; ++s) solve_lambert<NS, T>(opt, in, s, qx, qw, tu, wu, S, rad, refl, nf, st);
   return 0;
 }
+static int g_plane_parallel = 0;  // VLIDORT_Scalar_Lambert's plane_parallel flag for the next calls
+extern "C" void host_set_plane_parallel(int on) { g_plane_parallel = on ? 1 : 0; }
 template <typename T>
 static int dispatch(int km, int nch, int nobs, int nstreams, int nmom, const double* rot, const double* depol,
     const double* tau, const double* ssa, const double* pmom, const double* he, const double* albedo, const double* sza,
     const double* raa, const double* vza, const int* nadir, double missing, int max_fourier,
     double* rad, double* refl, int* nf, int* st) {
-  RtOptions opt{1, 1, 0, 1, 3, 3, kAccuracySingle, 6371.0, 1.0, max_fourier};
+  RtOptions opt{1, 1, g_plane_parallel, 1, 3, 3, kAccuracySingle, 6371.0, 1.0, max_fourier};
   LambertInputs in{km, nch, nobs, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nullptr, nullptr, nullptr, nullptr, nadir, missing};
   switch (nstreams) {
     case 4: return run<4, T>(opt, in, rad, refl, nf, st);

@@ -100,3 +100,28 @@ def test_more_input_moments_than_streams(host_lib):
     for fn, tol in (("host_scalar_lambert", 1e-9), ("host_scalar_lambert_mixed", 1e-4)):
         rad, nf, st = _host(host_lib, c, 6, fn)
         assert np.all(st == 0) and np.max(np.abs(rad / orad - 1)) < tol
+
+
+@pytest.mark.parametrize("nstreams,km", [(8, 30), (4, 12), (16, 8)])
+def test_plane_parallel_flag(host_lib, team_lib, nstreams, km):
+    # VLIDORT_Scalar_Lambert's plane_parallel = .true.: plane-parallel beam
+    # attenuation and single-scatter geometry instead of the pseudo-spherical ones
+    c = random_aop_case(nstreams, km, nobs=4, nch=1, seed=5 * km + nstreams)
+    args = list(rt_args(c, nstreams))
+    args[5] = True
+    orad, orefl, orc, onf, ost = oracle.scalar_lambert(*args, MISSING)
+    sph = oracle.scalar_lambert(*rt_args(c, nstreams), MISSING)[0]
+    assert orc == 0 and np.max(np.abs(orad / sph - 1)) > 1e-5  # the flag changes the answer
+    host_lib.host_set_plane_parallel(1)
+    team_lib.team_set_plane_parallel(1)
+    try:
+        rad, nf, st = _host(host_lib, c, nstreams)
+        mrad, _, mst = _host(host_lib, c, nstreams, "host_scalar_lambert_mixed")
+        trad, tnf, tst = _host(team_lib, c, nstreams, "team_scalar_lambert")
+    finally:
+        host_lib.host_set_plane_parallel(0)
+        team_lib.team_set_plane_parallel(0)
+    assert np.array_equal(nf, onf) and np.all(st == 0) and np.all(mst == 0)
+    assert np.max(np.abs(rad / orad - 1)) < 1e-9
+    assert np.max(np.abs(mrad / orad - 1)) < 1e-4
+    assert np.array_equal(tnf, nf) and np.all(tst == 0) and np.max(np.abs(trad / rad - 1)) < 1e-12

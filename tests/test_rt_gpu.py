@@ -102,3 +102,20 @@ def test_repeat_calls_are_bitwise_deterministic():
     a = vlidort.vlidort_scalar_lambert(*rt_args(c, 8), MISSING=MISSING)[0]
     b = vlidort.vlidort_scalar_lambert(*rt_args(c, 8), MISSING=MISSING)[0]
     assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nstreams,km", [(8, 48), (16, 20)])
+def test_plane_parallel_flag(nstreams, km):
+    # plane_parallel = .true. (VLIDORT_LAMBERT.F90 argument): plane-parallel beam
+    # attenuation and single-scatter geometry; same bars as the default mode
+    c = random_aop_case(nstreams, km, nobs=16, nch=2, seed=nstreams + 3 * km)
+    args = list(rt_args(c, nstreams))
+    args[5] = True
+    rad, refl, rc, nf, st = vlidort.vlidort_scalar_lambert(*args, MISSING=MISSING, diagnostics=True)
+    orad, orefl, orc, onf, ost = oracle.scalar_lambert(*args, MISSING)
+    assert rc == 0 and orc == 0
+    assert np.array_equal(st, ost) and np.array_equal(nf, onf)
+    ok = orad != MISSING
+    assert np.max(np.abs(rad[ok] / orad[ok] - 1.0)) <= 1e-8
+    assert np.max(np.abs(refl[ok] / orefl[ok] - 1.0)) <= 1e-8
