@@ -317,3 +317,19 @@ def test_chem_mie_from_resource_file(tmp_path):
     assert got[4] == 0 and want[4] == 0
     for a, b in zip(got[:4], want[:4]):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_unsorted_wavelength_grid_follows_polint():
+    # polint assumes ascending wavelengths; on any other grid its segment search
+    # (the last node at or below the channel) and end rules still decide the
+    # result, and the library must follow them exactly
+    t = _raw_table(21, nlam=6)
+    perm = [0, 2, 1, 3, 5, 4]
+    for k in ("bext", "bsca", "g", "pmom"):
+        t[k] = np.ascontiguousarray(t[k][perm])
+    t["lam"] = t["lam"][perm]
+    ch = (np.array([260.0, 320.0, 390.0, 460.0, 500.0, 240.0]) * 1e-9).astype(np.float32)
+    tab, _ = mie.table_from_file_arrays("xx", t["lam"], t["rh"], t["bext"], t["bsca"], t["g"], t["pmom"], ch, 9)
+    want = oracle.mie_table_interp(t["lam"], t["rh"], t["bext"], t["bsca"], t["g"], t["pmom"], ch, 9)
+    for got, w in zip((tab.bext, tab.bsca, tab.g, tab.pmom), want[1:5]):
+        assert np.array_equal(got.view(np.uint32), w.view(np.uint32))
