@@ -551,8 +551,17 @@ int dispatch_lambert(Context& c, int precision, int nstreams, const RtOptions& o
   return rc ? rc : rc2;
 }
 
+// Largest nobs * nch of one RT call.  The persistent kernels hand out solves
+// with an int work counter that every resident warp bumps (by up to 32) once
+// more after the queue runs dry; the 16 Mi of headroom below INT_MAX covers
+// 32 x (resident warps + 1) on any GPU with fewer than 512 Ki resident warps
+// (GB300: 152 SMs x 64 warps), so the counter never wraps.
+constexpr long long kMaxSolves = 0x7f000000LL;
+
 int lambert_checks(int km, int nch, int nobs, int nstreams, int nMom) {
   if (km <= 0 || nch <= 0 || nobs < 0) return set_error(AERORT_RC_ARG, "scalar_lambert: bad sizes");
+  if ((long long)nobs * nch > kMaxSolves)
+    return set_error(AERORT_RC_ARG, "scalar_lambert: nobs * nch too large (at most 2130706432 solves per call)");
   if (nstreams > 25) return set_error(AERORT_RC_NSTREAMS, "NSTREAMS > MAXSTREAMS");
   if (km > kMaxLayers) return set_error(AERORT_RC_NLAYERS, "NLAYERS > MAXLAYERS");
   if (nMom > 1000) return set_error(AERORT_RC_NMOMENTS, "nmom > MAXMOMENTS_INPUT");
@@ -784,7 +793,6 @@ extern "C" int aerort_vlidort_scalar_lambert_ws_dev(
   if (int rc = lambert_checks(km, nch, nobs, nstreams, nMom)) return rc;
   if ((!tau_f && (!tau || !ssa || !pmom)) || (tau_f && (!ssa_f || !pmom_f)))
     return set_error(AERORT_RC_ARG, "scalar_lambert_ws_dev: optics missing");
-  if ((long)nobs * nch > 0x7fffff00L) return set_error(AERORT_RC_ARG, "scalar_lambert_ws_dev: nobs * nch too large");
   Schedule sc, sc64;
   {
     Context& c = ctx();
@@ -810,7 +818,6 @@ extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
   if (int rc = lambert_checks(km, nch, nobs, nstreams, nMom)) return rc;
   if ((!tau_f && (!tau || !ssa || !pmom)) || (tau_f && (!ssa_f || !pmom_f)))
     return set_error(AERORT_RC_ARG, "scalar_lambert_noalloc: optics missing");
-  if ((long)nobs * nch > 0x7fffff00L) return set_error(AERORT_RC_ARG, "scalar_lambert_noalloc: nobs * nch too large");
   double* arena = nullptr;
   size_t arena_doubles = 0;
   int* sched = nullptr;
@@ -818,7 +825,8 @@ extern "C" int aerort_vlidort_scalar_lambert_batch_dev_noalloc(
   if (int rc = static_arena(&arena, &arena_doubles, &sched, &num_sms)) return rc;
   LambertInputs in{km, nch, nobs, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth,
                    sensor_zenith, nlay, tau_f, ssa_f, pmom_f, nullptr, MISSING};
-  Schedule sc;  // the library's kernel choice for this stream count; 64 threads per block, occupancy-limited
+  Schedule sc;  // the library's kernel choice for this stream count; 32-thread blocks (thread kernel) or
+                // two-warp blocks (team kernel), occupancy-limited
   {
     Context& c = ctx();
     std::lock_guard<std::mutex> lk(c.mu);
@@ -970,6 +978,7 @@ extern "C" int aerort_release(void) {
   Context& c = ctx();
   std::lock_guard<std::mutex> lk(c.mu);
   c.release();
+  static_arena_forget();
   return AERORT_OK;
 }
 

@@ -78,7 +78,7 @@ struct Pad {
 // handed from one stream to another makes the new stream wait, on the device,
 // for the work last enqueued on it.
 struct Context {
-  static constexpr int kPads = 8;
+  static constexpr int kPads = 16;
   std::mutex mu;
   bool init = false;
   int device = -1, num_sms = 0;
@@ -120,5 +120,6 @@ int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::Lamb
 // Static device arena of the allocation-free entry point (rt_static.cu):
 // address of the calling thread's current device's copy, set up on first use.
 int static_arena(double** arena, size_t* arena_doubles, int** sched, int* num_sms);
+void static_arena_forget();
 
 }  // namespace aerort_internal

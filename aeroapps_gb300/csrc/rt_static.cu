@@ -7,16 +7,20 @@
 // unrelated work.  For them the RT scratch lives in a file-scope array that
 // the CUDA module reserves when it is loaded, so a call only launches kernels.
 //
-// The arena is in its own translation unit, hence its own CUDA module, so a
-// process that never uses this entry point does not reserve it.
+// The arena is in its own translation unit, hence its own CUDA module.  Under
+// lazy module loading (the CUDA default) a process that never calls this entry
+// point does not reserve it; with CUDA_MODULE_LOADING=EAGER every process that
+// loads the library reserves the 256 MiB on each device it initialises.
 #include "aerort_internal.cuh"
 
 namespace aerort_internal {
 
-// 256 MiB of FP64 scratch.  One 64-thread block of the RT kernel needs
-// 64 x ScratchLayout(km).total doubles (about 22 MiB at 16 streams and 72
-// layers), so every supported (nstreams, km) fits; the grid is capped to what
-// the arena holds, which bounds throughput at large stream counts.
+// 256 MiB of FP64 scratch.  One 32-thread block of the thread-per-solve RT
+// kernel needs 32 x ScratchLayout(km).total doubles (about 11 MiB at 16
+// streams and 72 layers), one two-warp block of the team kernel 64 set-up
+// scratches plus two sweep regions, so every supported (nstreams, km) fits;
+// the grid is capped to what the arena holds, which bounds throughput at
+// large stream counts.
 constexpr size_t kArenaDoubles = (size_t)32 << 20;
 static __device__ __align__(256) double g_rt_arena[kArenaDoubles];
 // Work counter and sticky-nadir index; reset on the stream by every call.
@@ -60,6 +64,13 @@ int static_arena(double** arena, size_t* arena_doubles, int** sched, int* num_sm
   *sched = slot.sched;
   *num_sms = slot.num_sms;
   return 0;
+}
+
+// Forget the cached symbol addresses (aerort_release): after a device reset
+// the module is loaded again, possibly at another address.
+void static_arena_forget() {
+  std::lock_guard<std::mutex> lk(g_arena_mu);
+  for (auto& slot : g_arena) slot = ArenaSlot();
 }
 
 }  // namespace aerort_internal

@@ -2,7 +2,7 @@
 benchmark configurations (the reference runs on GEOS model fields, which are
 not available here).
 
-Per column: a 72-level hybrid sigma-pressure grid (top 1 Pa), a standard-
+Per column: the GEOS-5 72-level hybrid sigma-pressure grid (top 1 Pa), a standard-
 atmosphere temperature profile, edge heights from hydrostatic balance (as
 getEdgeVars, src/Shared/GMAO_Shared/Chem_Base/MieObs_py.F90:27-83), uniform
 relative humidity, lognormal aerosol mass mixing ratios for 5 species x 4 bins
@@ -19,23 +19,33 @@ NLEV72 = 72
 NTRACER = 20
 
 
-def hybrid_coefficients(nlev=NLEV72, ptop=PTOP, ps_ref=101325.0):
-    """(A, B) of a hybrid sigma-pressure grid: pe = A + B * ps, index 0 = top.
+# GEOS-5 72-level hybrid sigma-pressure coefficients, edge 1 = model top:
+# pe_k = A72_k + B72_k * ps, A72 in Pa (A72_1 = ptop = 1 Pa), B72 dimensionless
+# (GMAO_hermes/m_set_eta.F90:512-549, the default 72-level branch).  A model
+# grid is a data table, reproduced exactly so that the layer thicknesses, and
+# with them the Rayleigh and aerosol loads, are the model's.
+A72 = np.array([
+    1.0000000, 2.0000002, 3.2700005, 4.7585009, 6.6000011, 8.9345014, 11.970302, 15.949503, 21.134903,
+    27.852606, 36.504108, 47.580610, 61.677911, 79.513413, 101.94402, 130.05102, 165.07903, 208.49704,
+    262.02105, 327.64307, 407.65710, 504.68010, 621.68012, 761.98417, 929.29420, 1127.6902, 1364.3402,
+    1645.7103, 1979.1604, 2373.0405, 2836.7806, 3381.0007, 4017.5409, 4764.3911, 5638.7912, 6660.3412,
+    7851.2316, 9236.5722, 10866.302, 12783.703, 15039.303, 17693.003, 20119.201, 21686.501, 22436.301,
+    22389.800, 21877.598, 21214.998, 20325.898, 19309.696, 18161.897, 16960.896, 15625.996, 14290.995,
+    12869.594, 11895.862, 10918.171, 9936.5219, 8909.9925, 7883.4220, 7062.1982, 6436.2637, 5805.3211,
+    5169.6110, 4533.9010, 3898.2009, 3257.0809, 2609.2006, 1961.3106, 1313.4804, 659.37527, 4.8048257,
+    0.0000000])
+B72 = np.array([0.0] * 41 + [
+    8.1754130e-09, 0.0069600246, 0.028010041, 0.063720063, 0.11360208, 0.15622409, 0.20035011, 0.24674112,
+    0.29440312, 0.34338113, 0.39289115, 0.44374018, 0.49459020, 0.54630418, 0.58104151, 0.61581843,
+    0.65063492, 0.68589990, 0.72116594, 0.74937819, 0.77063753, 0.79194696, 0.81330397, 0.83466097,
+    0.85601798, 0.87742898, 0.89890800, 0.92038701, 0.94186501, 0.96340602, 0.98495195, 1.0000000])
 
-    Upper levels are log-spaced in pressure, the lowest ~25 levels thin out
-    towards the surface; B rises smoothly from 0 above 10 kPa to 1 at the
-    surface.  Own construction with the GEOS-5 72-level character.
-    """
-    k = np.arange(nlev + 1, dtype=np.float64)
-    n_up = 46
-    p_up = ptop * (20000.0 / ptop) ** (k[: n_up + 1] / n_up)
-    v = (k[n_up:] - n_up) / (nlev - n_up)
-    p_lo = 20000.0 + (ps_ref - 20000.0) * (1.0 - (1.0 - v) ** 1.6)
-    p = np.concatenate([p_up, p_lo[1:]])
-    pt = 10000.0
-    B = np.where(p > pt, ((p - pt) / (ps_ref - pt)) ** 2, 0.0)
-    A = p - B * ps_ref
-    return A, B
+
+def hybrid_coefficients(nlev=NLEV72):
+    """(A, B) of the GEOS-5 72-level grid: pe = A + B * ps [Pa], index 0 = top."""
+    if nlev != NLEV72:
+        raise ValueError("only the 72-level GEOS-5 grid is tabulated")
+    return A72.copy(), B72.copy()
 
 
 def coef_depol(lam_um):

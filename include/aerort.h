@@ -126,7 +126,8 @@ int aerort_get_aop_scalar_dev(aerort_mie* mie, int km, int nobs, int nch, int nq
  * solar_zenith/relat_azymuth/sensor_zenith(nobs) [deg], radiance_VL/reflectance_VL(nobs,nch).
  * Pixels whose angles or albedo are MISSING (|x/MISSING-1| < 1e-3), or whose
  * solve fails, get MISSING, as in the reference.  FP64.  nstreams must be one
- * of 4, 6, 8, 12, 16 (the compiled stream counts). */
+ * of 4, 6, 8, 12, 16 (the compiled stream counts).  Every RT entry point
+ * rejects nobs * nch above 2,130,706,432 solves with AERORT_RC_ARG. */
 int aerort_vlidort_scalar_lambert(int km, int nch, int nobs, const double* channels, int nstreams,
                                   int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
                                   const double* tau, const double* ssa, const double* g, const double* pmom,
@@ -165,7 +166,7 @@ int aerort_vlidort_scalar_lambert_dev(int km, int nch, int nobs, int nstreams, i
  * (dble(), geo_vlidort.F90:598-601) happens on load.  No counterpart routine in
  * the reference: it batches many VLIDORT_Scalar_Lambert calls into one launch.
  * Calls on different streams use different library scratch (one pad per
- * stream, up to 8 streams at once), so groups of different stream counts may
+ * stream, up to 16 streams at once), so groups of different stream counts may
  * be enqueued on separate streams and run concurrently. */
 int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
                                             const int* nlay, const double* ROT, const double* depol,
@@ -236,7 +237,7 @@ int aerort_vlidort_rot_calc_dev(int km, int nch, int nobs, const double* channel
  * device memory once; launches through aerort_vlidort_scalar_lambert_ws_dev
  * then allocate nothing, and launches on different workspaces may overlap on
  * different streams (the batched entry points above keep one library
- * scratch pad per stream, for up to 8 streams at once, and allocate it on
+ * scratch pad per stream, for up to 16 streams at once, and allocate it on
  * first use).  The grid is capped to the threads whose
  * scratch fits: bytes_per_thread(km, nstreams, precision) x threads; one
  * block (32-128 threads) must fit.  The precision argument selects
@@ -294,9 +295,17 @@ int aerort_get_kernel(int nstreams, int precision);
  * ints) reserved when the library's CUDA module for it is loaded.  The first
  * call on a device, made with that device current, does the set-up (symbol
  * lookup, which may load that module); make it before any stream capture.
- * Limits: the kernel's resident threads are capped so their scratch fits the
- * arena (throughput drops at 12-16 streams); nobs * nch must stay below 2^31
- * - 256; a configuration whose 64-thread block would not fit is rejected with
+ * The arena is reserved on every device where that module is loaded: with
+ * lazy module loading (the CUDA default) only when a process first calls this
+ * entry point, with CUDA_MODULE_LOADING=EAGER by every process that loads the
+ * library.  After cudaDeviceReset (or any teardown of the primary context)
+ * call aerort_release before the next call, so that the arena address is
+ * looked up again.
+ * Limits: the kernel's resident blocks are capped so their scratch fits the
+ * arena (throughput drops at 12-16 streams); nobs * nch is at most
+ * 2,130,706,432 (as for every RT entry point); a configuration of which not
+ * even one block fits (32 threads for the thread-per-solve kernel, two warps
+ * with their 64 set-up scratches for the team kernel) is rejected with
  * AERORT_RC_ARG.  Nothing needs zeroing beforehand: the work counter is reset
  * on the stream by each call and every output element is written.  Calls
  * share the arena: two calls that may overlap (different streams, or threads

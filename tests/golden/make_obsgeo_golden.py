@@ -1,7 +1,7 @@
 """Build tests/golden/obsgeo_lpcs.json from the reference's own VLIDORT test data.
 
-Run in a checkout that has the reference tree (default: /root/reference, or the
-path given as argv[1]).  It reads
+Run with the path of an AeroApps checkout as the only argument
+(`python make_obsgeo_golden.py <aeroapps-tree>`).  It reads
 
   src/Components/rtms/RTSI/VLIDORT2p8p3/vlidort_v_test/input_atmos.dat
   src/Components/rtms/RTSI/VLIDORT2p8p3/vlidort_v_test/ProblemIII.Moms
@@ -28,7 +28,9 @@ import json
 import os
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python %s <path of an AeroApps checkout>" % os.path.basename(__file__))
+REF = sys.argv[1]
 BASE = os.path.join(REF, "src/Components/rtms/RTSI/VLIDORT2p8p3/vlidort_v_test")
 
 

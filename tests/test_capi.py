@@ -41,3 +41,23 @@ def test_argument_checks_return_reference_rc_codes():
     assert rc == 2  # NSTREAMS > MAXSTREAMS
     rc = L.aerort_vlidort_scalar_lambert(72, 1, 1, null, 8, 0, 2000, 1, *([null] * 13), -1e15, 0, null, null)
     assert rc == 5  # nmom > MAXMOMENTS_INPUT
+
+
+def test_solve_count_beyond_work_counter_range_is_rejected_on_the_host():
+    # nobs * nch past the int work counter's headroom (2^30 x 4 would also wrap
+    # the 32-bit product to 0): every RT entry point returns AERORT_RC_ARG
+    # before any CUDA call (the dummy addresses are never dereferenced)
+    L = _lib.lib()
+    fake = ctypes.c_void_p(256)
+    for nobs, nch in ((1 << 30, 4), (0x7f000000 // 2 + 1, 2)):
+        rc = L.aerort_vlidort_scalar_lambert_batch_dev(72, nch, nobs, 8, 0, 16, None, fake, fake, fake, fake, fake,
+                                                       None, None, None, fake, fake, fake, fake, fake, -1e15, fake,
+                                                       fake, None, None, None)
+        assert rc == 1002 and "too large" in _lib.last_error()
+        rc = L.aerort_vlidort_scalar_lambert_mixed_batch_dev(72, nch, nobs, 8, 0, 16, None, fake, fake, fake, fake,
+                                                             fake, None, None, None, fake, fake, fake, fake, fake,
+                                                             -1e15, fake, fake, None, None, None)
+        assert rc == 1002 and "too large" in _lib.last_error()
+    # the largest accepted count still passes the check (then fails on the null outputs, not the size)
+    rc = L.aerort_vlidort_scalar_lambert(72, 1, 1, None, 8, 0, 16, 1, *([None] * 13), -1e15, 0, None, None)
+    assert rc == 1002 and "too large" not in _lib.last_error()

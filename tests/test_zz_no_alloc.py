@@ -27,33 +27,47 @@ def test_rejects_oversized_batch_before_touching_the_device():
     assert "too large" in _lib.last_error()
 
 
-def _device_case(c, nl):
+def _device_case(c, nl, fp32_optics):
     import torch
     d = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dt).ravel(order="F"))).cuda()
-    keys = ("ROT", "depol", "tau", "ssa", "pmom", "he", "albedo", "sza", "raa", "vza")
+    keys = ("ROT", "depol", "he", "albedo", "sza", "raa", "vza")
     arrs = {k: d(c[k], np.float64) for k in keys}
+    opt = np.float32 if fp32_optics else np.float64
+    arrs["tau"], arrs["ssa"] = d(c["tau"], opt), d(c["ssa"], opt)
+    arrs["pmom"] = d(c["pmom"][..., 0], opt)
     arrs["nlay"] = d(nl, np.int32)
+    arrs["fp32"] = fp32_optics
     return arrs
 
 
-def _run(fn, c, N, a, out, stream):
+def _run(fn, c, N, a, out, stream, plane_parallel):
     km, nch, nobs = c["km"], c["nch"], c["ncol"]
     rad, refl, nf, st = out
-    rc = fn(km, nch, nobs, N, 0, c["nmom"], a["nlay"].data_ptr(), a["ROT"].data_ptr(), a["depol"].data_ptr(),
-            a["tau"].data_ptr(), a["ssa"].data_ptr(), a["pmom"].data_ptr(), None, None, None, a["he"].data_ptr(),
-            a["albedo"].data_ptr(), a["sza"].data_ptr(), a["raa"].data_ptr(), a["vza"].data_ptr(), MISSING,
-            rad.data_ptr(), refl.data_ptr(), nf.data_ptr(), st.data_ptr(), stream)
+    opt = [a["tau"].data_ptr(), a["ssa"].data_ptr(), a["pmom"].data_ptr()]
+    f64, f32 = (None, None, None), tuple(opt)
+    if not a["fp32"]:
+        f64, f32 = tuple(opt), (None, None, None)
+    rc = fn(km, nch, nobs, N, plane_parallel, c["nmom"], a["nlay"].data_ptr(), a["ROT"].data_ptr(),
+            a["depol"].data_ptr(), *f64, *f32, a["he"].data_ptr(), a["albedo"].data_ptr(), a["sza"].data_ptr(),
+            a["raa"].data_ptr(), a["vza"].data_ptr(), MISSING, rad.data_ptr(), refl.data_ptr(), nf.data_ptr(),
+            st.data_ptr(), stream)
     assert rc == 0, _lib.last_error()
 
 
+# (8, 72, 700): two-pass team solve (the arena holds the slice); (16, 72, 300):
+# FP64 team scratch at 16 streams is too large for a two-solve-per-warp slice,
+# so the fused team kernel runs on a grid capped to the arena; (4, 30, 64):
+# thread-per-solve kernel; (8, 40, 500) with FP32 optics straight from the AOP
+# kernel and plane_parallel = 1
 @pytest.mark.gpu
-@pytest.mark.parametrize("N,km,nobs", [(8, 72, 700), (16, 72, 300), (4, 30, 64)])
-def test_noalloc_matches_allocating_entry_point(N, km, nobs):
+@pytest.mark.parametrize("N,km,nobs,fp32_optics,pp", [(8, 72, 700, False, 0), (16, 72, 300, False, 0),
+                                                      (4, 30, 64, False, 0), (8, 40, 500, True, 1)])
+def test_noalloc_matches_allocating_entry_point(N, km, nobs, fp32_optics, pp):
     import torch
     c = random_aop_case(N, km, nobs=nobs, nch=2, seed=4000 + N)
     nl = np.random.default_rng(N).integers(1, km + 1, nobs)
     nl[0] = km
-    a = _device_case(c, nl)
+    a = _device_case(c, nl, fp32_optics)
     L = _lib.lib()
     stream = torch.cuda.current_stream().cuda_stream
     n = nobs * c["nch"]
@@ -65,11 +79,11 @@ def test_noalloc_matches_allocating_entry_point(N, km, nobs):
                 torch.full((n,), -7, dtype=torch.int32, device="cuda"))
 
     ref = outputs()
-    _run(L.aerort_vlidort_scalar_lambert_batch_dev, c, N, a, ref, stream)
+    _run(L.aerort_vlidort_scalar_lambert_batch_dev, c, N, a, ref, stream, pp)
     got = []
     for _ in range(2):  # two calls in a row reuse the same static arena
         o = outputs()
-        _run(L.aerort_vlidort_scalar_lambert_batch_dev_noalloc, c, N, a, o, stream)
+        _run(L.aerort_vlidort_scalar_lambert_batch_dev_noalloc, c, N, a, o, stream, pp)
         got.append(o)
     torch.cuda.synchronize()
     rrad, rrefl, rnf, rst = [t.cpu().numpy() for t in ref]
