@@ -509,6 +509,234 @@ struct OracleOpts {
 
 // Status codes shared with the CUDA path.
 enum { ORC_OK = 0, ORC_EIGEN_FAIL = 1, ORC_BVP_SINGULAR = 2, ORC_BAD_INPUT = 3 };
+}  // extern "C"
+
+struct FoGeom {
+  double mu0, mu1, cosscat;
+  std::vector<double> atten, lostrans, mult;  // atten[0..L], lostrans[L], mult[L]
+};
+
+// FO single-scatter geometry of one (sza, vza, raa) observation, upwelling
+// (VFO_Master.f90:652 -> FO_SSWPgeometry_master.f90:101; regular pseudo-spherical
+// or plane-parallel: FO_WPgeometry_Routines.f90:776; enhanced pseudo-spherical:
+// :1511/:1700/:2409).  radii = earth radius + heights, ext = extinction per km
+// (delta-M scaled when delta-M is on), dts = layer optical depths used on the
+// line of sight.  Outputs: mu0, mu1, the scattering cosine, the solar
+// attenuation at every level (atten[L] at BOA), line-of-sight transmittances and
+// the layer source multipliers of SSV_Integral_I_UP (FO_VectorSS_RTCalcs_I.f90:116).
+void fo_geometry(const OracleOpts* o, int L, const double* heights, const std::vector<double>& radii,
+                 const std::vector<double>& ext, const std::vector<double>& dts, double sza, double vza,
+                 double raa, FoGeom& G) {
+  bool enhanced = !o->do_plane_parallel && !o->do_focorr_nadir && o->do_focorr_outgoing;
+  const int nf = o->nfinelayers;
+  std::vector<double> tf(nf > 0 ? nf : 1), af(nf > 0 ? nf : 1);
+  const double vsign = 1.0;
+  double alpha_boa = vza, theta_boa = sza, phi_boa = raa;
+  if (phi_boa < 0.0) phi_boa = -phi_boa;
+  if (phi_boa > 360.0) phi_boa = 360.0 - phi_boa - 360.0;
+  bool overhead = (theta_boa == 0.0);
+  double theta_boa_R = theta_boa * DTR, ctheta_boa, stheta_boa;
+  if (theta_boa == 90.0) { ctheta_boa = 0.0; stheta_boa = 1.0; }
+  else { stheta_boa = std::sin(theta_boa_R); ctheta_boa = std::cos(theta_boa_R); }
+  double phi_boa_R = phi_boa * DTR, cphi = std::cos(phi_boa_R), sphi = std::sin(phi_boa_R);
+  std::vector<double> atten(L + 1, 0.0), suntau(L + 1, 0.0), lostrans(L, 0.0), mult(L, 0.0);
+  double mu0, mu1, cosscat;
+  // findsunpaths_D: paths through layers 1..nn of a ray leaving radius radstart
+  auto sunpaths_D = [&](bool zero_sun_boa, double radstart, double thstart, double sthstart, int nn,
+                        double* sp) {
+    int n1 = nn - 1;
+    if (zero_sun_boa) {
+      sp[nn] = radii[n1] - radstart;
+      for (int k = n1; k >= 1; --k) sp[k] = radii[k - 1] - radii[k];
+      return;
+    }
+    double sth0 = sthstart, th0 = thstart;
+    double sth1 = sth0 * radstart / radii[n1], th1 = std::asin(sth1), ks1 = th0 - th1;
+    sp[nn] = std::sin(ks1) * radstart / sth1;
+    sth0 = sth1; th0 = th1;
+    for (int k = n1; k >= 1; --k) {
+      sth1 = sth0 * radii[k] / radii[k - 1];
+      th1 = std::asin(sth1);
+      ks1 = th0 - th1;
+      sp[k] = std::sin(ks1) * radii[k] / sth1;
+      sth0 = sth1; th0 = th1;
+    }
+  };
+  // findsunpaths_T: tangent-point paths (sun below the local horizon)
+  auto sunpaths_T = [&](double radstart, double thstart, double sthstart, int nn, double* sp) -> int {
+    int n1 = nn - 1, nt = nn;
+    double tanr = sthstart * radstart;
+    int k = n1;
+    bool trawl = true;
+    while (k >= n1 && trawl && k <= L) { trawl = (radii[k] > tanr); k = k + 1; }
+    nt = k - 1;
+    if (nt > nn) {
+      double th0 = PIE - thstart, sth0 = sthstart;
+      double sth1 = sth0 * radstart / radii[nn], th1 = std::asin(sth1), ks1 = th0 - th1;
+      sp[nn] = 2.0 * std::sin(ks1) * radstart / sth1;
+      sth0 = sth1; th0 = th1;
+      for (int kk = nn + 1; kk <= nt - 1; ++kk) {
+        sth1 = sth0 * radii[kk - 1] / radii[kk];
+        th1 = std::asin(sth1); ks1 = th0 - th1;
+        sp[kk] = 2.0 * std::sin(ks1) * radii[kk] / sth0;
+        sth0 = sth1; th0 = th1;
+      }
+      ks1 = 0.5 * PIE - th0;
+      sp[nt] = 2.0 * std::sin(ks1) * radii[nt - 1];
+    } else if (nt == nn) {
+      sp[nn] = -2.0 * radstart * std::cos(thstart);
+    }
+    double th0 = PIE - thstart, sth0 = sthstart;
+    double sth1 = sth0 * radstart / radii[n1], th1 = std::asin(sth1), ks1 = th0 - th1;
+    sp[nn] = sp[nn] + std::sin(ks1) * radstart / sth1;
+    sth0 = sth1; th0 = th1;
+    for (int kk = n1; kk >= 1; --kk) {
+      sth1 = sth0 * radii[kk] / radii[kk - 1];
+      th1 = std::asin(sth1); ks1 = th0 - th1;
+      sp[kk] = std::sin(ks1) * radii[kk] / sth1;
+      sth0 = sth1; th0 = th1;
+    }
+    return nt;
+  };
+  std::vector<double> sp(L + 2, 0.0);
+  auto path_tau = [&](int nt) {
+    double s = 0.0;
+    for (int k = 1; k <= nt; ++k) s += ext[k - 1] * sp[k];
+    return s;
+  };
+  if (!enhanced) {
+    // regular PS (FO_WPgeometry_Routines.f90:776) or plane-parallel
+    double calpha_boa, salpha_boa, alpha_boa_R = alpha_boa * DTR;
+    if (alpha_boa == 90.0) { calpha_boa = 0.0; salpha_boa = 1.0; }
+    else { calpha_boa = std::cos(alpha_boa_R); salpha_boa = std::sin(alpha_boa_R); }
+    mu0 = ctheta_boa; mu1 = calpha_boa;
+    if (overhead) { cosscat = -vsign * calpha_boa; if (calpha_boa == 0.0) cosscat = calpha_boa; }
+    else cosscat = -vsign * calpha_boa * ctheta_boa + salpha_boa * stheta_boa * cphi;
+    atten[0] = 1.0;
+    for (int n = 1; n <= L; ++n) {
+      std::fill(sp.begin(), sp.end(), 0.0);
+      if (o->do_plane_parallel) {
+        for (int k = 1; k <= n; ++k) sp[k] = (heights[k - 1] - heights[k]) / ctheta_boa;
+      } else {
+        sunpaths_D(overhead, radii[n], theta_boa_R, stheta_boa, n, sp.data());
+      }
+      double s = path_tau(n);
+      suntau[n] = s;
+      if (s < FO_CUTOFF) atten[n] = std::exp(-s);
+    }
+    for (int n = L; n >= 1; --n) {
+      if (mu1 > 0.0) {
+        double lostau = dts[n - 1] / mu1;
+        if (lostau < FO_CUTOFF) lostrans[n - 1] = std::exp(-lostau);
+        double f1 = atten[n - 1] - atten[n] * lostrans[n - 1];
+        double f2 = 1.0 + (suntau[n] - suntau[n - 1]) / lostau;
+        mult[n - 1] = f1 / f2;
+      }
+    }
+  } else {
+    // enhanced PS: LosOut_EnhancedPS_Initial_WP, _Quadrature_WP, SolarIn_..._SunPaths_WP
+    bool donadir = (alpha_boa == 0.0);
+    std::vector<double> losw(L + 1, 0.0), alpha(L + 1, 0.0), cosa(L + 1, 0.0), sina(L + 1, 0.0);
+    double raycon = 0.0;
+    if (donadir) {
+      for (int n = L; n >= 1; --n) losw[n] = radii[n - 1] - radii[n];
+    } else {
+      double a_R = alpha_boa * DTR, salpha, calpha1;
+      if (alpha_boa == 90.0) { salpha = 1.0; calpha1 = 0.0; }
+      else { salpha = std::sin(a_R); calpha1 = std::cos(a_R); }
+      cosa[L] = calpha1; sina[L] = salpha; alpha[L] = a_R;
+      raycon = salpha * radii[L];
+      for (int n = L - 1; n >= 0; --n) {
+        sina[n] = raycon / radii[n];
+        alpha[n] = std::asin(sina[n]);
+        double calpha = std::cos(alpha[n]);
+        cosa[n] = calpha;
+        losw[n + 1] = radii[n] * calpha - radii[n + 1] * calpha1;
+        calpha1 = calpha;
+      }
+    }
+    // fine-layer quadrature (upwelling)
+    std::vector<double> xfine(L * nf), wfine(L * nf), rfine(L * nf), afine(L * nf, 0.0);
+    for (int n = L; n >= 1; --n) {
+      if (donadir) {
+        double difh = radii[n - 1] - radii[n];
+        getquad2(0.0, difh, nf, tf.data(), af.data());
+        for (int j = 0; j < nf; ++j) {
+          rfine[(n - 1) * nf + j] = radii[n] + tf[j];
+          xfine[(n - 1) * nf + j] = tf[j];
+          wfine[(n - 1) * nf + j] = af[j];
+        }
+      } else {
+        double rcn = radii[n] * cosa[n];
+        getquad2(0.0, losw[n], nf, tf.data(), af.data());
+        for (int j = 0; j < nf; ++j) {
+          double tanfine = raycon / (rcn + tf[j]);
+          double al = std::atan(tanfine);
+          double sn = std::sin(al);
+          afine[(n - 1) * nf + j] = al;
+          rfine[(n - 1) * nf + j] = raycon / sn;
+          xfine[(n - 1) * nf + j] = tf[j];
+          wfine[(n - 1) * nf + j] = af[j];
+        }
+      }
+    }
+    double calpha_boa, salpha_boa;
+    if (alpha_boa == 90.0) { calpha_boa = 0.0; salpha_boa = 1.0; }
+    else { salpha_boa = std::sin(alpha[L]); calpha_boa = std::cos(alpha[L]); }
+    mu1 = calpha_boa; mu0 = ctheta_boa;
+    double sdir[3] = {0.0, 0.0, 0.0};
+    if (!overhead) { sdir[0] = -stheta_boa * cphi * vsign; sdir[1] = -stheta_boa * sphi; sdir[2] = -ctheta_boa; }
+    if (overhead) { cosscat = -vsign * calpha_boa; if (calpha_boa == 0.0) cosscat = calpha_boa; }
+    else cosscat = -vsign * calpha_boa * ctheta_boa + salpha_boa * stheta_boa * cphi;
+    auto findsun = [&](double radius, double cumangle, double* th, double* sth, bool* dirsun) {
+      if (donadir) { *dirsun = true; *th = theta_boa_R; *sth = std::sin(theta_boa_R); return; }
+      if (overhead) { *dirsun = true; *sth = std::sin(cumangle); *th = cumangle; return; }
+      double px0 = -radius * std::sin(cumangle), px2 = radius * std::cos(cumangle);
+      double b = px0 * sdir[0] + px2 * sdir[2];
+      double ct = -b / radius;
+      *dirsun = (ct >= 0.0);
+      *sth = std::sqrt(1.0 - ct * ct);
+      *th = std::acos(ct);
+    };
+    // whole-layer boundary at BOA (attenuation used by the direct bounce)
+    for (int n = L; n >= 1; --n) {
+      bool zero_sun_boa = overhead && (n == L || donadir);
+      double th, sth; bool ds;
+      if (n == L) { th = theta_boa_R; sth = stheta_boa; ds = true; }
+      else findsun(radii[n], alpha[L] - alpha[n], &th, &sth, &ds);
+      std::fill(sp.begin(), sp.end(), 0.0);
+      int nt = n;
+      if (ds) sunpaths_D(zero_sun_boa, radii[n], th, sth, n, sp.data());
+      else nt = sunpaths_T(radii[n], th, sth, n, sp.data());
+      double s = path_tau(nt);
+      suntau[n] = s;
+      if (s < FO_CUTOFF) atten[n] = std::exp(-s);
+      // fine-layer attenuations and the layer multiplier
+      double kn = ext[n - 1];
+      double lostau = kn * losw[n];
+      if (lostau < FO_CUTOFF) lostrans[n - 1] = std::exp(-lostau);
+      double sum = 0.0;
+      for (int j = 0; j < nf; ++j) {
+        double thf, sthf; bool dsf;
+        findsun(rfine[(n - 1) * nf + j], alpha[L] - afine[(n - 1) * nf + j], &thf, &sthf, &dsf);
+        std::fill(sp.begin(), sp.end(), 0.0);
+        int ntf = n;
+        if (dsf) sunpaths_D(zero_sun_boa, rfine[(n - 1) * nf + j], thf, sthf, n, sp.data());
+        else ntf = sunpaths_T(rfine[(n - 1) * nf + j], thf, sthf, n, sp.data());
+        double sd = path_tau(ntf);
+        double attf = sd < FO_CUTOFF ? std::exp(-sd) : 0.0;
+        double dj = losw[n] - xfine[(n - 1) * nf + j];
+        double tran = std::exp(-kn * dj);
+        sum += attf * tran * wfine[(n - 1) * nf + j];
+      }
+      mult[n - 1] = sum * kn;
+    }
+  }
+  G.mu0 = mu0; G.mu1 = mu1; G.cosscat = cosscat;
+  G.atten = atten; G.lostrans = lostrans; G.mult = mult;
+}
+
+extern "C" {
 
 // One scalar VLIDORT solve for a single solar beam (sza) with nvza user zenith
 // angles and nraa azimuths (lattice of one beam; nvza=nraa=1 is the AeroApps
@@ -686,7 +914,6 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
   const int NG = nvza * nraa;
   std::vector<double> ss(NG, 0.0), db(NG, 0.0);
   if (o->do_focorr) {
-    bool enhanced = !o->do_plane_parallel && !o->do_focorr_nadir && o->do_focorr_outgoing;
     const double flux = o->flux_factor / PI4;
     std::vector<double> radii(L + 1), ext(L), dts(L), tms(L);
     for (int n = 0; n <= L; ++n) radii[n] = o->earth_radius + heights[n];
@@ -696,213 +923,15 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
       ext[n] = dts[n] / dz;
       tms[n] = o->do_deltam ? omega_in[n] / (1.0 - trunc[n] * omega_in[n]) : omega_in[n];
     }
-    const int nf = o->nfinelayers;
-    std::vector<double> tf(nf > 0 ? nf : 1), af(nf > 0 ? nf : 1);
     for (int u = 0; u < nvza; ++u)
       for (int a = 0; a < nraa; ++a) {
         const int g = a + nraa * u;
-        const double vsign = 1.0;
-        double alpha_boa = vza[u], theta_boa = sza, phi_boa = raa[a];
-        if (phi_boa < 0.0) phi_boa = -phi_boa;
-        if (phi_boa > 360.0) phi_boa = 360.0 - phi_boa - 360.0;
-        bool overhead = (theta_boa == 0.0);
-        double theta_boa_R = theta_boa * DTR, ctheta_boa, stheta_boa;
-        if (theta_boa == 90.0) { ctheta_boa = 0.0; stheta_boa = 1.0; }
-        else { stheta_boa = std::sin(theta_boa_R); ctheta_boa = std::cos(theta_boa_R); }
-        double phi_boa_R = phi_boa * DTR, cphi = std::cos(phi_boa_R), sphi = std::sin(phi_boa_R);
-        std::vector<double> atten(L + 1, 0.0), suntau(L + 1, 0.0), lostrans(L, 0.0), mult(L, 0.0);
-        double mu0, mu1, cosscat;
-        // findsunpaths_D: paths through layers 1..nn of a ray leaving radius radstart
-        auto sunpaths_D = [&](bool zero_sun_boa, double radstart, double thstart, double sthstart, int nn,
-                              double* sp) {
-          int n1 = nn - 1;
-          if (zero_sun_boa) {
-            sp[nn] = radii[n1] - radstart;
-            for (int k = n1; k >= 1; --k) sp[k] = radii[k - 1] - radii[k];
-            return;
-          }
-          double sth0 = sthstart, th0 = thstart;
-          double sth1 = sth0 * radstart / radii[n1], th1 = std::asin(sth1), ks1 = th0 - th1;
-          sp[nn] = std::sin(ks1) * radstart / sth1;
-          sth0 = sth1; th0 = th1;
-          for (int k = n1; k >= 1; --k) {
-            sth1 = sth0 * radii[k] / radii[k - 1];
-            th1 = std::asin(sth1);
-            ks1 = th0 - th1;
-            sp[k] = std::sin(ks1) * radii[k] / sth1;
-            sth0 = sth1; th0 = th1;
-          }
-        };
-        // findsunpaths_T: tangent-point paths (sun below the local horizon)
-        auto sunpaths_T = [&](double radstart, double thstart, double sthstart, int nn, double* sp) -> int {
-          int n1 = nn - 1, nt = nn;
-          double tanr = sthstart * radstart;
-          int k = n1;
-          bool trawl = true;
-          while (k >= n1 && trawl && k <= L) { trawl = (radii[k] > tanr); k = k + 1; }
-          nt = k - 1;
-          if (nt > nn) {
-            double th0 = PIE - thstart, sth0 = sthstart;
-            double sth1 = sth0 * radstart / radii[nn], th1 = std::asin(sth1), ks1 = th0 - th1;
-            sp[nn] = 2.0 * std::sin(ks1) * radstart / sth1;
-            sth0 = sth1; th0 = th1;
-            for (int kk = nn + 1; kk <= nt - 1; ++kk) {
-              sth1 = sth0 * radii[kk - 1] / radii[kk];
-              th1 = std::asin(sth1); ks1 = th0 - th1;
-              sp[kk] = 2.0 * std::sin(ks1) * radii[kk] / sth0;
-              sth0 = sth1; th0 = th1;
-            }
-            ks1 = 0.5 * PIE - th0;
-            sp[nt] = 2.0 * std::sin(ks1) * radii[nt - 1];
-          } else if (nt == nn) {
-            sp[nn] = -2.0 * radstart * std::cos(thstart);
-          }
-          double th0 = PIE - thstart, sth0 = sthstart;
-          double sth1 = sth0 * radstart / radii[n1], th1 = std::asin(sth1), ks1 = th0 - th1;
-          sp[nn] = sp[nn] + std::sin(ks1) * radstart / sth1;
-          sth0 = sth1; th0 = th1;
-          for (int kk = n1; kk >= 1; --kk) {
-            sth1 = sth0 * radii[kk] / radii[kk - 1];
-            th1 = std::asin(sth1); ks1 = th0 - th1;
-            sp[kk] = std::sin(ks1) * radii[kk] / sth1;
-            sth0 = sth1; th0 = th1;
-          }
-          return nt;
-        };
-        std::vector<double> sp(L + 2, 0.0);
-        auto path_tau = [&](int nt) {
-          double s = 0.0;
-          for (int k = 1; k <= nt; ++k) s += ext[k - 1] * sp[k];
-          return s;
-        };
-        if (!enhanced) {
-          // regular PS (FO_WPgeometry_Routines.f90:776) or plane-parallel
-          double calpha_boa, salpha_boa, alpha_boa_R = alpha_boa * DTR;
-          if (alpha_boa == 90.0) { calpha_boa = 0.0; salpha_boa = 1.0; }
-          else { calpha_boa = std::cos(alpha_boa_R); salpha_boa = std::sin(alpha_boa_R); }
-          mu0 = ctheta_boa; mu1 = calpha_boa;
-          if (overhead) { cosscat = -vsign * calpha_boa; if (calpha_boa == 0.0) cosscat = calpha_boa; }
-          else cosscat = -vsign * calpha_boa * ctheta_boa + salpha_boa * stheta_boa * cphi;
-          atten[0] = 1.0;
-          for (int n = 1; n <= L; ++n) {
-            std::fill(sp.begin(), sp.end(), 0.0);
-            if (o->do_plane_parallel) {
-              for (int k = 1; k <= n; ++k) sp[k] = (heights[k - 1] - heights[k]) / ctheta_boa;
-            } else {
-              sunpaths_D(overhead, radii[n], theta_boa_R, stheta_boa, n, sp.data());
-            }
-            double s = path_tau(n);
-            suntau[n] = s;
-            if (s < FO_CUTOFF) atten[n] = std::exp(-s);
-          }
-          for (int n = L; n >= 1; --n) {
-            if (mu1 > 0.0) {
-              double lostau = dts[n - 1] / mu1;
-              if (lostau < FO_CUTOFF) lostrans[n - 1] = std::exp(-lostau);
-              double f1 = atten[n - 1] - atten[n] * lostrans[n - 1];
-              double f2 = 1.0 + (suntau[n] - suntau[n - 1]) / lostau;
-              mult[n - 1] = f1 / f2;
-            }
-          }
-        } else {
-          // enhanced PS: LosOut_EnhancedPS_Initial_WP, _Quadrature_WP, SolarIn_..._SunPaths_WP
-          bool donadir = (alpha_boa == 0.0);
-          std::vector<double> losw(L + 1, 0.0), alpha(L + 1, 0.0), cosa(L + 1, 0.0), sina(L + 1, 0.0);
-          double raycon = 0.0;
-          if (donadir) {
-            for (int n = L; n >= 1; --n) losw[n] = radii[n - 1] - radii[n];
-          } else {
-            double a_R = alpha_boa * DTR, salpha, calpha1;
-            if (alpha_boa == 90.0) { salpha = 1.0; calpha1 = 0.0; }
-            else { salpha = std::sin(a_R); calpha1 = std::cos(a_R); }
-            cosa[L] = calpha1; sina[L] = salpha; alpha[L] = a_R;
-            raycon = salpha * radii[L];
-            for (int n = L - 1; n >= 0; --n) {
-              sina[n] = raycon / radii[n];
-              alpha[n] = std::asin(sina[n]);
-              double calpha = std::cos(alpha[n]);
-              cosa[n] = calpha;
-              losw[n + 1] = radii[n] * calpha - radii[n + 1] * calpha1;
-              calpha1 = calpha;
-            }
-          }
-          // fine-layer quadrature (upwelling)
-          std::vector<double> xfine(L * nf), wfine(L * nf), rfine(L * nf), afine(L * nf, 0.0);
-          for (int n = L; n >= 1; --n) {
-            if (donadir) {
-              double difh = radii[n - 1] - radii[n];
-              getquad2(0.0, difh, nf, tf.data(), af.data());
-              for (int j = 0; j < nf; ++j) {
-                rfine[(n - 1) * nf + j] = radii[n] + tf[j];
-                xfine[(n - 1) * nf + j] = tf[j];
-                wfine[(n - 1) * nf + j] = af[j];
-              }
-            } else {
-              double rcn = radii[n] * cosa[n];
-              getquad2(0.0, losw[n], nf, tf.data(), af.data());
-              for (int j = 0; j < nf; ++j) {
-                double tanfine = raycon / (rcn + tf[j]);
-                double al = std::atan(tanfine);
-                double sn = std::sin(al);
-                afine[(n - 1) * nf + j] = al;
-                rfine[(n - 1) * nf + j] = raycon / sn;
-                xfine[(n - 1) * nf + j] = tf[j];
-                wfine[(n - 1) * nf + j] = af[j];
-              }
-            }
-          }
-          double calpha_boa, salpha_boa;
-          if (alpha_boa == 90.0) { calpha_boa = 0.0; salpha_boa = 1.0; }
-          else { salpha_boa = std::sin(alpha[L]); calpha_boa = std::cos(alpha[L]); }
-          mu1 = calpha_boa; mu0 = ctheta_boa;
-          double sdir[3] = {0.0, 0.0, 0.0};
-          if (!overhead) { sdir[0] = -stheta_boa * cphi * vsign; sdir[1] = -stheta_boa * sphi; sdir[2] = -ctheta_boa; }
-          if (overhead) { cosscat = -vsign * calpha_boa; if (calpha_boa == 0.0) cosscat = calpha_boa; }
-          else cosscat = -vsign * calpha_boa * ctheta_boa + salpha_boa * stheta_boa * cphi;
-          auto findsun = [&](double radius, double cumangle, double* th, double* sth, bool* dirsun) {
-            if (donadir) { *dirsun = true; *th = theta_boa_R; *sth = std::sin(theta_boa_R); return; }
-            if (overhead) { *dirsun = true; *sth = std::sin(cumangle); *th = cumangle; return; }
-            double px0 = -radius * std::sin(cumangle), px2 = radius * std::cos(cumangle);
-            double b = px0 * sdir[0] + px2 * sdir[2];
-            double ct = -b / radius;
-            *dirsun = (ct >= 0.0);
-            *sth = std::sqrt(1.0 - ct * ct);
-            *th = std::acos(ct);
-          };
-          // whole-layer boundary at BOA (attenuation used by the direct bounce)
-          for (int n = L; n >= 1; --n) {
-            bool zero_sun_boa = overhead && (n == L || donadir);
-            double th, sth; bool ds;
-            if (n == L) { th = theta_boa_R; sth = stheta_boa; ds = true; }
-            else findsun(radii[n], alpha[L] - alpha[n], &th, &sth, &ds);
-            std::fill(sp.begin(), sp.end(), 0.0);
-            int nt = n;
-            if (ds) sunpaths_D(zero_sun_boa, radii[n], th, sth, n, sp.data());
-            else nt = sunpaths_T(radii[n], th, sth, n, sp.data());
-            double s = path_tau(nt);
-            suntau[n] = s;
-            if (s < FO_CUTOFF) atten[n] = std::exp(-s);
-            // fine-layer attenuations and the layer multiplier
-            double kn = ext[n - 1];
-            double lostau = kn * losw[n];
-            if (lostau < FO_CUTOFF) lostrans[n - 1] = std::exp(-lostau);
-            double sum = 0.0;
-            for (int j = 0; j < nf; ++j) {
-              double thf, sthf; bool dsf;
-              findsun(rfine[(n - 1) * nf + j], alpha[L] - afine[(n - 1) * nf + j], &thf, &sthf, &dsf);
-              std::fill(sp.begin(), sp.end(), 0.0);
-              int ntf = n;
-              if (dsf) sunpaths_D(zero_sun_boa, rfine[(n - 1) * nf + j], thf, sthf, n, sp.data());
-              else ntf = sunpaths_T(rfine[(n - 1) * nf + j], thf, sthf, n, sp.data());
-              double sd = path_tau(ntf);
-              double attf = sd < FO_CUTOFF ? std::exp(-sd) : 0.0;
-              double dj = losw[n] - xfine[(n - 1) * nf + j];
-              double tran = std::exp(-kn * dj);
-              sum += attf * tran * wfine[(n - 1) * nf + j];
-            }
-            mult[n - 1] = sum * kn;
-          }
-        }
+        FoGeom G;
+        fo_geometry(o, L, heights, radii, ext, dts, sza, vza[u], raa[a], G);
+        const double mu0 = G.mu0, cosscat = G.cosscat;
+        const std::vector<double>& atten = G.atten;
+        const std::vector<double>& lostrans = G.lostrans;
+        const std::vector<double>& mult = G.mult;
         // scattering-angle Legendre sum (FO_VectorSS_Spherfuncs.f90, NSTOKES=1)
         std::vector<double> gs(ngreek + 1);
         gs[0] = 1.0;
