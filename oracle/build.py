@@ -1,6 +1,7 @@
 """Build recipe of the CPU oracle (test infrastructure only).
 
-Compiles the oracle's own C/C++ restatement (vlidort_oracle.cpp, mie_oracle.c,
+Compiles the oracle's own C/C++ restatement (vlidort_oracle.cpp,
+vlidort_vector_oracle.cpp, mie_oracle.c,
 rot_oracle.c, edge_oracle.c)
 into oracle/_build/liboracle.so with strict IEEE semantics (no contraction of
 a*b+c into FMA, so the FP32 Mie path reproduces the reference arithmetic).
@@ -14,13 +15,14 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboracle.so")
-SRCS = ["vlidort_oracle.cpp", "mie_oracle.c", "rot_oracle.c", "edge_oracle.c"]
+SRCS = ["vlidort_oracle.cpp", "vlidort_vector_oracle.cpp", "mie_oracle.c", "rot_oracle.c", "edge_oracle.c"]
 
 
 def build(force=False):
     os.makedirs(OUT, exist_ok=True)
     srcs = [os.path.join(HERE, s) for s in SRCS]
-    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs + [__file__]):
+    deps = srcs + [__file__, os.path.join(HERE, "vlidort_oracle.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in deps):
         return LIB
     objs = []
     for s in srcs:

@@ -30,6 +30,7 @@ def lib():
     if _lib is None:
         _lib = ctypes.CDLL(_build.build())
         _lib.oracle_vlidort_solve.restype = ctypes.c_int
+        _lib.oracle_vlidort_vector_solve.restype = ctypes.c_int
         _lib.oracle_scalar_lambert.restype = ctypes.c_int
         _lib.oracle_get_aop_vector.restype = ctypes.c_int
         _lib.oracle_set_asymtx_tol.restype = None
@@ -58,6 +59,26 @@ def vlidort_solve(opts, heights, deltau, omega, greek, albedo, sza, vzas, raas, 
                                     _p(omega, P_d), _p(greek, P_d), ctypes.c_double(albedo), ctypes.c_double(sza),
                                     len(vz), _p(vz, P_d), len(ra), _p(ra, P_d), _p(out, P_d), ctypes.byref(nf))
     return out.reshape(len(vz), len(ra)), nf.value, st
+
+
+def vlidort_vector_solve(opts, nstokes, heights, deltau, omega, greek16, albedo, sza, vzas, raas, nstreams):
+    """Single-beam polarized solve (lattice of vzas x raas).  greek16: (16, L,
+    ngreek+1), entry k of the row-major 4x4 Greek matrix.  Returns (out[nvza,
+    nraa, nstokes], nfourier, status)."""
+    heights = np.ascontiguousarray(heights, np.float64)
+    deltau = np.ascontiguousarray(deltau, np.float64)
+    omega = np.ascontiguousarray(omega, np.float64)
+    greek = np.ascontiguousarray(greek16, np.float64)
+    _, L, g1 = greek.shape
+    vz = np.ascontiguousarray(vzas, np.float64)
+    ra = np.ascontiguousarray(raas, np.float64)
+    out = np.zeros(len(vz) * len(ra) * nstokes)
+    nf = ctypes.c_int(0)
+    st = lib().oracle_vlidort_vector_solve(ctypes.byref(opts), nstokes, L, nstreams, g1 - 1, _p(heights, P_d),
+                                           _p(deltau, P_d), _p(omega, P_d), _p(greek, P_d), ctypes.c_double(albedo),
+                                           ctypes.c_double(sza), len(vz), _p(vz, P_d), len(ra), _p(ra, P_d),
+                                           _p(out, P_d), ctypes.byref(nf))
+    return out.reshape(len(vz), len(ra), nstokes), nf.value, st
 
 
 def scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g, pmom, pe, he,

@@ -19,15 +19,9 @@
 
 #include <omp.h>
 
-namespace {
+#include "vlidort_oracle.h"
 
-// vlidort_def/vlidort_pars.f90:386-444 (truncated DEG_TO_RAD is reproduced on purpose)
-const double DTR = 1.7453292519943e-02;
-const double PIE = 180.0 * DTR;
-const double PI4 = 4.0 * PIE;
-const double TAYLOR_SMALL = 1.0e-4;
-const double MAX_TAU_SPATH = 32.0, MAX_TAU_UPATH = 32.0, MAX_TAU_QPATH = 32.0;
-const double FO_CUTOFF = 88.0;  // vlidort_focode/FO_VectorSS_RTCalcs_I.f90:325
+namespace orc {
 
 typedef std::vector<double> dvec;
 
@@ -486,44 +480,6 @@ void band_solve(int n, int kl, int ku, const double* ab, int ldab, const int* ip
   }
 }
 
-}  // namespace
-
-extern "C" {
-
-// Options of one VLIDORT master call (the subset of VLIDORT_FixIn/ModIn that the
-// AeroApps wrapper VLIDORT2p8p3/VLIDORT_Mod.F90:65-383 and the solar tester use).
-struct OracleOpts {
-  int do_focorr;           // DO_FOCORR (FO single scatter + direct bounce)
-  int do_focorr_nadir;     // DO_FOCORR_NADIR (regular pseudo-spherical FO)
-  int do_focorr_outgoing;  // DO_FOCORR_OUTGOING (enhanced pseudo-spherical FO)
-  int do_deltam;           // DO_DELTAM_SCALING
-  int do_plane_parallel;   // DO_PLANE_PARALLEL
-  int do_double_convtest;  // DO_DOUBLE_CONVTEST
-  int nfinelayers;         // NFINELAYERS
-  int taylor_order;        // TAYLOR_ORDER
-  double accuracy;         // VLIDORT_ACCURACY
-  double asymtx_tol;       // ASYMTX_TOLERANCE
-  double earth_radius;     // EARTH_RADIUS [km]
-  double flux_factor;      // FLUX_FACTOR
-};
-
-// Status codes shared with the CUDA path.
-enum { ORC_OK = 0, ORC_EIGEN_FAIL = 1, ORC_BVP_SINGULAR = 2, ORC_BAD_INPUT = 3 };
-}  // extern "C"
-
-struct FoGeom {
-  double mu0, mu1, cosscat;
-  std::vector<double> atten, lostrans, mult;  // atten[0..L], lostrans[L], mult[L]
-};
-
-// FO single-scatter geometry of one (sza, vza, raa) observation, upwelling
-// (VFO_Master.f90:652 -> FO_SSWPgeometry_master.f90:101; regular pseudo-spherical
-// or plane-parallel: FO_WPgeometry_Routines.f90:776; enhanced pseudo-spherical:
-// :1511/:1700/:2409).  radii = earth radius + heights, ext = extinction per km
-// (delta-M scaled when delta-M is on), dts = layer optical depths used on the
-// line of sight.  Outputs: mu0, mu1, the scattering cosine, the solar
-// attenuation at every level (atten[L] at BOA), line-of-sight transmittances and
-// the layer source multipliers of SSV_Integral_I_UP (FO_VectorSS_RTCalcs_I.f90:116).
 void fo_geometry(const OracleOpts* o, int L, const double* heights, const std::vector<double>& radii,
                  const std::vector<double>& ext, const std::vector<double>& dts, double sza, double vza,
                  double raa, FoGeom& G) {
@@ -735,6 +691,10 @@ void fo_geometry(const OracleOpts* o, int L, const double* heights, const std::v
   G.mu0 = mu0; G.mu1 = mu1; G.cosscat = cosscat;
   G.atten = atten; G.lostrans = lostrans; G.mult = mult;
 }
+
+}  // namespace orc
+
+using namespace orc;
 
 extern "C" {
 

@@ -24,3 +24,10 @@ def golden_obsgeo():
     import json
     with open(os.path.join(ROOT, "tests", "golden", "obsgeo_lpcs.json")) as f:
         return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def golden_iqu():
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "solar_tester_iqu.json")) as f:
+        return json.load(f)
