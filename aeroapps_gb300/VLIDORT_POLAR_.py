@@ -11,10 +11,13 @@ The same calls work here:
   scalar_lambert(channels, nstreams, plane_parallel, ROT, depol, tau, ssa, g, pmom, pe, he, te, albedo,
                  solar_zenith, relat_azymuth, sensor_zenith, MISSING, verbose)
                                                               -> (radiance, reflectance, rc)  (:606-671)
+  vector_lambert(channels, nstreams, plane_parallel, ROT, depol, alpha, tau, ssa, pmom, pe, he, te, albedo,
+                 solar_zenith, relat_azymuth, sensor_zenith, flux_factor, MISSING, verbose)
+                                                              -> (radiance, reflectance, Q, U, rc)  (:457-526)
 Shapes are the Fortran ones: ROT (km, nobs, nch), tau/ssa/g (km, nch, nobs),
 pmom (km, nch, nobs, nMom, nPol), pe/he/te (km+1, nobs), albedo (nobs, nch).
-The vector, BRDF, BPDF, ocean and cloud entries of the module
-(VECTOR_*, :43-604 and :673-1145) need the polarised RT and the BRDF surface
+The BRDF, BPDF, ocean and cloud entries of the module (VECTOR_BRDF_*,
+VECTOR_*CX*, *_CLOUD; :43-455, :528-604, :673-1145) need the BRDF surface
 supplement, which this package does not have; they are not defined, so a
 call to one fails with AttributeError rather than running something else.
 """
@@ -46,3 +49,19 @@ def scalar_lambert(channels, nstreams, plane_parallel, ROT, depol, tau, ssa, g, 
     return vlidort.vlidort_scalar_lambert(k, c, o, channels, int(nstreams), plane_parallel, m, p, ROT, depol, tau,
                                           ssa, g, pmom, pe, he, te, albedo, solar_zenith, relat_azymuth,
                                           sensor_zenith, MISSING, verbose)
+
+
+def vector_lambert(channels, nstreams, plane_parallel, ROT, depol, alpha, tau, ssa, pmom, pe, he, te, albedo,
+                   solar_zenith, relat_azymuth, sensor_zenith, flux_factor, MISSING, verbose=0, km=None, nch=None,
+                   nobs=None, nmom=None, npol=None):
+    """VECTOR_LAMBERT (VLIDORT_POLAR_py.F90:457-526) -> (radiance, reflectance, Q, U, rc)."""
+    tau = np.asarray(tau)
+    pmom = np.asarray(pmom)
+    k, c, o = tau.shape
+    m, p = pmom.shape[3], pmom.shape[4]
+    for given, have, name in ((km, k, "km"), (nch, c, "nch"), (nobs, o, "nobs"), (nmom, m, "nmom"), (npol, p, "npol")):
+        if given is not None and given != have:
+            raise ValueError("vector_lambert: %s = %d disagrees with the arrays (%d)" % (name, given, have))
+    return vlidort.vlidort_vector_lambert(k, c, o, channels, int(nstreams), plane_parallel, m, p, ROT, depol, alpha, tau,
+                                          ssa, pmom, pe, he, te, albedo, solar_zenith, relat_azymuth, sensor_zenith,
+                                          flux_factor, MISSING, verbose)

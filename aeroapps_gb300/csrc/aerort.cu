@@ -87,10 +87,12 @@ int Context::bind(cudaStream_t s) {
   if (!p) {
     for (auto& q : pads)
       if (!q.used) { p = &q; break; }
-    if (!p) {  // all taken: the least recently used one
-      p = &pads[0];
+    if (!p) {  // all taken: the least recently used one that no captured graph holds
       for (auto& q : pads)
-        if (q.last < p->last) p = &q;
+        if (!q.captured && (!p || q.last < p->last)) p = &q;
+      if (!p)
+        return set_error(AERORT_RC_ARG, "every library scratch pad is held by a stream whose work was captured "
+                                        "in a CUDA graph (at most 16 such streams)");
     }
     if (!p->done) CUDA_TRY(cudaEventCreateWithFlags(&p->done, cudaEventDisableTiming));
     if (p->used) CUDA_TRY(cudaStreamWaitEvent(s, p->done, 0));
@@ -102,8 +104,17 @@ int Context::bind(cudaStream_t s) {
   return 0;
 }
 
+// Work enqueued while `s` is being captured into a CUDA graph is replayed
+// later, any number of times, on the pad's scratch: such a pad stays with its
+// stream for good (never handed to another stream), and no event is recorded
+// for it (an event recorded during capture cannot be waited on outside it).
 int Context::unbind(cudaStream_t s) {
-  if (pad) CUDA_TRY(cudaEventRecord(pad->done, s));
+  if (pad) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CUDA_TRY(cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusNone) CUDA_TRY(cudaEventRecord(pad->done, s));
+    else pad->captured = true;
+  }
   pad = nullptr;
   return 0;
 }

@@ -67,6 +67,7 @@ struct Pad {
   DevBuf scratch, counter, redo;
   cudaStream_t owner = nullptr;
   cudaEvent_t done = nullptr;  // recorded on `owner` after the last launch that used the pad
+  bool captured = false;       // used by work captured into a CUDA graph: stays with `owner`
   unsigned long last = 0;
   bool used = false;
 };

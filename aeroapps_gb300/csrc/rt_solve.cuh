@@ -39,6 +39,10 @@ struct LambertInputs {
   // pixel from there on uses the nadir (regular pseudo-spherical) correction.
   const int* nadir_first;  // device scalar, nobs if never triggered; may be null
   double missing;
+  // Trace-gas absorption optical depth alpha(km, nobs, nch) of the polarized
+  // wrapper (VLIDORT_LAMBERT.F90:192, VLIDORT_ScatMod.F90:488-497); null = 0
+  // (the scalar wrapper has none).
+  const double* alpha = nullptr;
 };
 
 // Scratch element counts per thread for a solve with at most L layers: an
@@ -1228,7 +1232,8 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
     const long a = k + (long)in.km * (i + (long)in.nch * j);
     const double tl = in.tau_f ? (double)in.tau_f[a] : in.tau[a];
     const double sl = in.ssa_f ? (double)in.ssa_f[a] : in.ssa[a];
-    const double tau_ext = 0.0 + ray + tl;
+    const double alpha_l = in.alpha ? in.alpha[k + (long)in.km * (j + (long)in.nobs * i)] : 0.0;
+    const double tau_ext = alpha_l + ray + tl;
     const double tau_scat = ray + sl * tl;
     if (!(tau_ext > 0.0) || !(tau_scat > 0.0)) {
       radiance[o] = in.missing; reflectance[o] = in.missing;

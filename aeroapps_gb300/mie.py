@@ -62,14 +62,22 @@ def _cache_dir():
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "mie_cache")
 
 
-def generate_tables(channels_nm, nmom=64, nrh=NRH, nradii=160, use_cache=True):
+def generate_tables(channels_nm, nmom=64, nrh=NRH, nradii=160, use_cache=True, npol=1):
     """Synthetic GEOS-style Mie tables at the requested channels [nm].
 
     RH nodes: nrh values evenly spaced on [0, 0.99] (REAL*4).  Wet particles:
-    radius x (1-RH)^-0.2, refractive index volume-mixed with water.
+    radius x (1-RH)^-0.2, refractive index volume-mixed with water.  npol = 1:
+    P11 Legendre moments; npol = 6: the Greek coefficients of P11, P12, P33,
+    P34, P22, P44 (the layout of the GEOS optics tables used by the polarized
+    path).
     """
+    if npol not in (1, 6):
+        raise ValueError("npol must be 1 or 6")
     channels_nm = np.asarray(channels_nm, dtype=np.float64)
-    key = hashlib.sha256(repr((channels_nm.tolist(), nmom, nrh, nradii, SPECIES, BIN_RG_UM, BIN_SIGMA)).encode()).hexdigest()[:16]
+    ident = (channels_nm.tolist(), nmom, nrh, nradii, SPECIES, BIN_RG_UM, BIN_SIGMA)
+    if npol != 1:
+        ident = ident + (npol,)
+    key = hashlib.sha256(repr(ident).encode()).hexdigest()[:16]
     path = os.path.join(_cache_dir(), "mie_%s.npz" % key)
     rh = np.linspace(0.0, 0.99, nrh).astype(np.float32)
     if use_cache and os.path.exists(path):
@@ -92,14 +100,13 @@ def generate_tables(channels_nm, nmom=64, nrh=NRH, nradii=160, use_cache=True):
         bext = np.zeros((nrh, nch, NBIN), np.float32, order="F")
         bsca = np.zeros_like(bext)
         g = np.zeros_like(bext)
-        pm = np.zeros((nrh, nch, NBIN, nmom), np.float32, order="F")
-        rc = L.aerort_miegen_lognormal(nch, _lib.ptr(lam, _lib.P_d), nrh, _lib.ptr(rh64, _lib.P_d), NBIN,
-                                       _lib.ptr(rg, _lib.P_d), _lib.ptr(sg, _lib.P_d), nr, ni, int(hyg), rho, nmom,
-                                       nradii, _lib.ptr(bext, _lib.P_f), _lib.ptr(bsca, _lib.P_f),
-                                       _lib.ptr(g, _lib.P_f), _lib.ptr(pm, _lib.P_f))
+        pm = np.zeros((nrh, nch, NBIN, nmom, npol), np.float32, order="F")
+        rc = L.aerort_miegen_lognormal_pol(nch, _lib.ptr(lam, _lib.P_d), nrh, _lib.ptr(rh64, _lib.P_d), NBIN,
+                                           _lib.ptr(rg, _lib.P_d), _lib.ptr(sg, _lib.P_d), nr, ni, int(hyg), rho, nmom,
+                                           npol, nradii, _lib.ptr(bext, _lib.P_f), _lib.ptr(bsca, _lib.P_f),
+                                           _lib.ptr(g, _lib.P_f), _lib.ptr(pm, _lib.P_f))
         if rc != 0:
             raise RuntimeError("Mie table generation failed for %s" % name)
-        pm = np.asfortranarray(pm.reshape(nrh, nch, NBIN, nmom, 1, order="F"))
         tabs.append(MieTable(name, rh, bext, bsca, g, pm))
         save.update({name + "_bext": bext, name + "_bsca": bsca, name + "_g": g, name + "_pmom": pm})
     if use_cache:

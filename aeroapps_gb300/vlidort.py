@@ -1,4 +1,5 @@
-"""VLIDORT_Scalar_Lambert on the GPU, with the reference's argument list.
+"""VLIDORT_Scalar_Lambert and VLIDORT_Vector_Lambert on the GPU, with the
+reference's argument lists.
 
 Mirrors src/Components/rtms/geo_vlidort/VLIDORT_LAMBERT.F90:34-168 (and its
 f2py exposure, src/Components/rtms/leo_vlidort/VLIDORT_POLAR_py.F90): every
@@ -91,6 +92,40 @@ def vlidort_scalar_lambert_batch(km, nch, nobs, nstreams, nMom, nlay, ROT, depol
         raise RuntimeError("aerort_vlidort_scalar_lambert_batch rc=%d: %s" % (rc, _lib.last_error()))
     return rad, refl, rc, nf, st
 
+
+
+def vlidort_vector_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, alpha, tau, ssa,
+                           pmom, pe, he, te, albedo, solar_zenith, relat_azymuth, sensor_zenith, flux_factor,
+                           MISSING=MISSING, verbose=0, diagnostics=False):
+    """VLIDORT_Vector_Lambert (geo_vlidort/VLIDORT_LAMBERT.F90:172-342), NSTOKES = 3.
+
+    Shapes: channels(nch) [nm], ROT/alpha(km,nobs,nch) (alpha may be None),
+    tau/ssa(km,nch,nobs), pmom(km,nch,nobs,nMom,6) (P11, P12, P33, P34, P22,
+    P44), pe/he/te(km+1,nobs), albedo(nobs,nch), angles(nobs),
+    flux_factor(nch,nobs).  Returns (radiance, reflectance, Q, U, rc), plus
+    (nfourier, status) with diagnostics=True.
+    """
+    ch, ROT, depol, tau, ssa, pmom, pe, he, te, albedo, sza, raa, vza, ff = [
+        _f64(a) for a in (channels, ROT, depol, tau, ssa, pmom, pe, he, te, albedo, solar_zenith, relat_azymuth,
+                          sensor_zenith, flux_factor)]
+    al = None if alpha is None else _f64(alpha)
+    if ROT.shape != (km, nobs, nch) or tau.shape != (km, nch, nobs) or he.shape != (km + 1, nobs):
+        raise ValueError("array shapes do not match (km, nch, nobs) = (%d, %d, %d)" % (km, nch, nobs))
+    if pmom.shape != (km, nch, nobs, nMom, nPol) or ff.shape != (nch, nobs):
+        raise ValueError("pmom must have shape (km, nch, nobs, nMom, nPol) and flux_factor (nch, nobs)")
+    out = [np.zeros((nobs, nch), np.float64, order="F") for _ in range(4)]
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    P = lambda a: None if a is None else _lib.ptr(a, _lib.P_d)
+    rc = _lib.lib().aerort_vlidort_vector_lambert_ex(
+        km, nch, nobs, P(ch), nstreams, int(bool(plane_parallel)), nMom, nPol, P(ROT), P(depol), P(al), P(tau), P(ssa),
+        P(pmom), P(pe), P(he), P(te), P(albedo), P(sza), P(raa), P(vza), P(ff), float(MISSING), int(verbose),
+        *[P(a) for a in out], _lib.ptr(nf, _lib.P_i), _lib.ptr(st, _lib.P_i))
+    if rc >= 1000:
+        raise RuntimeError("aerort_vlidort_vector_lambert rc=%d: %s" % (rc, _lib.last_error()))
+    if diagnostics:
+        return out[0], out[1], out[2], out[3], rc, nf, st
+    return out[0], out[1], out[2], out[3], rc
 
 
 def rot_calc(channels, pe, he, te, MISSING, verbose=0):

@@ -167,7 +167,11 @@ int aerort_vlidort_scalar_lambert_dev(int km, int nch, int nobs, int nstreams, i
  * the reference: it batches many VLIDORT_Scalar_Lambert calls into one launch.
  * Calls on different streams use different library scratch (one pad per
  * stream, up to 16 streams at once), so groups of different stream counts may
- * be enqueued on separate streams and run concurrently. */
+ * be enqueued on separate streams and run concurrently.  The calls may be
+ * captured into a CUDA graph once an eager call of the same size on the same
+ * stream has sized the scratch (no allocation is allowed during capture); a
+ * pad used by captured work then stays with its stream for good, so graph
+ * replays never share scratch with other streams. */
 int aerort_vlidort_scalar_lambert_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
                                             const int* nlay, const double* ROT, const double* depol,
                                             const double* tau, const double* ssa, const double* pmom,
@@ -204,6 +208,54 @@ int aerort_vlidort_scalar_lambert_mixed_batch(int km, int nch, int nobs, int nst
                                               const double* relat_azymuth, const double* sensor_zenith,
                                               double MISSING, double* radiance_VL, double* reflectance_VL,
                                               int* nfourier, int* status);
+
+/* VLIDORT_Vector_Lambert (geo_vlidort/VLIDORT_LAMBERT.F90:172-342, single
+ * geometry per pixel; f2py VECTOR_LAMBERT, leo_vlidort/VLIDORT_POLAR_py.F90
+ * :457-526): TOA radiance, reflectance and Stokes Q, U for nobs pixels x nch
+ * channels with NSTOKES = 3, the VLIDORT_Init settings of the scalar call and
+ * the 16-entry Greek-matrix mixing of VLIDORT_Run_Vector_SingleGeom
+ * (VLIDORT_ScatMod.F90:284-617).  Same arguments as the reference:
+ * alpha(km,nobs,nch) trace-gas absorption (may be NULL = 0),
+ * pmom(km,nch,nobs,nMom,nPol) with nPol = 6 elements P11, P12, P33, P34, P22,
+ * P44 (as aerort_get_aop_vector with nPol = 6 writes them), flux_factor(nch,nobs)
+ * solar flux F0 (reflectance = pi I / (cos(sza) F0), single-precision pi),
+ * radiance_VL, reflectance_VL, Q, U (nobs,nch).  A pixel with MISSING angles
+ * or albedo, or whose solve fails, gets MISSING in all four outputs (the
+ * reference writes Q, U of a missing-angle pixel only at a stale channel
+ * index).  FP64 with a real eigen-decomposition per layer (the reference's
+ * real eigensolver mask is always set for NSTOKES = 3); nstreams one of 4, 6,
+ * 8, 12, 16.  rc: 0; 2, 3, 5 as the scalar call; AERORT_RC_ARG for nPol != 6. */
+int aerort_vlidort_vector_lambert(int km, int nch, int nobs, const double* channels, int nstreams,
+                                  int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                  const double* alpha, const double* tau, const double* ssa, const double* pmom,
+                                  const double* pe, const double* he, const double* te, const double* albedo,
+                                  const double* solar_zenith, const double* relat_azymuth,
+                                  const double* sensor_zenith, const double* flux_factor, double MISSING,
+                                  int verbose, double* radiance_VL, double* reflectance_VL, double* Q, double* U);
+/* Same, plus nfourier(nobs,nch) (last Fourier term) and status(nobs,nch)
+ * (AERORT_ST_*); either may be NULL. */
+int aerort_vlidort_vector_lambert_ex(int km, int nch, int nobs, const double* channels, int nstreams,
+                                     int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                     const double* alpha, const double* tau, const double* ssa, const double* pmom,
+                                     const double* pe, const double* he, const double* te, const double* albedo,
+                                     const double* solar_zenith, const double* relat_azymuth,
+                                     const double* sensor_zenith, const double* flux_factor, double MISSING,
+                                     int verbose, double* radiance_VL, double* reflectance_VL, double* Q, double* U,
+                                     int* nfourier, int* status);
+/* Batched device form (no counterpart routine in the reference): every array
+ * a device pointer, nlay(nobs) per-column layer counts (may be NULL), optics
+ * either FP64 (tau, ssa, pmom) or FP32 straight from aerort_get_aop_vector_dev
+ * with nPol = 6 (tau_f, ssa_f, pmom_f), flux_factor may be NULL (1).  Enqueued
+ * on `stream` with the library's scratch pad of that stream. */
+int aerort_vlidort_vector_lambert_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                            const int* nlay, const double* ROT, const double* depol,
+                                            const double* alpha, const double* tau, const double* ssa,
+                                            const double* pmom, const float* tau_f, const float* ssa_f,
+                                            const float* pmom_f, const double* he, const double* albedo,
+                                            const double* solar_zenith, const double* relat_azymuth,
+                                            const double* sensor_zenith, const double* flux_factor, double MISSING,
+                                            double* radiance_VL, double* reflectance_VL, double* Q, double* U,
+                                            int* nfourier, int* status, void* stream);
 
 /* Edge pressure pe (Pa), height above the surface ze (m) and temperature te
  * (K), each (km+1,nobs), from layer air density airdens (kg m-3) and pressure

@@ -31,6 +31,7 @@ def lib():
         _lib = ctypes.CDLL(_build.build())
         _lib.oracle_vlidort_solve.restype = ctypes.c_int
         _lib.oracle_vlidort_vector_solve.restype = ctypes.c_int
+        _lib.oracle_vector_lambert.restype = ctypes.c_int
         _lib.oracle_scalar_lambert.restype = ctypes.c_int
         _lib.oracle_get_aop_vector.restype = ctypes.c_int
         _lib.oracle_set_asymtx_tol.restype = None
@@ -99,6 +100,27 @@ def scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol
                                      _p(nf, P_i), _p(st, P_i),
                                      None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
     return rad, refl, rc, nf, st
+
+
+def vector_lambert(km, nch, nobs, nstreams, plane_parallel, nMom, ROT, depol, alpha, tau, ssa, pmom, he, albedo,
+                   solar_zenith, relat_azymuth, sensor_zenith, flux_factor, MISSING, nlay=None):
+    """Oracle VLIDORT_Vector_Lambert (NSTOKES = 3); pmom (km, nch, nobs, nMom, 6).
+    Returns (radiance, reflectance, Q, U, rc, nfourier, status), each (nobs, nch)."""
+    F = lambda a: np.asfortranarray(a, np.float64)
+    arr = [F(x) for x in (ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith, relat_azymuth, sensor_zenith)]
+    al = None if alpha is None else F(alpha)
+    ff = None if flux_factor is None else F(flux_factor)
+    out = [np.zeros((nobs, nch), order="F") for _ in range(4)]
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    rot, dep, ta, ss, pm, h_e, alb, sz, ra, vz = arr
+    rc = lib().oracle_vector_lambert(km, nch, nobs, nstreams, int(plane_parallel), nMom, _p(rot, P_d), _p(dep, P_d),
+                                     None if al is None else _p(al, P_d), _p(ta, P_d), _p(ss, P_d), _p(pm, P_d),
+                                     _p(h_e, P_d), _p(alb, P_d), _p(sz, P_d), _p(ra, P_d), _p(vz, P_d),
+                                     None if ff is None else _p(ff, P_d), ctypes.c_double(MISSING),
+                                     *[_p(a, P_d) for a in out], _p(nf, P_i), _p(st, P_i),
+                                     None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
+    return out[0], out[1], out[2], out[3], rc, nf, st
 
 
 def set_threads(n):

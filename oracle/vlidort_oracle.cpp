@@ -1359,6 +1359,7 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
 // that tolerance moves the reference algorithm from the converged solution.
 static double g_asymtx_tol = 1.0e-12;
 extern "C" void oracle_set_asymtx_tol(double tol) { g_asymtx_tol = tol; }
+extern "C" double oracle_get_asymtx_tol() { return g_asymtx_tol; }
 
 // Threads of the OpenMP loop over pixels (n <= 0: every host core).
 extern "C" void oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }

@@ -11,7 +11,7 @@
 // polarized kernel; no product code links it.  Paths are relative to the
 // reference project root (src/Components/rtms/RTSI/VLIDORT2p8p3/...).
 //
-// Parity pin: tests/test_oracle_golden.py compares this oracle with the
+// Parity pin: tests/test_oracle_golden_vector.py compares this oracle with the
 // reference's saved gfortran results vlidort_v_test/saved_results/gfortran/
 // nstokes3/results_solar_tester_IQU0.all (I, Q, U) and
 // results_solar_tester_I000.all (NSTOKES = 1 through this vector code).
@@ -931,3 +931,122 @@ int oracle_vlidort_vector_solve(const OracleOpts* o, int NS, int L, int N, int n
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// The AeroApps glue: VLIDORT_Vector_Lambert (geo_vlidort/VLIDORT_LAMBERT.F90:172-342)
+// calling VLIDORT_Init (VLIDORT2p8p3/VLIDORT_Mod.F90:65-383) and
+// VLIDORT_Run_Vector_SingleGeom (VLIDORT2p8p3/VLIDORT_ScatMod.F90:284-617) per
+// (observation, channel), NSTOKES = 3.  Arrays are Fortran column-major exactly
+// as the reference declares them; pmom(km,nch,nobs,nMom,6) holds P11, P12,
+// P33, P34, P22, P44.  alpha (km,nobs,nch) may be NULL (no gas absorption),
+// flux_factor (nch,nobs) may be NULL (1).  A pixel with MISSING angles or
+// albedo gets MISSING in all four outputs.  nfourier/status/nlay optional.
+extern "C" double oracle_get_asymtx_tol();
+extern "C" int oracle_vector_lambert(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                     const double* ROT, const double* depol, const double* alpha, const double* tau,
+                                     const double* ssa, const double* pmom, const double* he, const double* albedo,
+                                     const double* solar_zenith, const double* relat_azymuth,
+                                     const double* sensor_zenith, const double* flux_factor, double MISSING,
+                                     double* radiance, double* reflectance, double* Q, double* U, int* nfourier,
+                                     int* status, const int* nlay) {
+  if (km > 72) return 3;
+  if (nMom > 1000) return 5;
+  auto is_missing = [&](double x) { return std::fabs(x / MISSING - 1.0) < 0.001; };
+  std::vector<char> nadir(nobs, 0);  // sticky DO_FOCORR_NADIR (VLIDORT_ScatMod.F90:395-398)
+  {
+    bool flag = false;
+    for (int j = 0; j < nobs; ++j) {
+      bool geo_ok = !(is_missing(solar_zenith[j]) || is_missing(sensor_zenith[j]) || is_missing(relat_azymuth[j]));
+      if (geo_ok && solar_zenith[j] == 0.0) {
+        for (int i = 0; i < nch; ++i)
+          if (!is_missing(albedo[j + nobs * i])) { flag = true; break; }
+      }
+      nadir[j] = flag;
+    }
+  }
+  const double pi_sp = (double)(4.0f * std::atan(1.0f));
+  const double height_scale = (double)1.0e-3f;
+  const double ssa_cap = (double)0.99999f;
+  const size_t nk = (size_t)km * nch * nobs;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int p = 0; p < nobs * nch; ++p) {
+    int j = p / nch, i = p % nch;
+    size_t o = (size_t)j + (size_t)nobs * i;
+    if (nfourier) nfourier[o] = -1;
+    if (status) status[o] = 0;
+    if (is_missing(solar_zenith[j]) || is_missing(sensor_zenith[j]) || is_missing(relat_azymuth[j]) ||
+        is_missing(albedo[o])) {
+      radiance[o] = MISSING; reflectance[o] = MISSING; Q[o] = MISSING; U[o] = MISSING;
+      continue;
+    }
+    const int L = nlay ? nlay[j] : km;
+    const int G1 = nMom + 1;
+    std::vector<double> dt(L), om(L), gr((size_t)G1 * L * 16, 0.0), hg(L + 1);
+    const double dep = depol[i];
+    // Rayleigh Greek moments (VLIDORT_ScatMod.F90:446-480; SQRT(6.) is REAL*4)
+    const double gammamom2 = -(double)std::sqrt(6.0f) * (1.0 - dep) / (2.0 + dep);
+    const double alphamom2 = 6.0 * (1.0 - dep) / (2.0 + dep);
+    const double deltamom1 = 3.0 * (1.0 - 2.0 * dep) / (2.0 + dep);
+    const double raysmom2 = (1.0 - dep) / (2.0 + dep);
+    double ray[3][16] = {};
+    ray[0][0] = 1.0; ray[2][0] = raysmom2; ray[2][1] = gammamom2; ray[2][4] = gammamom2; ray[2][5] = alphamom2;
+    ray[1][15] = deltamom1;
+    for (int k = 0; k < L; ++k) {
+      double ray_l = ROT[k + (size_t)km * (j + (size_t)nobs * i)];
+      double alpha_l = alpha ? alpha[k + (size_t)km * (j + (size_t)nobs * i)] : 0.0;
+      size_t a = k + (size_t)km * (i + (size_t)nch * j);
+      double tau_l = tau[a], ssa_l = ssa[a];
+      double tau_ext = alpha_l + ray_l + tau_l;
+      double tau_scat = ray_l + ssa_l * tau_l;
+      double ssa_tot = tau_scat / tau_ext;
+      if (ssa_tot > ssa_cap) ssa_tot = ssa_cap;
+      dt[k] = tau_ext; om[k] = ssa_tot;
+      double aerswt = ssa_l * tau_l / tau_scat;
+      double rayswt = ray_l / tau_scat;
+      auto aer = [&](int l, int ent) -> double {  // aervmoms(l, k, ent): entries from pmom(:, :, 1..6)
+        if (l >= nMom) return 0.0;
+        auto pm = [&](int ip) { return pmom[a + nk * ((size_t)l + (size_t)nMom * ip)]; };
+        switch (ent) {
+          case 0: return pm(0);
+          case 1: case 4: return pm(1);
+          case 10: return pm(2);
+          case 11: return pm(3);
+          case 14: return -pm(3);
+          case 5: return pm(4);
+          case 15: return pm(5);
+        }
+        return 0.0;
+      };
+      for (int ent = 0; ent < 16; ++ent) {
+        for (int l = 0; l <= 2 && l <= nMom; ++l)
+          gr[l + G1 * (k + (size_t)L * ent)] = ray[l][ent] * rayswt + aer(l, ent) * aerswt;
+        for (int l = 3; l <= nMom; ++l) gr[l + G1 * (k + (size_t)L * ent)] = aer(l, ent) * aerswt;
+      }
+      gr[0 + G1 * (k + (size_t)L * 0)] = 1.0;
+    }
+    for (int k = 0; k <= L; ++k) hg[k] = he[k + (size_t)(km + 1) * j] * height_scale;
+    OracleOpts op;
+    op.do_focorr = 1;
+    op.do_focorr_nadir = nadir[j] ? 1 : 0;
+    op.do_focorr_outgoing = nadir[j] ? 0 : 1;
+    op.do_deltam = 1;
+    op.do_plane_parallel = plane_parallel;
+    op.do_double_convtest = 1;
+    op.nfinelayers = 3;
+    op.taylor_order = 3;
+    op.accuracy = (double)0.0001f;
+    op.asymtx_tol = oracle_get_asymtx_tol();
+    op.earth_radius = 6371.0;
+    op.flux_factor = flux_factor ? flux_factor[i + (size_t)nch * j] : 1.0;
+    double sza = solar_zenith[j], vz = sensor_zenith[j], az = relat_azymuth[j], res[3] = {0.0, 0.0, 0.0};
+    int nf = -1;
+    int rc = oracle_vlidort_vector_solve(&op, 3, L, nstreams, nMom, hg.data(), dt.data(), om.data(), gr.data(),
+                                         albedo[o], sza, 1, &vz, 1, &az, res, &nf);
+    if (nfourier) nfourier[o] = nf;
+    if (status) status[o] = rc;
+    if (rc != 0) { radiance[o] = MISSING; reflectance[o] = MISSING; Q[o] = MISSING; U[o] = MISSING; continue; }
+    radiance[o] = res[0]; Q[o] = res[1]; U[o] = res[2];
+    reflectance[o] = (pi_sp * res[0]) / (std::cos(sza * pi_sp / 180.0) * op.flux_factor);
+  }
+  return 0;
+}

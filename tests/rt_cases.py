@@ -26,3 +26,29 @@ def random_aop_case(nstreams, km, nobs, nch=2, seed=0, ssa_range=(0.8, 1.0)):
 def rt_args(c, nstreams):
     return (c["km"], c["nch"], c["ncol"], c["channels"], nstreams, False, c["nmom"], 1, c["ROT"], c["depol"], c["tau"],
             c["ssa"], c["g"], c["pmom"], c["pe"], c["he"], c["te"], c["albedo"], c["sza"], c["raa"], c["vza"])
+
+
+def vector_mie_case(nstreams, nobs, nch=2, seed=0, nlayers=72, chem_channels=(470.0, 550.0, 670.0, 865.0)):
+    """Columns from synth with the six-element Mie optics of the aerosol tracers
+    (oracle VLIDORT_getAOPvector with nPol = 6 on synthetic Lorenz-Mie tables):
+    the inputs of VLIDORT_Vector_Lambert, FP64 as the reference driver passes them."""
+    from aeroapps_gb300 import mie
+    from oracle import oracle
+    ch = list(chem_channels[:nch])
+    c = synth.make_columns(nobs, ch, seed=seed + 11, nlayers=nlayers)
+    nmom = 2 * nstreams
+    tabs = mie.generate_tables(ch, nmom=nmom, npol=6)
+    qidx = {}
+    for ti, t in enumerate(tabs.tables):
+        for b in range(t.bext.shape[2]):
+            qidx["%s%03d" % (t.name, b + 1)] = (ti, b)
+    qt, qb = zip(*[qidx[n] for n in synth.tracer_names()])
+    km = c["km"]
+    tau, ssa, g, pm, rc = oracle.get_aop_vector(tabs, km, nobs, nch, 20, np.float32(ch), qt, qb, c["qm"], c["rh"],
+                                                nmom, 6)
+    assert rc == 0
+    F = np.asfortranarray
+    c.update(tau=F(tau.astype(np.float64)), ssa=F(ssa.astype(np.float64)), g=F(g.astype(np.float64)),
+             pmom=F(pm.astype(np.float64)), nmom=nmom, tau32=tau, ssa32=ssa, pmom32=pm, tables=tabs, qt=qt, qb=qb,
+             flux=F(np.ones((nch, nobs))))
+    return c

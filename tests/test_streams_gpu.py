@@ -65,7 +65,7 @@ def test_concurrent_streams_match_serial_runs(precision):
 
 @pytest.mark.gpu
 def test_more_streams_than_scratch_pads():
-    # 11 streams over 8 pads: the least recently used pad changes hands, and
+    # 19 streams over 16 pads: the least recently used pad changes hands, and
     # the new stream waits on the device for the old stream's work
     import torch
     L = _lib.lib()
@@ -76,7 +76,7 @@ def test_more_streams_than_scratch_pads():
     torch.cuda.synchronize()
     ref = out["rad"].clone()
     outs = []
-    streams = [torch.cuda.Stream() for _ in range(11)]
+    streams = [torch.cuda.Stream() for _ in range(19)]
     for s in streams:
         o = {k: torch.zeros_like(v) for k, v in out.items()}
         assert _launch(L, c, t, o, N, s.cuda_stream, _lib.PREC_FP64) == 0, _lib.last_error()

@@ -25,8 +25,8 @@ def test_sizes_and_missing_entries():
         VLIDORT_POLAR_.scalar_lambert(*_f2py_args(c, 8), km=c["km"] + 1)
     with pytest.raises(ValueError):
         VLIDORT_POLAR_.scalar_lambert(*_f2py_args(c, 8), nmom=c["nmom"] + 1)
-    # the polarised and BRDF entries are not provided: a call fails loudly
-    for name in ("vector_lambert", "vector_brdf_modis", "vector_cx"):
+    # the BRDF, ocean and cloud entries are not provided: a call fails loudly
+    for name in ("vector_brdf_modis", "vector_cx", "vector_lambert_cloud"):
         assert not hasattr(VLIDORT_POLAR_, name)
 
 
