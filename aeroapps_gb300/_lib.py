@@ -52,9 +52,9 @@ _SIGNATURES = {
                                                       [c_void_p] * 14 + [c_double] + [c_void_p] * 5),
     "aerort_vlidort_scalar_lambert_mixed_batch": (c_int, [c_int, c_int, c_int, c_int, c_int, c_int, P_i] + [P_d] * 10 +
                                                   [c_double, P_d, P_d, P_i, P_i]),
-    "aerort_vlidort_vector_lambert": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 15 +
+    "aerort_vlidort_vector_lambert": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 14 +
                                       [c_double, c_int, P_d, P_d, P_d, P_d]),
-    "aerort_vlidort_vector_lambert_ex": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 15 +
+    "aerort_vlidort_vector_lambert_ex": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 14 +
                                          [c_double, c_int, P_d, P_d, P_d, P_d, P_i, P_i]),
     "aerort_vlidort_vector_lambert_batch_dev": (c_int, [c_int] * 6 + [c_void_p] * 16 + [c_double] + [c_void_p] * 7),
     "aerort_get_edge_vars": (c_int, [c_int, c_int, P_f, P_f, ctypes.c_float, P_f, P_f, P_f]),

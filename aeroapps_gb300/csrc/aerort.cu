@@ -1,7 +1,7 @@
 // aerort: CUDA implementation of the C ABI declared in include/aerort.h.
 //
 // Kernels
-//   k_aop<>           Mie-table RH interpolation + species mixing (FP32, one
+//   k_aop<MC>         Mie-table RH interpolation + species mixing (FP32, one
 //                     thread per output (layer, channel, pixel); HBM/L2-gather bound)
 //   k_nadir_first     sticky nadir-FO flag of the reference wrapper, as a device atomicMin
 //   k_scalar_lambert  FP64 scalar RT, one thread per (pixel, channel) solve,
@@ -196,10 +196,53 @@ struct AopMeta {
   int q_bin[kMaxTracers];
 };
 
-__global__ void k_aop(const DevMieTable* __restrict__ tabs, int km, int nobs, int nch, int nq, const AopMeta meta,
-                      const float* __restrict__ qm, const float* __restrict__ rh, int nMom, int nPol,
-                      float* __restrict__ tau, float* __restrict__ ssa, float* __restrict__ g,
-                      float* __restrict__ pmom) {
+// One tracer's contribution at one output element: its table, the two RH rows
+// b0, b1, the interpolation weights, and tau, ssa of the tracer
+// (Chem_MieQueryByInt, Chem_MieMod.F90:860-905, and VLIDORT_MieMod.F90:291-318).
+struct TracerRow {
+  const DevMieTable* T;
+  int b0, b1;
+  float arh, w0, tau, ssa;
+};
+
+// Fills r for tracer iq; false for a tracer without optics (q_table < 0).
+// Recomputed in every pass of k_aop instead of kept in per-thread arrays:
+// the same operations in the same order give the same bits each time.
+__device__ __forceinline__ bool tracer_row(const DevMieTable* __restrict__ tabs, const AopMeta& meta, int iq,
+                                           int ich, int isnap, float qmv, TracerRow& r) {
+  const int tb = meta.q_table[iq];
+  if (tb < 0) return false;
+  const DevMieTable& T = tabs[tb];
+  r.T = &T;
+  r.arh = T.rha[isnap - 1];
+  const int irh = T.rhi[isnap - 1];
+  const int irhp1 = irh + 1 > T.nrh ? T.nrh : irh + 1;
+  const int row = T.nrh * (ich + T.nch * meta.q_bin[iq]);
+  r.b0 = (irh - 1) + row;
+  r.b1 = (irhp1 - 1) + row;
+  r.w0 = __fsub_rn(1.0f, r.arh);
+  const float bext = lerp_ref(T.bext[r.b0], T.bext[r.b1], r.w0, r.arh);
+  const float bsca = lerp_ref(T.bsca[r.b0], T.bsca[r.b1], r.w0, r.arh);
+  r.tau = __fmul_rn(bext, qmv);
+  r.ssa = __fdiv_rn(bsca, bext);
+  return true;
+}
+
+// VLIDORT_getAOPvector (VLIDORT_MieMod.F90:124-336) with Chem_MieQuery per
+// tracer, one thread per output element (layer fastest, so the qm, rh reads
+// and every output store are coalesced).  Nothing is kept per tracer: a
+// first pass sums tau, ssa, g over the tracers; then, per chunk of MC
+// moments and per group of scattering-matrix elements, a pass over the
+// tracers accumulates the moments in registers.  Elements that the
+// reference couples travel together: for a four-element (spherical) table
+// under nPol = 6 the reference sets P22 to the P11 sum and P44 to the P33
+// sum after that tracer, so (P11, P22) and (P33, P44) share a pass.
+template <int MC>
+__global__ void __launch_bounds__(256) k_aop(const DevMieTable* __restrict__ tabs, int km, int nobs, int nch, int nq,
+                                             const AopMeta meta, const float* __restrict__ qm,
+                                             const float* __restrict__ rh, int nMom, int nPol,
+                                             float* __restrict__ tau, float* __restrict__ ssa,
+                                             float* __restrict__ g, float* __restrict__ pmom) {
   const long total = (long)km * nch * nobs;
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
@@ -207,65 +250,85 @@ __global__ void k_aop(const DevMieTable* __restrict__ tabs, int km, int nobs, in
   const long r = t / km;
   const int n = (int)(r % nch);
   const int i = (int)(r / nch);
-  const int* q_table = meta.q_table;
-  const int* q_bin = meta.q_bin;
   const int ich = meta.idxch[n];
   const float rhv = rh[k + (long)km * i];
   // RH snapping (Chem_MieMod.F90:860-867); the max(rh,0) result is discarded there too
   const float rhUse = fminf(rhv, 0.99f);
   int isnap = (int)__fmul_rn(__fadd_rn(rhUse, 0.001f), 1000.0f);
   if (isnap < 1) isnap = 1;
-  float tq[kMaxTracers], sq[kMaxTracers], aq[kMaxTracers];
-  int b0q[kMaxTracers], b1q[kMaxTracers];
+  const float* qcol = qm + k + (long)km * (long)nq * i;
   float ts = 0.0f, ss = 0.0f, gs = 0.0f;
   for (int iq = 0; iq < nq; ++iq) {
-    const int tb = q_table[iq];
-    if (tb < 0) continue;
-    const DevMieTable& T = tabs[tb];
-    const float arh = T.rha[isnap - 1];
-    const int irh = T.rhi[isnap - 1];
-    const int irhp1 = irh + 1 > T.nrh ? T.nrh : irh + 1;
-    const int b0 = (irh - 1) + T.nrh * (ich + T.nch * q_bin[iq]);
-    const int b1 = (irhp1 - 1) + T.nrh * (ich + T.nch * q_bin[iq]);
-    const float w0 = __fsub_rn(1.0f, arh);
-    const float bext = lerp_ref(T.bext[b0], T.bext[b1], w0, arh);
-    const float bsca = lerp_ref(T.bsca[b0], T.bsca[b1], w0, arh);
-    const float gg = lerp_ref(T.g[b0], T.g[b1], w0, arh);
-    const float tau_ = __fmul_rn(bext, qm[k + (long)km * (iq + (long)nq * i)]);
-    const float ssa_ = __fdiv_rn(bsca, bext);
-    ts = __fadd_rn(ts, tau_);
-    ss = __fadd_rn(ss, __fmul_rn(ssa_, tau_));
-    gs = __fadd_rn(gs, __fmul_rn(__fmul_rn(gg, ssa_), tau_));
-    tq[iq] = tau_; sq[iq] = ssa_; aq[iq] = arh; b0q[iq] = b0; b1q[iq] = b1;
+    TracerRow q;
+    if (!tracer_row(tabs, meta, iq, ich, isnap, qcol[(long)km * iq], q)) continue;
+    const float gg = lerp_ref(q.T->g[q.b0], q.T->g[q.b1], q.w0, q.arh);
+    ts = __fadd_rn(ts, q.tau);
+    ss = __fadd_rn(ss, __fmul_rn(q.ssa, q.tau));
+    gs = __fadd_rn(gs, __fmul_rn(__fmul_rn(gg, q.ssa), q.tau));
   }
   // normalisation (VLIDORT_MieMod.F90:320-334)
   const float ssa_out = ts > 0.0f ? __fdiv_rn(ss, ts) : ss;
   const float st = __fmul_rn(ssa_out, ts);
   const float g_out = st > 0.0f ? __fdiv_rn(gs, st) : gs;
   const long o = k + (long)km * (n + (long)nch * i);
-  tau[o] = ts; ssa[o] = ssa_out; g[o] = g_out;
+  tau[o] = ts;
+  ssa[o] = ssa_out;
+  g[o] = g_out;
   const long stride = total;
-  for (int im = 0; im < nMom; ++im) {
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int iq = 0; iq < nq; ++iq) {
-      const int tb = q_table[iq];
-      if (tb < 0) continue;
-      const DevMieTable& T = tabs[tb];
-      const bool sph = (nPol == 6 && T.npol == 4);
-      const int np_ = sph ? 4 : nPol;
-      const float arh = aq[iq], w0 = __fsub_rn(1.0f, arh);
-      const long s = (long)T.nrh * T.nch * T.nbin;
-      for (int ip = 0; ip < np_; ++ip) {
-        const long oo = (long)(im + T.nmom * ip) * s;
-        const float p = lerp_ref(T.pmom[oo + b0q[iq]], T.pmom[oo + b1q[iq]], w0, arh);
-        acc[ip] = __fadd_rn(acc[ip], __fmul_rn(__fmul_rn(p, sq[iq]), tq[iq]));
+  // element groups: (first, partner or -1); the partner is the element a
+  // spherical table copies from `first` under nPol = 6
+  const int ngroups = nPol == 6 ? 4 : nPol;
+  for (int grp = 0; grp < ngroups; ++grp) {
+    const int ea = grp;
+    const int eb = nPol == 6 ? (grp == 0 ? 4 : (grp == 2 ? 5 : -1)) : -1;
+    for (int m0 = 0; m0 < nMom; m0 += MC) {
+      const int mc = nMom - m0 < MC ? nMom - m0 : MC;
+      float a[MC], b[MC];
+#pragma unroll
+      for (int j = 0; j < MC; ++j) { a[j] = 0.0f; b[j] = 0.0f; }
+      for (int iq = 0; iq < nq; ++iq) {
+        TracerRow q;
+        if (!tracer_row(tabs, meta, iq, ich, isnap, qcol[(long)km * iq], q)) continue;
+        const DevMieTable& T = *q.T;
+        const bool sph = (nPol == 6 && T.npol == 4);
+        const long s = (long)T.nrh * T.nch * T.nbin;
+        const float* pa = T.pmom + (long)(m0 + T.nmom * ea) * s;
+#pragma unroll
+        for (int j = 0; j < MC; ++j) {
+          if (j < mc) {
+            const float p = lerp_ref(pa[(long)j * s + q.b0], pa[(long)j * s + q.b1], q.w0, q.arh);
+            a[j] = __fadd_rn(a[j], __fmul_rn(__fmul_rn(p, q.ssa), q.tau));
+          }
+        }
+        if (eb >= 0) {
+          if (sph) {
+#pragma unroll
+            for (int j = 0; j < MC; ++j) b[j] = a[j];
+          } else {
+            const float* pb = T.pmom + (long)(m0 + T.nmom * eb) * s;
+#pragma unroll
+            for (int j = 0; j < MC; ++j) {
+              if (j < mc) {
+                const float p = lerp_ref(pb[(long)j * s + q.b0], pb[(long)j * s + q.b1], q.w0, q.arh);
+                b[j] = __fadd_rn(b[j], __fmul_rn(__fmul_rn(p, q.ssa), q.tau));
+              }
+            }
+          }
+        }
       }
-      if (sph) { acc[4] = acc[0]; acc[5] = acc[2]; }
-    }
-    for (int ip = 0; ip < nPol; ++ip) {
-      float v = acc[ip];
-      if (st > 0.0f) v = __fdiv_rn(v, st);
-      pmom[o + stride * (im + (long)nMom * ip)] = v;
+#pragma unroll
+      for (int j = 0; j < MC; ++j) {
+        if (j < mc) {
+          float v = a[j];
+          if (st > 0.0f) v = __fdiv_rn(v, st);
+          pmom[o + stride * (m0 + j + (long)nMom * ea)] = v;
+          if (eb >= 0) {
+            float w = b[j];
+            if (st > 0.0f) w = __fdiv_rn(w, st);
+            pmom[o + stride * (m0 + j + (long)nMom * eb)] = w;
+          }
+        }
+      }
     }
   }
 }
@@ -387,9 +450,10 @@ int aop_launch(aerort_mie* mie, int km, int nobs, int nch, int nq, const std::ve
   for (int q = 0; q < nq; ++q) { meta.q_table[q] = q_table[q]; meta.q_bin[q] = q_bin[q]; }
   long total = (long)km * nch * nobs;
   if (total == 0) return 0;
-  int bs = 128;
-  long nb = (total + bs - 1) / bs;
-  k_aop<<<(unsigned)nb, bs, 0, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, tau, ssa, g, pmom);
+  const int bs = 256;
+  const long nb = (total + bs - 1) / bs;
+  k_aop<16><<<(unsigned)nb, bs, 0, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, tau, ssa, g,
+                                        pmom);
   CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;

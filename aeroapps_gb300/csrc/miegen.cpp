@@ -195,7 +195,11 @@ int aerort_miegen_lognormal_pol(int nlam, const double* lam_um, int nrh, const d
                                 double rho_dry, int nmom, int npol, int nradii, float* bext, float* bsca, float* g,
                                 float* pmom) {
   if (nlam <= 0 || nrh <= 0 || nbin <= 0 || nmom < 1 || nradii < 8 || (npol != 1 && npol != 6)) return 1;
-  const int na = 2 * nmom + 32;
+  // angular quadrature of the moment integrals: fixed at 512 nodes (up to
+  // 240 moments), so a table's first moments do not depend on how many it
+  // holds, and fine enough for the diffraction peak of the largest wet
+  // particles (size parameter ~270 at 470 nm)
+  const int na = std::max(2 * nmom + 32, 512);
   std::vector<double> mu(na), wa(na);
   gauss_legendre(na, mu.data(), wa.data());
   // common dry-radius grid covering +-3 sigma of every bin

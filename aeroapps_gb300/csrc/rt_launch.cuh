@@ -67,8 +67,7 @@ template <int NS, typename T, int WPB>
 // warps, <= 128 registers) up to 8 streams, 6 blocks (12 warps, <= 170
 // registers) above, where 128 registers would spill (measured on GB300).
 __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 8 ? 8 : 6) : 1) k_scalar_lambert_team(RtOptions opt, LambertInputs in, Quad q,
-                                                                   void* scratch, long nthreads, T* sweep,
-                                                                   long sweep_per_warp, int nsolve, int chunk,
+                                                                   void* scratch, long nthreads, int nsolve, int chunk,
                                                                    int* counter, double* rad, double* refl, int* nf,
                                                                    int* st, Worklist wl) {
   extern __shared__ __align__(16) unsigned char team_smem[];
@@ -76,7 +75,6 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 
   TeamMem<NS, T>& M = reinterpret_cast<TeamMem<NS, T>*>(team_smem)[threadIdx.x >> 5];
   const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long tid0 = tid - lane;
-  T* sw = sweep + (tid >> 5) * sweep_per_warp;
   const ScratchLayout<NS> lay(in.km, false);
   const SolveScratch<T> S = make_scratch<NS, T>(scratch, tid, nthreads, in.km, false);
   const Team tm{lane, nullptr, nullptr};
@@ -113,7 +111,7 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 
       SetupRecord rb;
       rb.load(Sb.D, lay.rec);
       const int sb = __shfl_sync(0xffffffffu, sidx, b);
-      team_fourier_series<NS, T>(tm, M, opt, in, rb, q.qx, q.qw, Sb.W, lay, sw, rad, refl, nf, st, wl, sb);
+      team_fourier_series<NS, T>(tm, M, opt, in, rb, q.qx, q.qw, Sb.W, lay, rad, refl, nf, st, wl, sb);
     }
   }
 }
@@ -146,14 +144,11 @@ __global__ void __launch_bounds__(32) k_team_setup(RtOptions opt, LambertInputs 
 // 12-stream series kernel also fits 128 registers (16 warps per SM, no spills).
 template <int NS, typename T, int WPB>
 __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 12 ? 8 : 6) : 1)
-    k_team_series(RtOptions opt, LambertInputs in, Quad q, void* scratch, int base, int count, T* sweep,
-                  long sweep_per_warp, int* counter, const unsigned char* live, double* rad, double* refl, int* nf,
-                  int* st, Worklist wl) {
+    k_team_series(RtOptions opt, LambertInputs in, Quad q, void* scratch, int base, int count, int* counter,
+                  const unsigned char* live, double* rad, double* refl, int* nf, int* st, Worklist wl) {
   extern __shared__ __align__(16) unsigned char team_smem[];
   const int lane = threadIdx.x & 31;
   TeamMem<NS, T>& M = reinterpret_cast<TeamMem<NS, T>*>(team_smem)[threadIdx.x >> 5];
-  const long warp = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  T* sw = sweep + warp * sweep_per_warp;
   const ScratchLayout<NS> lay(in.km, false);
   const Team tm{lane, nullptr, nullptr};
   for (;;) {
@@ -165,20 +160,19 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 
     const SolveScratch<T> S = make_scratch<NS, T>(scratch, s, count, in.km, false);
     SetupRecord r;
     r.load(S.D, lay.rec);
-    team_fourier_series<NS, T>(tm, M, opt, in, r, q.qx, q.qw, S.W, lay, sw, rad, refl, nf, st, wl, base + s);
+    team_fourier_series<NS, T>(tm, M, opt, in, r, q.qx, q.qw, S.W, lay, rad, refl, nf, st, wl, base + s);
   }
 }
 
 // Enqueue the two-pass team solve on storage at `base`: per-solve scratch for
-// `slice` solves, their live flags at live_off, the per-warp sweep regions at
-// sweep_off (nblocks x 2 warps); counter and first are two scheduling ints.
+// `slice` solves and their live flags at live_off; counter and first are two
+// scheduling ints.
 template <int NS, typename T>
 int enqueue_team_two_pass(const RtOptions& opt, const LambertInputs& in, const Quad& q, char* base, size_t live_off,
-                          size_t sweep_off, long nblocks, int slice, int* counter, int* first, double* rad,
-                          double* refl, int* nf, int* st, cudaStream_t s, const Worklist& wl) {
+                          long nblocks, int slice, int* counter, int* first, double* rad, double* refl, int* nf,
+                          int* st, cudaStream_t s, const Worklist& wl) {
   constexpr int WPB = 2;
   const int nsolve = in.nobs * in.nch;
-  const SweepLayout<NS> swl(in.km);
   const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
   k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
   k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo, in.missing,
@@ -193,8 +187,7 @@ int enqueue_team_two_pass(const RtOptions& opt, const LambertInputs& in, const Q
     k_team_setup<NS, T><<<(unsigned)((cnt + 31) / 32), 32, 0, s>>>(opt, in2, q, base, b0, cnt, rad, refl, nf, st,
                                                                    (unsigned char*)(base + live_off));
     k_team_series<NS, T, WPB><<<(unsigned)nblocks, 32 * WPB, smem, s>>>(
-        opt, in2, q, base, b0, cnt, (T*)(base + sweep_off), swl.total, counter,
-        (const unsigned char*)(base + live_off), rad, refl, nf, st, wl);
+        opt, in2, q, base, b0, cnt, counter, (const unsigned char*)(base + live_off), rad, refl, nf, st, wl);
     CUDA_TRY(cudaGetLastError());
     count_launches(2);
   }
@@ -233,16 +226,13 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
     long nblocks = (long)per_sm * c.num_sms;
     if (nblocks > (slice + WPB - 1) / WPB) nblocks = (slice + WPB - 1) / WPB;
     const ScratchLayout<NS> lay(in.km, false);
-    const SweepLayout<NS> swl(in.km);
     auto up256 = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t live_off = up256((size_t)lay.template bytes<T>() * slice);
-    const size_t sweep_off = live_off + up256((size_t)slice);
-    const size_t sweep_bytes = sizeof(T) * (size_t)swl.total * (size_t)(nblocks * WPB);
-    if (int rc = c.pad->scratch.ensure(sweep_off + sweep_bytes)) return rc;
+    if (int rc = c.pad->scratch.ensure(live_off + up256((size_t)slice))) return rc;
     if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
     int* counter = (int*)c.pad->counter.p;
-    return enqueue_team_two_pass<NS, T>(opt, in, q, (char*)c.pad->scratch.p, live_off, sweep_off, nblocks, slice,
-                                        counter, counter + 1, rad, refl, nf, st, s, wl);
+    return enqueue_team_two_pass<NS, T>(opt, in, q, (char*)c.pad->scratch.p, live_off, nblocks, slice, counter,
+                                        counter + 1, rad, refl, nf, st, s, wl);
   }
   CUDA_TRY(cudaFuncSetAttribute(k_scalar_lambert_team<NS, T, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
@@ -259,11 +249,7 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
                                                                                 : (nsolve + WPB - 1) / WPB;
   const long nthreads = nblocks * bs;
   const ScratchLayout<NS> lay(in.km, false);
-  const SweepLayout<NS> swl(in.km);
-  const size_t thread_bytes = (size_t)lay.template bytes<T>() * nthreads;
-  const size_t sweep_off = (thread_bytes + 255) / 256 * 256;
-  const size_t sweep_bytes = sizeof(T) * (size_t)swl.total * (nthreads / 32);
-  if (int rc = c.pad->scratch.ensure(sweep_off + sweep_bytes)) return rc;
+  if (int rc = c.pad->scratch.ensure((size_t)lay.template bytes<T>() * nthreads)) return rc;
   if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
   int* counter = (int*)c.pad->counter.p;
   int* first = counter + 1;
@@ -273,10 +259,9 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   CUDA_TRY(cudaGetLastError());
   LambertInputs in2 = in;
   in2.nadir_first = first;
-  T* sweep = (T*)((char*)c.pad->scratch.p + sweep_off);
   k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, bs, smem, s>>>(opt, in2, q, c.pad->scratch.p, nthreads,
-                                                                        sweep, swl.total, nsolve, chunk, counter, rad,
-                                                                        refl, nf, st, wl);
+                                                                        nsolve, chunk, counter, rad, refl, nf, st,
+                                                                        wl);
   CUDA_TRY(cudaGetLastError());
   count_launches(3);
   return 0;
@@ -340,11 +325,9 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
     long nblocks = (long)per_sm * num_sms;
     if (nblocks > ((long)nsolve + WPB - 1) / WPB) nblocks = ((long)nsolve + WPB - 1) / WPB;
     const ScratchLayout<NS> lay(in.km, false);
-    const SweepLayout<NS> swl(in.km);
     auto up256 = [](size_t b) { return (b + 255) / 256 * 256; };
-    const size_t sweep_bytes = up256(sizeof(T) * (size_t)swl.total * (size_t)(nblocks * WPB));
     const size_t per_solve = (size_t)lay.template bytes<T>() + 1;
-    long fit = arena_bytes > sweep_bytes + 1024 ? (long)((arena_bytes - sweep_bytes - 1024) / per_solve) : 0;
+    long fit = arena_bytes > 1024 ? (long)((arena_bytes - 1024) / per_solve) : 0;
     long slice = nsolve < kSetupSlice ? nsolve : kSetupSlice;
     if (slice > fit) slice = fit;
     if (slice >= nsolve || slice >= 2 * nblocks * WPB) {
@@ -353,17 +336,15 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
       gauss_legendre01(NS, q.qx, q.qw);
       if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
       const size_t live_off = up256((size_t)lay.template bytes<T>() * slice);
-      const size_t sweep_off = live_off + up256((size_t)slice);
-      return enqueue_team_two_pass<NS, T>(opt, in, q, (char*)arena, live_off, sweep_off, nblocks, (int)slice, sched,
-                                          sched + 1, rad, refl, nf, st, s, wl);
+      return enqueue_team_two_pass<NS, T>(opt, in, q, (char*)arena, live_off, nblocks, (int)slice, sched, sched + 1,
+                                          rad, refl, nf, st, s, wl);
     }
   }
   if (sc.kernel == 1) {
-    // fused team kernel: per warp 32 set-up scratches + one sweep region, all inside the arena
+    // fused team kernel: per warp 32 set-up scratches inside the arena
     constexpr int WPB = 2;
     const ScratchLayout<NS> tlay(in.km, false);
-    const SweepLayout<NS> swl(in.km);
-    const size_t per_warp = 32 * (size_t)tlay.template bytes<T>() + sizeof(T) * (size_t)swl.total + 256;
+    const size_t per_warp = 32 * (size_t)tlay.template bytes<T>();
     const long fit_blocks_t = (long)(arena_bytes / (per_warp * WPB));
     if (fit_blocks_t < 1)
       return set_error(AERORT_RC_ARG, "scalar_lambert: one team block needs more scratch than the workspace holds");
@@ -384,7 +365,6 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
     const int chunk = team_chunk(wl.in_list ? 1 : nsolve, resident, WPB, &nblocks);
     if (wl.in_list) nblocks = resident < (nsolve + WPB - 1) / WPB ? resident : (nsolve + WPB - 1) / WPB;
     const long nthreads = nblocks * 32 * WPB;
-    const size_t sweep_off = ((size_t)tlay.template bytes<T>() * nthreads + 255) / 256 * 256;
     int* counter = sched;
     int* first = sched + 1;
     k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
@@ -394,8 +374,7 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
     LambertInputs in2 = in;
     in2.nadir_first = first;
     k_scalar_lambert_team<NS, T, WPB><<<(unsigned)nblocks, 32 * WPB, smem, s>>>(
-        opt, in2, q, arena, nthreads, (T*)((char*)arena + sweep_off), swl.total, nsolve, chunk, counter, rad, refl,
-        nf, st, wl);
+        opt, in2, q, arena, nthreads, nsolve, chunk, counter, rad, refl, nf, st, wl);
     CUDA_TRY(cudaGetLastError());
     count_launches(3);
     return 0;

@@ -18,7 +18,7 @@ namespace aerort_internal {
 // 256 MiB of FP64 scratch.  One 32-thread block of the thread-per-solve RT
 // kernel needs 32 x ScratchLayout(km).total doubles (about 11 MiB at 16
 // streams and 72 layers), one two-warp block of the team kernel 64 set-up
-// scratches plus two sweep regions, so every supported (nstreams, km) fits;
+// scratches, so every supported (nstreams, km) fits;
 // the grid is capped to what the arena holds, which bounds throughput at
 // large stream counts.
 constexpr size_t kArenaDoubles = (size_t)32 << 20;

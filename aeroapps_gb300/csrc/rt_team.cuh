@@ -160,6 +160,8 @@ struct TeamMem {
   alignas(16) T work[NWORK];         // eigen phase: Sp Bs H G V | interface system
   T kv[NS], norm[NS], uhd[NS], uhu[NS], hm1[NS], hm2[NS], gup[NS], gdn[NS], dpi[NS], dmi[NS], rv[NS];
   T rbeta;
+  T la[NS], lb[NS], ls;              // source coefficients a, b, s of the current layer
+  T adj[NS];                         // TOA source per unit of the current layer's M (adjoint of the sweep)
   T P[2][NS * LD], Q[2][NS * LD];    // layer solutions (prev / cur)
   T t[2][NS], wt[2][2 * NS], wb[2][2 * NS];
   T F[NS * LD], f[NS];               // L = F M + f of the current interface
@@ -168,20 +170,6 @@ struct TeamMem {
   int vp_valid;
   T red[2 * kTeam];
   int flag;
-};
-
-// Per-solve sweep storage in global memory (one region per warp, contiguous,
-// element-parallel access): F_n, f_n, C_n, c_n, a_n, b_n, s_n for every layer.
-template <int NS>
-struct SweepLayout {
-  long F, f, C, c, a, b, s, total;
-  RT_HD explicit SweepLayout(int L) {
-    long o = 0;
-    F = o; o += (long)NS * NS * L; f = o; o += (long)NS * L;
-    C = o; o += (long)NS * NS * L; c = o; o += (long)NS * L;
-    a = o; o += (long)NS * L; b = o; o += (long)NS * L; s = o; o += L;
-    total = o;
-  }
 };
 
 // ---------------------------------------------------------------------------------- dense steps
@@ -617,10 +605,10 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
 }
 
 // Layer n of term m: eigen-solution, multipliers, Green's particular solution,
-// source coefficients a, b, s into the sweep storage (layer_solution).
+// source coefficients a, b, s of the layer into M.la, M.lb, M.ls (layer_solution).
 template <int NS, typename T>
 RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T>& c, const RtOptions& opt,
-                              int m, int n, bool laysc, int cur, T* sw, const SweepLayout<NS>& swl) {
+                              int m, int n, bool laysc, int cur) {
   constexpr int LD = TeamMem<NS, T>::LD;
   const int N = NS, NM = c.NM;
   int st = team_layer_eigen<NS, T>(tm, M, c, m, cur);
@@ -639,8 +627,8 @@ RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<
       if (fabs(rho_m) < kTaylorSmall) M.hm1[a] = taylor1<T>(opt.taylor_order, rho_m, dtau, tuser, smu);
       else M.hm1[a] = smu * (zdel - tuser) * (1.0 / rho_m);
     }
-    sw[swl.a + a + N * (long)n] = M.uhd[a] * M.hm2[a];
-    sw[swl.b + a + N * (long)n] = M.uhu[a] * M.hm1[a];
+    M.la[a] = M.uhd[a] * M.hm2[a];
+    M.lb[a] = M.uhu[a] * M.hm1[a];
   }
   for (int e = tm.lane; e < 2 * N; e += kTeam) { M.wt[cur][e] = 0; M.wb[cur][e] = 0; }
   tm.sync();
@@ -781,19 +769,28 @@ RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<
       spart += upar * emult;
     }
   }
-  if (tm.lane == 0) sw[swl.s + n] = laysc ? spart : (T)0;
+  if (tm.lane == 0) M.ls = laysc ? spart : (T)0;
   tm.sync();
   return RT_OK;
 }
 
 // One Fourier term (fourier_term): layer solutions, block interface sweep,
-// surface closure, bottom-up recovery with the TOA source recursion.
-// Per-layer inputs come from the set-up thread's scratch W; the sweep arrays
-// live in sw.  Every lane returns the same status and *out.
+// surface closure, TOA source.  Per-layer inputs come from the set-up
+// thread's scratch W.
+//
+// The sweep leaves, per interface, M_{n-1} = c_{n-1} + C_{n-1} M_n and
+// L_n = f_n + F_n M_n, and the TOA source is the recursion
+// cum_n = s_n + a_n.L_n + b_n.M_n + tuser_n cum_{n+1} (the back-substitution
+// and UPUSER_INTENSITY of the reference).  That value is linear in the
+// M_n, so it is accumulated top-down during the sweep instead:
+//   out = sum_n T_n (s_n + a_n.f_n) + sum_{n<L-1} v_n.c_n + v_{L-1}.M_{L-1} + T_L cum_L,
+//   v_n = C_{n-1}^T v_{n-1} + T_n (F_n^T a_n + b_n),   T_n = prod_{k<n} tuser_k,
+// with cum_L the surface term.  Nothing per layer is stored, so the term's
+// memory traffic is its inputs W alone.  Every lane returns the same status
+// and *out.
 template <int NS, typename T>
 RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& c, const RtOptions& opt, int m,
-                            const ScratchT<T>& W, const ScratchLayout<NS>& lay, T* sw, const SweepLayout<NS>& swl,
-                            T* out) {
+                            const ScratchT<T>& W, const ScratchLayout<NS>& lay, T* out) {
   constexpr int LD = TeamMem<NS, T>::LD;
   constexpr int LR = TeamMem<NS, T>::LR;
   const int N = NS, NM = c.NM, L = c.L;
@@ -811,6 +808,8 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
   T* K = M.work;  // interface systems, row-major (team_lu_solve)
   int cur = 1, prev = 0;
   if (tm.lane == 0) M.vp_valid = 0;
+  for (int i = tm.lane; i < N; i += kTeam) M.adj[i] = 0;
+  T acc = 0, tcum = 1;  // the TOA source so far and T_n (every lane the same)
   tm.sync();
   for (int n = 0; n < L; ++n) {
     // per-layer inputs of layer n
@@ -821,7 +820,7 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
     }
     tm.sync();
     const bool lsc = (m < 3) || ((T)m <= M.lsc[7]);
-    int st = team_layer_solution<NS, T>(tm, M, c, opt, m, n, lsc, cur, sw, swl);
+    int st = team_layer_solution<NS, T>(tm, M, c, opt, m, n, lsc, cur);
     if (st != RT_OK) return st;
     if (n == 0) {
       const int nb = rhs_col(N);
@@ -836,9 +835,8 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
       for (int e = tm.lane; e < N * N; e += kTeam) {
         const int i = e % N, j = e / N;
         M.F[i + LD * j] = K[LR * i + nb + j];
-        sw[swl.F + i + NS * j + (long)NS * NS * n] = K[LR * i + nb + j];
       }
-      for (int i = tm.lane; i < N; i += kTeam) { M.f[i] = K[LR * i + nb + N]; sw[swl.f + i + NS * (long)n] = M.f[i]; }
+      for (int i = tm.lane; i < N; i += kTeam) M.f[i] = K[LR * i + nb + N];
       tm.sync();
     } else {
       const int nb = rhs_col(2 * N);
@@ -894,19 +892,33 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
       }
       tm.sync();
       if (!team_lu_solve<LR>(tm, 2 * N, K, N + 1, M.red)) return RT_BVP_SINGULAR;
-      const long oC = swl.C + (long)NS * NS * (n - 1), oc = swl.c + (long)NS * (n - 1);
-      const long oF = swl.F + (long)NS * NS * n, of = swl.f + (long)NS * n;
+      // through M_{n-1} = c_{n-1} + C_{n-1} M_n (C, c in the upper rows of the solution)
+      T d = 0;
+      for (int k = 0; k < N; ++k) d += M.adj[k] * K[LR * k + nb + N];
+      acc += d;
+      T vn = 0;
+      if (tm.lane < N)
+        for (int i = 0; i < N; ++i) vn += M.adj[i] * K[LR * i + nb + tm.lane];
       for (int e = tm.lane; e < N * N; e += kTeam) {
         const int i = e % N, j = e / N;
-        sw[oC + i + NS * j] = K[LR * i + nb + j];
         M.F[i + LD * j] = K[LR * (N + i) + nb + j];
-        sw[oF + i + NS * j] = K[LR * (N + i) + nb + j];
       }
-      for (int i = tm.lane; i < N; i += kTeam) {
-        sw[oc + i] = K[LR * i + nb + N];
-        M.f[i] = K[LR * (N + i) + nb + N];
-        sw[of + i] = M.f[i];
+      for (int i = tm.lane; i < N; i += kTeam) M.f[i] = K[LR * (N + i) + nb + N];
+      tm.sync();
+      if (tm.lane < N) M.adj[tm.lane] = vn;
+    }
+    // source of layer n: T_n (s_n + a_n.(f_n + F_n M_n) + b_n.M_n)
+    {
+      T d = M.ls;
+      for (int k = 0; k < N; ++k) d += M.la[k] * M.f[k];
+      acc += tcum * d;
+      if (tm.lane < N) {
+        const int k = tm.lane;
+        T v = M.lb[k];
+        for (int i = 0; i < N; ++i) v += M.F[i + LD * k] * M.la[i];
+        M.adj[k] += tcum * v;
       }
+      tcum *= M.lsc[2];
       tm.sync();
     }
     prev = cur;
@@ -944,10 +956,9 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
   }
   tm.sync();
   if (!team_lu_solve<LR>(tm, N, K, 1, M.red)) return RT_BVP_SINGULAR;
-  // Mc in the solved right-hand side, Lc in M.gup, Mn in M.gdn
+  // M_{L-1} (Mc) from the solved right-hand side, L_{L-1} (Lc) in M.gup
   T* Mc = M.hm1;
   T* Lc = M.gup;
-  T* Mn = M.gdn;
   if (tm.lane < N) Mc[tm.lane] = K[LR * tm.lane + nbc];
   tm.sync();
   if (tm.lane < N) {
@@ -973,37 +984,11 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
     if (incl_directrf) cum += direct_beam;
     tm.sync();
   }
-  for (int n = L - 1; n >= 0; --n) {
-    if (n < L - 1) {
-      const long oC = swl.C + (long)NS * NS * n, oc = swl.c + (long)NS * n;
-      const long oF = swl.F + (long)NS * NS * n, of = swl.f + (long)NS * n;
-      if (tm.lane < N) {
-        const int i = tm.lane;
-        T s = sw[oc + i];
-        for (int k = 0; k < N; ++k) s += sw[oC + i + NS * k] * Mc[k];
-        Mn[i] = s;
-      }
-      tm.sync();
-      if (tm.lane < N) {
-        const int i = tm.lane;
-        T s = sw[of + i];
-        for (int k = 0; k < N; ++k) s += sw[oF + i + NS * k] * Mn[k];
-        Lc[i] = s;
-        Mc[i] = Mn[i];
-      }
-      tm.sync();
-    }
-    if (tm.lane < N) {
-      const int k = tm.lane;
-      M.red[k] = Lc[k] * sw[swl.a + k + N * (long)n] + Mc[k] * sw[swl.b + k + N * (long)n];
-    }
-    tm.sync();
-    T src = sw[swl.s + n];
-    for (int k = 0; k < N; ++k) src += M.red[k];
-    cum = src + W[lay.tuser + n] * cum;
-    tm.sync();
-  }
-  *out = delta_factor * cum;
+  T d = 0;
+  for (int k = 0; k < N; ++k) d += M.adj[k] * Mc[k];
+  const T total = acc + d + tcum * cum;
+  tm.sync();
+  *out = delta_factor * total;
   return RT_OK;
 }
 
@@ -1012,7 +997,7 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
 template <int NS, typename T>
 RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOptions& opt, const LambertInputs& in,
                                const SetupRecord& r, const double* qx, const double* qw, const ScratchT<T>& W,
-                               const ScratchLayout<NS>& lay, T* sw, double* radiance, double* reflectance,
+                               const ScratchLayout<NS>& lay, double* radiance, double* reflectance,
                                int* nfourier, int* status, const Worklist& wl = Worklist(), int sidx = 0) {
   SolveCtx<NS, T> c;
   make_ctx<NS, T>(r, qx, qw, c);
@@ -1026,12 +1011,11 @@ RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOption
   }
   if (tm.lane == 0) { M.pimu = 0; M.pim0 = 0; }
   tm.sync();
-  const SweepLayout<NS> swl(r.L);
   FourierSum sum;
   int m = 0, st = RT_OK;
   for (m = 0; m <= r.n_fouriers; ++m) {
     T sf = 0;
-    st = team_fourier_term<NS, T>(tm, M, c, opt, m, W, lay, sw, swl, &sf);
+    st = team_fourier_term<NS, T>(tm, M, c, opt, m, W, lay, &sf);
     if (st != RT_OK || sum.add(opt, r, m, (double)sf)) break;
   }
   if (tm.lane == 0) {

@@ -74,7 +74,7 @@ def generate_tables(channels_nm, nmom=64, nrh=NRH, nradii=160, use_cache=True, n
     if npol not in (1, 6):
         raise ValueError("npol must be 1 or 6")
     channels_nm = np.asarray(channels_nm, dtype=np.float64)
-    ident = (channels_nm.tolist(), nmom, nrh, nradii, SPECIES, BIN_RG_UM, BIN_SIGMA)
+    ident = (channels_nm.tolist(), nmom, nrh, nradii, SPECIES, BIN_RG_UM, BIN_SIGMA, "quad512")
     if npol != 1:
         ident = ident + (npol,)
     key = hashlib.sha256(repr(ident).encode()).hexdigest()[:16]

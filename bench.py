@@ -64,6 +64,7 @@ def parse(argv=None):
     ap.add_argument("--stress-cols", type=int, default=96, help="columns per stream count of the SSA stress set")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-config0", action="store_true")
+    ap.add_argument("--config3-cols", type=int, default=8192, help="columns of the polarized sample (0 = skip)")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate [requests/s]")
     ap.add_argument("--serve-max-cols", type=int, default=16384, help="largest swath of the serving run")
@@ -490,6 +491,98 @@ def config0(torch, L, fp64_peak, ftab, cpu=True):
     return out
 
 
+def config3(torch, L, ncols, ocols=32, cpu=True):
+    """The polarized configuration: NSTOKES = 3, 12 streams, 64 Greek
+    coefficients of the six scattering-matrix elements (from the same
+    Lorenz-Mie tables, mixed by the AOP kernel with nPol = 6), 72 layers, 8
+    wavelengths (SERVE_CHANNELS), Lambertian albedo U(0.02, 0.40).  A bounded
+    sample of the 65,536-column workload: `ncols` columns at every wavelength
+    in one AOP + vector RT launch pair (FP32 optics straight into the FP64
+    polarized solve), 1 warm-up + 2 timed launches with CUDA events.  I, Q, U
+    of the first `ocols` columns against the polarized FP64 oracle (I
+    relative; Q and U relative to I, as they pass through zero), and the
+    oracle's own rate on the host cores."""
+    from aeroapps_gb300 import _lib, mie, synth
+    from oracle import oracle
+    N, km, nmom, ch = 12, 72, 64, list(SERVE_CHANNELS)
+    nch = len(ch)
+    cols = synth.make_columns(ncols, ch, seed=SEED + 3, nlayers=km)
+    cols["albedo"] = np.asfortranarray(np.random.default_rng(SEED + 33).uniform(0.02, 0.40, (ncols, nch)))
+    tabs = mie.generate_tables(ch, nmom=nmom, npol=6)
+    chem = mie.ChemMie(tabs)
+    names = synth.tracer_names()
+    qt = np.array([chem.query_idx(n)[0] for n in names], np.int32)
+    qb = np.array([chem.query_idx(n)[1] for n in names], np.int32)
+    dev = lambda a, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(a, dt).ravel(order="F"))).cuda()
+    d = {k: dev(cols[k], np.float64) for k in ("ROT", "depol", "he", "albedo", "sza", "raa", "vza")}
+    qm, rh = dev(cols["qm"], np.float32), dev(cols["rh"], np.float32)
+    nl = km * nch * ncols
+    tau = torch.empty(nl, dtype=torch.float32, device="cuda")
+    ssa, g = torch.empty_like(tau), torch.empty_like(tau)
+    pm = torch.empty(nl * nmom * 6, dtype=torch.float32, device="cuda")
+    out = {k: torch.empty(ncols * nch, dtype=torch.float64, device="cuda") for k in ("rad", "refl", "q", "u")}
+    nf = torch.empty(ncols * nch, dtype=torch.int32, device="cuda")
+    st = torch.empty_like(nf)
+    stream = torch.cuda.current_stream().cuda_stream
+    ch32 = np.array(ch, np.float32)
+    P = lambda t: t.data_ptr()
+
+    def run():
+        rc = L.aerort_get_aop_vector_dev(chem.handle, km, ncols, nch, 20, _lib.ptr(ch32, _lib.P_f),
+                                         _lib.ptr(qt, _lib.P_i), _lib.ptr(qb, _lib.P_i), P(qm), P(rh), nmom, 6,
+                                         P(tau), P(ssa), P(g), P(pm), stream)
+        assert rc == 0, _lib.last_error()
+        rc = L.aerort_vlidort_vector_lambert_batch_dev(km, nch, ncols, N, 0, nmom, None, P(d["ROT"]), P(d["depol"]),
+                                                        None, None, None, None, P(tau), P(ssa), P(pm), P(d["he"]),
+                                                        P(d["albedo"]), P(d["sza"]), P(d["raa"]), P(d["vza"]), None,
+                                                        MISSING, P(out["rad"]), P(out["refl"]), P(out["q"]),
+                                                        P(out["u"]), P(nf), P(st), stream)
+        assert rc == 0, _lib.last_error()
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 2
+    e0.record()
+    for _ in range(reps):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    res = {"workload": "polarized: NSTOKES=3, 12 streams, 64 Greek coefficients x 6 elements, 72 layers, 8 wavelengths "
+                       "(340-2130 nm), Lambertian albedo U(0.02,0.40); AOP (nPol=6) + FP64 vector RT per launch",
+           "columns": ncols, "solves": ncols * nch, "value": ncols * nch / (ms * 1e-3), "unit": "radiances/s",
+           "ms_per_launch": ms, "sample": "%d of the workload's 65,536 columns, all 8 wavelengths" % ncols,
+           "failed_solves": int((st.cpu().numpy() != 0).sum())}
+    g_out = {k: v.cpu().numpy().reshape(ncols, nch, order="F") for k, v in out.items()}
+    gnf = nf.cpu().numpy().reshape(ncols, nch, order="F")
+    chem.destroy()
+    if cpu:
+        sub = subset(cols, np.arange(ocols))
+        t0 = time.perf_counter()
+        otau, ossa, _, opm, rc = oracle.get_aop_vector(tabs, km, ocols, nch, 20, ch32, qt, qb, sub["qm"], sub["rh"],
+                                                       nmom, 6)
+        F = lambda a: np.asfortranarray(a.astype(np.float64))
+        orad, _, oq, ou, rc2, onf, ost = oracle.vector_lambert(km, nch, ocols, N, 0, nmom, sub["ROT"], sub["depol"],
+                                                               None, F(otau), F(ossa), F(opm), sub["he"],
+                                                               sub["albedo"], sub["sza"], sub["raa"], sub["vza"],
+                                                               None, MISSING)
+        dt = time.perf_counter() - t0
+        ok = (orad != MISSING) & (ost == 0)
+        gi, gq, gu = g_out["rad"][:ocols], g_out["q"][:ocols], g_out["u"][:ocols]
+        ei = np.abs(gi[ok] / orad[ok] - 1.0)
+        eq = np.abs(gq[ok] - oq[ok]) / orad[ok]
+        eu = np.abs(gu[ok] - ou[ok]) / orad[ok]
+        res["parity_vs_oracle"] = {"I_max_rel": float(ei.max()), "I_median_rel": float(np.median(ei)),
+                                   "Q_max_rel_to_I": float(eq.max()), "U_max_rel_to_I": float(eu.max()),
+                                   "fourier_terms_identical": bool(np.array_equal(onf, gnf[:ocols])),
+                                   "solves": int(ok.sum()), "bar": 1e-9}
+        res["cpu_baseline"] = {"value": ocols * nch / dt, "unit": "radiances/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "the first %d columns x 8 wavelengths: oracle AOP (nPol=6) "
+                                                         "+ polarized FP64 oracle, OpenMP over pixels; %.1f s"
+                                                         % (ocols, dt)}
+    return res
+
+
 def e2e_host_abi(L, chem, groups, qt, qb, ch32, steps):
     """End to end through the host-pointer C ABI, as a Fortran caller would
     drive it: per stream-count group, aerort_get_aop_vector on host
@@ -566,7 +659,7 @@ def serving_run(args, tabs):
     base = [serve.make_swath(i, int(sizes[i]), list(SERVE_CHANNELS[f:f + k]), seed=5000 + i)
             for i, (f, k) in enumerate(zip(firsts, nchs))]
     fresh = lambda: [serve.Swath(rid=s.rid, cols=s.cols, nstreams=s.nstreams, channels=s.channels) for s in base]
-    srv = serve.Server(tabs, nslots=4, precision="mixed", hbm_budget_gb=120.0)
+    srv = serve.Server(tabs, nslots=2, precision="mixed", hbm_budget_gb=120.0, max_batch_cols=65536)
     srv.submit(serve.make_swath(999, 256, list(SERVE_CHANNELS), seed=1))
     srv.drain()
     srv.done.clear()
@@ -591,7 +684,7 @@ def serving_run(args, tabs):
     out = dict(stats)
     out.update({"arrival_rate_per_s": args.serve_rate, "sustained_radiances_per_s": rads / wall,
                 "offline_batch_radiances_per_s": offline, "sustained_over_offline": rads / wall / offline,
-                "slots": 4, "precision": "mixed",
+                "batch_lanes": 2, "max_batch_cols": 65536, "precision": "mixed",
                 "swath_columns": "log-uniform %d..%d" % (64, args.serve_max_cols),
                 "wavelengths_per_request": "1-8 of %s nm" % list(SERVE_CHANNELS), "hbm_budget_gb": 120.0,
                 "note": "at the configured rate the GPU is saturated, so latency is queueing; at_half_capacity "
@@ -793,6 +886,16 @@ def main():
         flops += float(ftab[N][batch["nlayers"][sel][:, None], np.clip(nf_d[sel], 0, 63)].sum())
     okall = (rad_d != MISSING)
     dev_err = np.abs(rad_m[okall] / rad_d[okall] - 1.0)
+    # the solves furthest from the FP64 result: column, wavelength, streams,
+    # layers, error, Fourier terms (the batch is seeded, so each can be
+    # re-solved on the host)
+    err_full = np.zeros_like(rad_d)
+    err_full[okall] = dev_err
+    worst = []
+    for flat in np.argsort(err_full, axis=None)[::-1][:8]:
+        ci, wi = np.unravel_index(flat, err_full.shape)
+        worst.append({"col": int(ci), "nm": CHANNELS[wi], "N": int(batch["nstreams"][ci]),
+                      "L": int(batch["nlayers"][ci]), "err": float(err_full[ci, wi]), "nf": int(nf_d[ci, wi])})
     fp64_peak, fp32_peak, dgemm = pipe_peaks(torch, L, stream)
     ach_m = flops / (rt_ms_m * 1e-3) / 1e12
     ach_d = flops / (rt_ms_d * 1e-3) / 1e12
@@ -855,6 +958,11 @@ def main():
     if rank == 0 and not args.no_config0:
         c0 = config0(torch, L, fp64_peak, ftab, cpu=(world == 1 and not args.no_cpu))
 
+    # ---------------------------------------------------------------- config 3 (polarized)
+    c3 = None
+    if rank == 0 and args.config3_cols > 0:
+        c3 = config3(torch, L, args.config3_cols, cpu=(world == 1 and not args.no_cpu))
+
     # ---------------------------------------------------------------- front end kernels (ROT, edge, AOP)
     rot_line = edge_line = aop_line = None
     if rank == 0:
@@ -875,12 +983,13 @@ def main():
         "dtype": "f32+f64 (mixed: FP64 set-up and single scatter, FP32 Fourier series)", "data": "synthetic",
         "config": cfg, "gpu_launches": launches, "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
         "e2e": e2e, "rot_calc": rot_line, "edge_vars": edge_line, "aop": aop_line, "serving": serving,
-        "config0_plain_fp64": c0, "roofline_plain": roofline_plain,
+        "config3_polarized": c3, "config0_plain_fp64": c0, "roofline_plain": roofline_plain,
         "accuracy": acc, "accuracy_ssa_stress": stress,
         "plain_fp64": {"value": plain_value, "unit": "radiances/s", "ms_per_step": rt_ms_d, "steps": args.plain_steps,
                        "mixed_over_plain": value / plain_value,
                        "mixed_vs_fp64_gpu_max": float(dev_err.max()),
-                       "mixed_vs_fp64_gpu_median": float(np.median(dev_err)), "radiances": int(dev_err.size)},
+                       "mixed_vs_fp64_gpu_median": float(np.median(dev_err)), "radiances": int(dev_err.size),
+                       "mixed_over_1e-4": int((dev_err > 1e-4).sum()), "worst": worst},
     }
     if rank == 0:
         print(json.dumps(line))

@@ -27,9 +27,7 @@ static int run(const RtOptions& opt, const LambertInputs& in, double* rad, doubl
   gl(NS, qx, qw);
   gl(opt.nfine > 0 ? opt.nfine : 1, tu, wu);
   ScratchLayout<NS> lay(in.km, false);
-  SweepLayout<NS> swl(in.km);
   std::vector<double> scr((lay.template bytes<T>() + 7) / 8);
-  std::vector<T> sweep(swl.total);
   auto M = std::make_unique<TeamMem<NS, T>>();
   const SolveScratch<T> S = make_scratch<NS, T>(scr.data(), 0, 1, in.km, false);
   for (int s = 0; s < in.nobs * in.nch; ++s) {
@@ -43,7 +41,7 @@ static int run(const RtOptions& opt, const LambertInputs& in, double* rad, doubl
     for (int lane = 0; lane < kTeam; ++lane)
       th.emplace_back([&, lane] {
         const Team tm{lane, bar_sync, &bar};
-        team_fourier_series<NS, T>(tm, *M, opt, in, rb, qx, qw, S.W, lay, sweep.data(), rad, refl, nf, st);
+        team_fourier_series<NS, T>(tm, *M, opt, in, rb, qx, qw, S.W, lay, rad, refl, nf, st);
       });
     for (auto& t : th) t.join();
   }

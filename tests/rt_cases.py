@@ -28,7 +28,8 @@ def rt_args(c, nstreams):
             c["ssa"], c["g"], c["pmom"], c["pe"], c["he"], c["te"], c["albedo"], c["sza"], c["raa"], c["vza"])
 
 
-def vector_mie_case(nstreams, nobs, nch=2, seed=0, nlayers=72, chem_channels=(470.0, 550.0, 670.0, 865.0)):
+def vector_mie_case(nstreams, nobs, nch=2, seed=0, nlayers=72, chem_channels=(470.0, 550.0, 670.0, 865.0),
+                    nmom=None):
     """Columns from synth with the six-element Mie optics of the aerosol tracers
     (oracle VLIDORT_getAOPvector with nPol = 6 on synthetic Lorenz-Mie tables):
     the inputs of VLIDORT_Vector_Lambert, FP64 as the reference driver passes them."""
@@ -36,7 +37,7 @@ def vector_mie_case(nstreams, nobs, nch=2, seed=0, nlayers=72, chem_channels=(47
     from oracle import oracle
     ch = list(chem_channels[:nch])
     c = synth.make_columns(nobs, ch, seed=seed + 11, nlayers=nlayers)
-    nmom = 2 * nstreams
+    nmom = nmom or 2 * nstreams
     tabs = mie.generate_tables(ch, nmom=nmom, npol=6)
     qidx = {}
     for ti, t in enumerate(tabs.tables):

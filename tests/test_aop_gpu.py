@@ -71,3 +71,47 @@ def test_aop_scalar_equals_vector_without_moments(tables):
     assert sc[3] == 0 and vec[4] == 0 and miss[3] == 99
     for a, b in zip(sc[:3], vec[:3]):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.fixture(scope="module")
+def tables6():
+    return mie.generate_tables([470.0, 550.0, 670.0, 865.0], nmom=40, npol=6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("npol,nmom", [(6, 40), (6, 7), (3, 20), (1, 33)])
+def test_bit_identical_six_element_tables(tables6, npol, nmom):
+    # moment counts below, at and past one 16-moment chunk of the kernel
+    cols = synth.make_columns(24, [470.0, 550.0, 670.0, 865.0], seed=77 + nmom)
+    got, want = _run_both(tables6, cols, [470.0, 670.0, 865.0], nmom, npol)
+    assert got[4] == 0 and want[4] == 0
+    for a, b in zip(got[:4], want[:4]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_bit_identical_six_elements_with_four_element_tables(tables6):
+    # spherical species carry four elements (P11, P12, P33, P34); under
+    # nPol = 6 the reference sets P22 and P44 to the running P11 and P33 sums
+    # after each such tracer (VLIDORT_MieMod.F90:305-310), so the order of
+    # four- and six-element tracers shows in the result.  The six-element
+    # tables here get P22 != P11 and P44 != P33 (as non-spherical tables
+    # have; Lorenz-Mie tables have them equal), and the last species is one
+    # of them.
+    tabs = []
+    for j, t in enumerate(tables6.tables):
+        if j % 2:
+            pm = np.asfortranarray(t.pmom[..., :4])
+        else:
+            pm = np.array(t.pmom, order="F")
+            pm[..., 4] *= np.float32(0.9)
+            pm[..., 5] *= np.float32(0.8)
+        tabs.append(mie.MieTable(t.name, t.rh, t.bext, t.bsca, t.g, pm))
+    mixed = mie.MieTableSet(tables6.channels_m, tabs)
+    cols = synth.make_columns(24, [470.0, 550.0, 670.0, 865.0], seed=91)
+    got, want = _run_both(mixed, cols, [550.0, 865.0], 24, 6)
+    assert got[4] == 0 and want[4] == 0
+    for a, b in zip(got[:4], want[:4]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    p = got[3]
+    assert not np.array_equal(p[..., 4], p[..., 0]) and not np.array_equal(p[..., 5], p[..., 2])

@@ -61,3 +61,17 @@ def test_solve_count_beyond_work_counter_range_is_rejected_on_the_host():
     # the largest accepted count still passes the check (then fails on the null outputs, not the size)
     rc = L.aerort_vlidort_scalar_lambert(72, 1, 1, None, 8, 0, 16, 1, *([None] * 13), -1e15, 0, None, None)
     assert rc == 1002 and "too large" not in _lib.last_error()
+
+
+def test_ctypes_signatures_match_header_argument_counts():
+    # every signature the Python package binds has the argument count of the
+    # C prototype in include/aerort.h (a miscount shifts every later argument)
+    src = open(os.path.join(ROOT, "include", "aerort.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = {}
+    for name, args in re.findall(r"\b(aerort_\w+)\s*\(([^;{]*?)\)\s*;", src, flags=re.S):
+        protos[name] = 0 if args.strip() in ("", "void") else args.count(",") + 1
+    for name, (_, argtypes) in _lib._SIGNATURES.items():
+        if name in protos:
+            assert len(argtypes) == protos[name], (name, len(argtypes), protos[name])
+    assert "aerort_vlidort_vector_lambert_ex" in protos

@@ -58,3 +58,17 @@ def test_host_build_of_polarized_kernel_matches_oracle(vec_lib):
     assert np.max(np.abs(rad / orad - 1.0)) < 1e-9
     assert np.max(np.abs(q - oq) / orad) < 1e-9 and np.max(np.abs(u - ou) / orad) < 1e-9
     assert np.max(np.abs(refl / orefl - 1.0)) < 1e-9
+
+
+def test_host_build_with_more_moments_than_streams(vec_lib):
+    # nMom = 13 > 2N = 8: delta-M truncates at 2N-1 while the single scatter
+    # (I, Q and U) uses every input Greek coefficient
+    N = 4
+    c = vector_mie_case(N, nobs=1, nch=2, seed=19, nlayers=np.array([7]), nmom=13)
+    (rad, refl, q, u), nf, st = _host(vec_lib, c, N)
+    orad, orefl, oq, ou, rc, onf, ost = oracle.vector_lambert(
+        c["km"], 2, 1, N, 0, c["nmom"], c["ROT"], c["depol"], None, c["tau"], c["ssa"], c["pmom"], c["he"],
+        c["albedo"], c["sza"], c["raa"], c["vza"], c["flux"], MISSING, nlay=c["nlayers"])
+    assert rc == 0 and np.all(st == 0) and np.array_equal(nf, onf)
+    assert np.max(np.abs(rad / orad - 1.0)) < 1e-9
+    assert np.max(np.abs(q - oq) / orad) < 1e-9 and np.max(np.abs(u - ou) / orad) < 1e-9

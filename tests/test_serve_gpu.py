@@ -25,6 +25,48 @@ def test_request_bytes_counts_every_group():
     assert b >= lower
 
 
+def test_merge_group_over_the_union_of_wavelengths():
+    # two requests with different wavelength sets merged into one launch per
+    # stream count: each column's unrequested wavelengths get a MISSING
+    # albedo, its requested ones its own inputs; the scatter of a launch's
+    # outputs hands every request exactly its (column, wavelength) entries
+    a = serve.make_swath(0, 30, [550.0, 865.0], seed=1)
+    b = serve.make_swath(1, 25, [470.0, 550.0, 670.0], seed=2)
+    chans = sorted({*a.channels, *b.channels})
+    seen = {0: [], 1: []}
+    outs = []
+    for N in serve.STREAMS:
+        g = serve.merge_group([a, b], N, chans)
+        if g is None:
+            continue
+        n, nch = g["n"], len(chans)
+        assert g["ROT"].shape == (g["km"], n, nch) and g["albedo"].shape == (n, nch)
+        code = np.zeros((n, nch))
+        for sw, idx, r, pos in g["rows"]:
+            seen[sw.rid].extend(idx.tolist())
+            assert np.all(g["nlayers"][r] == sw.cols["nlayers"][idx])
+            for j, p in enumerate(pos):
+                assert np.array_equal(g["albedo"][r, p], sw.cols["albedo"][idx, j])
+                assert g["depol"][p] == sw.cols["depol"][j]
+                km_c = int(sw.cols["nlayers"][idx].max())
+                assert np.array_equal(g["ROT"][:km_c, r, p], sw.cols["ROT"][:km_c, idx, j])
+            others = [p for p in range(nch) if p not in pos]
+            assert np.all(g["albedo"][np.ix_(r, others)] == serve.MISSING)
+            # a distinct value per (request, column, wavelength) as the launch output
+            for j, p in enumerate(pos):
+                code[r, p] = 1000.0 * sw.rid + 10.0 * idx + chans.index(sw.channels[j]) * 0.1
+        import torch
+        host = [torch.from_numpy(np.asfortranarray(x).ravel(order="F")) for x in
+                (code, 2 * code, np.zeros((n, nch), np.int32), np.zeros((n, nch), np.int32))]
+        outs.append((g["rows"], host, n, nch))
+    assert sorted(seen[0]) == list(range(30)) and sorted(seen[1]) == list(range(25))
+    serve.Server._finish([a, b], outs)
+    for sw in (a, b):
+        want = np.array([[1000.0 * sw.rid + 10.0 * i + chans.index(c) * 0.1 for c in sw.channels]
+                         for i in range(sw.ncol)])
+        assert np.array_equal(sw.radiance, want) and np.array_equal(sw.reflectance, 2 * want)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["mixed", "fp64"])
 def test_results_identical_alone_and_in_the_mix(precision):

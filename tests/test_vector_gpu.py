@@ -56,6 +56,15 @@ def test_vector_lambert_matches_oracle(N, nobs):
 
 
 @pytest.mark.gpu
+def test_vector_lambert_twelve_streams_sixty_four_moments():
+    # the polarized workload's sizes: N = 12, 64 Greek coefficients (> 2N, so
+    # delta-M truncates and the single scatter uses all 64), 72 layers
+    N = 12
+    c = vector_mie_case(N, nobs=2, nch=2, seed=64, nmom=64, chem_channels=(340.0, 2130.0))
+    _check(_host_call(c, N), _oracle(c, N))
+
+
+@pytest.mark.gpu
 def test_vector_lambert_gas_absorption_flux_and_missing():
     # trace-gas absorption alpha, per-pixel flux factor, and one pixel with a
     # MISSING albedo and one with MISSING angles: all four outputs MISSING there
