@@ -189,8 +189,12 @@ class Server:
         # the mixed series and for the FP64 re-solves, so that results do not
         # depend on the batch a request lands in
         autotune.apply_defaults(torch.cuda.get_device_name(torch.cuda.current_device()))
+        self._saved = []  # the library's settings before the server's, put back by close()
         for N in STREAMS:
             for prec in {self.prec, _lib.PREC_FP64}:
+                tpb, bps = ctypes.c_int(), ctypes.c_int()
+                self.L.aerort_get_schedule(N, prec, ctypes.byref(tpb), ctypes.byref(bps))
+                self._saved.append((N, prec, self.L.aerort_get_kernel(N, prec), tpb.value, bps.value))
                 ent = autotune._active.get(autotune._key(N, 72, prec))
                 if ent is not None:
                     autotune._set(N, prec, ent["kernel"], ent["threads"], ent["blocks_per_sm"])
@@ -207,11 +211,14 @@ class Server:
         return time.perf_counter() - self.t0
 
     def close(self):
+        from . import autotune
         for s in self.slots:
             for st in s["streams"]:
                 st.synchronize()
         self.slots = []
         self.chem.destroy()
+        for N, prec, kern, tpb, bps in self._saved:
+            autotune._set(N, prec, kern, tpb, bps)
 
     # ------------------------------------------------------------------ request path
     def submit(self, swath):
