@@ -1,7 +1,7 @@
 """Build recipe of the CPU oracle (test infrastructure only).
 
 Compiles the oracle's own C/C++ restatement (vlidort_oracle.cpp,
-vlidort_vector_oracle.cpp, mie_oracle.c,
+vlidort_vector_oracle.cpp, brdf_oracle.cpp, mie_oracle.c,
 rot_oracle.c, edge_oracle.c)
 into oracle/_build/liboracle.so with strict IEEE semantics (no contraction of
 a*b+c into FMA, so the FP32 Mie path reproduces the reference arithmetic).
@@ -15,7 +15,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboracle.so")
-SRCS = ["vlidort_oracle.cpp", "vlidort_vector_oracle.cpp", "mie_oracle.c", "rot_oracle.c", "edge_oracle.c"]
+SRCS = ["vlidort_oracle.cpp", "vlidort_vector_oracle.cpp", "brdf_oracle.cpp", "mie_oracle.c", "rot_oracle.c",
+        "edge_oracle.c"]
 
 
 def build(force=False):

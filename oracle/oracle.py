@@ -30,6 +30,8 @@ def lib():
     if _lib is None:
         _lib = ctypes.CDLL(_build.build())
         _lib.oracle_vlidort_solve.restype = ctypes.c_int
+        _lib.oracle_vlidort_solve_brdf.restype = ctypes.c_int
+        _lib.oracle_brdf_supplement.restype = ctypes.c_int
         _lib.oracle_vlidort_vector_solve.restype = ctypes.c_int
         _lib.oracle_vector_lambert.restype = ctypes.c_int
         _lib.oracle_scalar_lambert.restype = ctypes.c_int
@@ -59,6 +61,49 @@ def vlidort_solve(opts, heights, deltau, omega, greek, albedo, sza, vzas, raas, 
     st = lib().oracle_vlidort_solve(ctypes.byref(opts), L, nstreams, g1 - 1, _p(heights, P_d), _p(deltau, P_d),
                                     _p(omega, P_d), _p(greek, P_d), ctypes.c_double(albedo), ctypes.c_double(sza),
                                     len(vz), _p(vz, P_d), len(ra), _p(ra, P_d), _p(out, P_d), ctypes.byref(nf))
+    return out.reshape(len(vz), len(ra)), nf.value, st
+
+
+def brdf_supplement(kernels, nstreams, sza, vzas, raas, nstreams_brdf=50, do_shadow=False, nmom=None):
+    """VBRDF supplement for one solar beam (oracle/brdf_oracle.cpp).  kernels:
+    [(which, factor, (p1, p2, p3)), ...] with `which` the VLIDORT kernel index
+    (1 Lambertian, 2 Ross-thin, 3 Ross-thick, 4 Li-sparse, 5 Li-dense, 9
+    Cox-Munk).  Returns dict f (m, i, j), f0 (m, i), uf (m, u, j), uf0 (m, u),
+    exactdb (u, a), m = 0..nmom (default 2 nstreams - 1)."""
+    nk = len(kernels)
+    which = np.array([k[0] for k in kernels], np.int32)
+    fac = np.array([k[1] for k in kernels], np.float64)
+    pars = np.array([list(k[2]) + [0.0] * (3 - len(k[2])) for k in kernels], np.float64).ravel()
+    vz = np.ascontiguousarray(vzas, np.float64)
+    ra = np.ascontiguousarray(raas, np.float64)
+    N, nu, na = nstreams, len(vz), len(ra)
+    nmom = 2 * N - 1 if nmom is None else nmom
+    M1 = nmom + 1
+    f = np.zeros((M1, N, N)); f0 = np.zeros((M1, N)); uf = np.zeros((M1, nu, N)); uf0 = np.zeros((M1, nu))
+    ex = np.zeros((nu, na))
+    lib().oracle_brdf_supplement(nk, _p(which, P_i), _p(fac, P_d), _p(pars, P_d), int(do_shadow), nstreams_brdf, N,
+                                 nmom, ctypes.c_double(sza), nu, _p(vz, P_d), na, _p(ra, P_d), _p(f, P_d),
+                                 _p(f0, P_d), _p(uf, P_d), _p(uf0, P_d), _p(ex, P_d))
+    return {"f": f, "f0": f0, "uf": uf, "uf0": uf0, "exactdb": ex}
+
+
+def vlidort_solve_brdf(opts, heights, deltau, omega, greek, brdf, sza, vzas, raas, nstreams):
+    """vlidort_solve with a BRDF surface: `brdf` from brdf_supplement for the
+    same beam, user angles and azimuths."""
+    heights = np.ascontiguousarray(heights, np.float64)
+    deltau = np.ascontiguousarray(deltau, np.float64)
+    omega = np.ascontiguousarray(omega, np.float64)
+    greek = np.ascontiguousarray(greek, np.float64)
+    L, g1 = greek.shape
+    vz = np.ascontiguousarray(vzas, np.float64)
+    ra = np.ascontiguousarray(raas, np.float64)
+    arr = [np.ascontiguousarray(brdf[k], np.float64) for k in ("f", "f0", "uf", "uf0", "exactdb")]
+    out = np.zeros(len(vz) * len(ra))
+    nf = ctypes.c_int(0)
+    st = lib().oracle_vlidort_solve_brdf(ctypes.byref(opts), L, nstreams, g1 - 1, _p(heights, P_d), _p(deltau, P_d),
+                                         _p(omega, P_d), _p(greek, P_d), ctypes.c_double(0.0), ctypes.c_double(sza),
+                                         len(vz), _p(vz, P_d), len(ra), _p(ra, P_d),
+                                         *[_p(a, P_d) for a in arr], _p(out, P_d), ctypes.byref(nf))
     return out.reshape(len(vz), len(ra)), nf.value, st
 
 

@@ -705,10 +705,18 @@ extern "C" {
 // (moment l of layer n at greek[l + (ngreek+1)*n]).  out[ua + nraa*um] is the
 // TOA upwelling intensity STOKES(1,geom,1,UPIDX).  nfourier_out = last Fourier
 // term summed.  Returns a status code.
-int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const double* heights,
-                         const double* deltau_in, const double* omega_in, const double* greek_in,
-                         double albedo, double sza, int nvza, const double* vza, int nraa,
-                         const double* raa, double* out, int* nfourier_out) {
+//
+// oracle_vlidort_solve_brdf: the same with a BRDF surface in place of the
+// Lambertian albedo (DO_LAMBERTIAN_SURFACE = .false.): the Fourier components
+// of oracle_brdf_supplement for m = 0..2N-1 (bf[(m N + i) N + j], bf0[m N + i],
+// buf[(m nvza + u) N + j], buf0[m nvza + u]) and the exact direct-bounce BRDF
+// bexact[u nraa + a].  bf == nullptr selects the Lambertian surface.
+int oracle_vlidort_solve_brdf(const OracleOpts* o, int L, int N, int ngreek, const double* heights,
+                              const double* deltau_in, const double* omega_in, const double* greek_in,
+                              double albedo, double sza, int nvza, const double* vza, int nraa,
+                              const double* raa, const double* bf, const double* bf0, const double* buf,
+                              const double* buf0, const double* bexact, double* out, int* nfourier_out) {
+  const bool brdf = bf != nullptr;
   const int order = o->taylor_order;
   const int NM = std::min(2 * N - 1, ngreek);  // vlidort_inputs.f90:4141
   const int G1 = ngreek + 1;
@@ -899,7 +907,9 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
         for (int l = 2; l <= ngreek; ++l)
           gs[l] = ((double)(2 * l - 1) / (double)l) * gs[l - 1] * cosscat - ((double)(l - 1) / (double)l) * gs[l - 2];
         double cum = 0.0;
-        double cumdb = 4.0 * mu0 * albedo * atten[L] * 1.0;
+        // FO direct bounce: the exact BRDF of the geometry (vlidort_vfo_interface.f90:594-617)
+        const double reflec_db = brdf ? bexact[u * nraa + a] : albedo;
+        double cumdb = 4.0 * mu0 * reflec_db * atten[L] * 1.0;
         for (int n = L; n >= 1; --n) {
           double fmat = 0.0;
           for (int l = 0; l <= ngreek; ++l) fmat += gs[l] * greek_in[l + G1 * (n - 1)];
@@ -943,18 +953,26 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
   while (iterate && fourier < n_fouriers) {
     fourier++;
     const int m = fourier;
-    const bool incl_surface = (m == 0) && (albedo != 0.0);
+    // a BRDF surface reflects in every Fourier term (vlidort_masters_V2p8p3.f90:2380-2400)
+    const bool incl_surface = brdf ? true : ((m == 0) && (albedo != 0.0));
     const double surface_factor = (m == 0) ? 2.0 : 1.0;
     const double delta_factor = (m == 0) ? 1.0 : 2.0;
     const double flux_multiplier = delta_factor;
     // DIRECTRADIANCE, miscsetups :1296 (Lambertian, Fourier 0 only)
-    double direct_beam = 0.0;
+    double direct_beam = 0.0, beam_attn = 0.0;
+    std::vector<double> direct_beam_q(N, 0.0);  // DIRECT_BEAM(i): per stream for a BRDF (miscsetups :1517-1545)
     bool localbeam = incl_surface ? refl_directbeam : false;
     if (incl_surface && refl_directbeam) {
       double x0_flux = 4.0 * cos_sza / delta_factor;
       x0_flux = o->flux_factor * x0_flux / PI4;
       double attn = x0_flux * trans_solar_beam;
-      if (m == 0) direct_beam = attn * albedo;
+      beam_attn = attn;
+      if (brdf) {
+        for (int i = 0; i < N; ++i) direct_beam_q[i] = attn * bf0[m * N + i];
+      } else if (m == 0) {
+        direct_beam = attn * albedo;
+        for (int i = 0; i < N; ++i) direct_beam_q[i] = direct_beam;
+      }
     }
     // PIMATRIX_SETUP_OMP, miscsetups :2273 (NSTOKES = 1)
     {
@@ -1152,17 +1170,29 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
         }
       }
       int c0 = N2 * L - N, ce = N2 * (L - 1);
-      std::vector<double> r2p(N, 0.0), r2m(N, 0.0);
+      // R2_HOMP/R2_HOMM (bvproblem.f90:538-614): one row for every stream i
+      // (Lambertian: the same for all i; BRDF: AXBID_F = QUAD_STRMWTS(j) BRDF_F(i, j))
+      std::vector<double> r2p(N * N, 0.0), r2m(N * N, 0.0);
       if (incl_surface)
-        for (int k = 0; k < N; ++k) {
-          double sp = 0.0, sm = 0.0;
-          for (int j = 0; j < N; ++j) { sp += strmwts[j] * XP(j, k, L - 1); sm += strmwts[j] * XN(j, k, L - 1); }
-          r2p[k] = sp * r2homp_fac; r2m[k] = sm * r2homp_fac;
-        }
+        for (int i = 0; i < N; ++i)
+          for (int k = 0; k < N; ++k) {
+            double sp = 0.0, sm = 0.0;
+            if (brdf) {
+              for (int j = 0; j < N; ++j) {
+                const double ax = strmwts[j] * bf[(m * N + i) * N + j];
+                sp += ax * XP(j, k, L - 1);
+                sm += ax * XN(j, k, L - 1);
+              }
+              r2p[i + N * k] = surface_factor * sp; r2m[i + N * k] = surface_factor * sm;
+            } else {
+              for (int j = 0; j < N; ++j) { sp += strmwts[j] * XP(j, k, L - 1); sm += strmwts[j] * XN(j, k, L - 1); }
+              r2p[i + N * k] = sp * r2homp_fac; r2m[i + N * k] = sm * r2homp_fac;
+            }
+          }
       for (int i = 0; i < N; ++i)
         for (int k = 0; k < N; ++k) {
-          double xpnet = XP(i + N, k, L - 1) - r2p[k];
-          double xmnet = XN(i + N, k, L - 1) - r2m[k];
+          double xpnet = XP(i + N, k, L - 1) - r2p[i + N * k];
+          double xmnet = XN(i + N, k, L - 1) - r2m[i + N * k];
           AB(c0 + i, ce + k) = teig[k + N * (L - 1)] * xpnet;
           AB(c0 + i, ce + k + N) = xmnet;
         }
@@ -1236,14 +1266,21 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
     }
     {
       int c0 = (L - 1) * N2 + N;
+      // R2_BEAM (bvproblem.f90:1680-1736) and the direct beam (:1903-1913)
       double r2b = 0.0;
-      if (incl_surface) {
+      if (incl_surface && !brdf) {
         for (int j = 0; j < N; ++j) r2b += strmwts[j] * wlower[j + N2 * (L - 1)];
         r2b = r2b * surface_factor * albedo;
       }
       for (int i = 0; i < N; ++i) {
-        col[c0 + i] = -wlower[i + N + N2 * (L - 1)] + (incl_surface ? r2b : 0.0);
-        if (localbeam && incl_surface) col[c0 + i] += direct_beam;
+        double r2bi = r2b;
+        if (incl_surface && brdf) {
+          double s = 0.0;
+          for (int j = 0; j < N; ++j) s += strmwts[j] * bf[(m * N + i) * N + j] * wlower[j + N2 * (L - 1)];
+          r2bi = surface_factor * s;
+        }
+        col[c0 + i] = -wlower[i + N + N2 * (L - 1)] + (incl_surface ? r2bi : 0.0);
+        if (localbeam && incl_surface) col[c0 + i] += direct_beam_q[i];
       }
     }
     band_solve(NT, KL, KU, ab.data(), LDAB, ipiv.data(), col.data());
@@ -1253,7 +1290,11 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
     std::vector<double> stokes_f(nvza, 0.0);
     {
       const bool incl_directrf = (localbeam && !do_dbcorr) && !msmode;
+      // BOA surface source (intensity.f90:1300-1420): STOKES_DOWNSURF(i) =
+      // QUAD_STRMWTS(i) * downwelling; Lambertian: albedo times their sum;
+      // BRDF: their product with USER_BRDF_F(u, i)
       double reflec = 0.0;
+      std::vector<double> downsurf(N, 0.0);
       if (incl_surface) {
         double s = 0.0;
         for (int i = 0; i < N; ++i) {
@@ -1263,13 +1304,23 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
             double mxr = MCON(k, L - 1) * XN(i, k, L - 1);
             shom = shom + lxr * teig[k + N * (L - 1)] + mxr;
           }
-          s += strmwts[i] * (wlower[i + N2 * (L - 1)] + shom);
+          downsurf[i] = strmwts[i] * (wlower[i + N2 * (L - 1)] + shom);
+          s += downsurf[i];
         }
         reflec = surface_factor * albedo * s;
       }
       for (int u = 0; u < nvza; ++u) {
-        double cum = incl_surface ? reflec : 0.0;
-        if (incl_surface && incl_directrf && !do_dbcorr) cum += direct_beam;
+        double cum = 0.0;
+        if (incl_surface) {
+          if (brdf) {
+            double s = 0.0;
+            for (int j = 0; j < N; ++j) s += downsurf[j] * buf[(m * nvza + u) * N + j];
+            cum = surface_factor * s;
+          } else {
+            cum = reflec;
+          }
+        }
+        if (incl_surface && incl_directrf && !do_dbcorr) cum += brdf ? beam_attn * buf0[m * nvza + u] : direct_beam;
         for (int n = L - 1; n >= 0; --n) {
           double src = 0.0;
           if (laysc[m + (NM + 1) * n]) {
@@ -1358,6 +1409,14 @@ int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const do
 // (VLIDORT2p8p3/VLIDORT_Mod.F90:355); tests may tighten it to check how far
 // that tolerance moves the reference algorithm from the converged solution.
 static double g_asymtx_tol = 1.0e-12;
+extern "C" int oracle_vlidort_solve(const OracleOpts* o, int L, int N, int ngreek, const double* heights,
+                                    const double* deltau_in, const double* omega_in, const double* greek_in,
+                                    double albedo, double sza, int nvza, const double* vza, int nraa,
+                                    const double* raa, double* out, int* nfourier_out) {
+  return oracle_vlidort_solve_brdf(o, L, N, ngreek, heights, deltau_in, omega_in, greek_in, albedo, sza, nvza, vza,
+                                   nraa, raa, nullptr, nullptr, nullptr, nullptr, nullptr, out, nfourier_out);
+}
+
 extern "C" void oracle_set_asymtx_tol(double tol) { g_asymtx_tol = tol; }
 extern "C" double oracle_get_asymtx_tol() { return g_asymtx_tol; }
 
