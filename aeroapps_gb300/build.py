@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD, "libaerort.so")
 
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_TUS = ["aerort.cu", "rt_ns4.cu", "rt_ns6.cu", "rt_ns8.cu", "rt_ns12.cu", "rt_ns16.cu", "rt_static.cu", "rt_rot.cu", "edge_vars.cu",
-            "rt_vector.cu"]
+            "rt_vector.cu", "rt_brdf.cu"]
 HOST_TUS = ["miegen.cpp", "mie_read.cpp"]
 
 

@@ -626,6 +626,9 @@ int dispatch_lambert(Context& c, int precision, int nstreams, const RtOptions& o
   return rc ? rc : rc2;
 }
 
+}  // namespace
+
+namespace aerort_internal {
 // Largest nobs * nch of one RT call.  The persistent kernels hand out solves
 // with an int work counter that every resident warp bumps (by up to 32) once
 // more after the queue runs dry; the 16 Mi of headroom below INT_MAX covers
@@ -643,7 +646,7 @@ int lambert_checks(int km, int nch, int nobs, int nstreams, int nMom) {
   if (nMom < 1) return set_error(AERORT_RC_ARG, "scalar_lambert: nMom must be >= 1");
   return 0;
 }
-}  // namespace
+}  // namespace aerort_internal
 
 extern "C" int aerort_vlidort_scalar_lambert_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
                                                  const double* ROT, const double* depol, const double* tau,

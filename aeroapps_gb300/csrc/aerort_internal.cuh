@@ -118,6 +118,16 @@ int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::Lamb
                                 size_t arena_bytes, int* sched, int num_sms, const Schedule& sc, double* rad,
                                 double* refl, int* nf, int* st, cudaStream_t s, const aerort::Worklist& wl);
 
+// VLIDORT_Init limits and the solve-count guard shared by every RT entry point
+// (rc 2, 3, 5 as the reference; AERORT_RC_ARG for bad sizes).
+int lambert_checks(int km, int nch, int nobs, int nstreams, int nMom);
+
+// VLIDORT_Scalar_LandMODIS (RTLS BRDF surface), FP64 two-pass team solve.
+template <int NS>
+int launch_scalar_landmodis(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in,
+                            const double* kw, const int* tab_host, const double* tpar_host, int ntab, double* rad,
+                            double* refl, double* br, int* nf, int* st, cudaStream_t s);
+
 // Static device arena of the allocation-free entry point (rt_static.cu):
 // address of the calling thread's current device's copy, set up on first use.
 int static_arena(double** arena, size_t* arena_doubles, int** sched, int* num_sms);

@@ -4,6 +4,10 @@
 #include "aerort_internal.cuh"
 #include "rt_team.cuh"
 
+#include <cmath>
+#include <cstring>
+#include <vector>
+
 namespace aerort_internal {
 using namespace aerort;
 
@@ -411,6 +415,160 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
   return 0;
 }
 
+// ---------------------------------------------------------------------------------- RTLS BRDF surface
+// VLIDORT_Scalar_LandMODIS on the two-pass team solve (FP64): k_brdf_setup
+// runs each solve's set-up with its BRDF block (rt_brdf.cuh), k_brdf_series
+// the Fourier series with the BRDF surface.  The BRDF inputs are a
+// __grid_constant__ parameter: the kernels read them from parameter space
+// through a pointer, without a per-thread copy.
+
+// Sticky nadir-FO flag of the BRDF wrapper (VLIDORT_BRDF_MODIS.F90:113-185):
+// the first pixel with valid angles, solar zenith exactly 0 and a channel
+// whose exact BRDF is not negative (such a call reaches Run_Scalar).
+template <int NS>
+__global__ void k_brdf_nadir_first(LambertInputs in, const __grid_constant__ BrdfInputs b, int* first) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= in.nobs) return;
+  auto miss = [&](double x) { return fabs(x / in.missing - 1.0) < 0.001; };
+  if (miss(in.sza[j]) || miss(in.vza[j]) || miss(in.raa[j]) || in.sza[j] != 0.0) return;
+  for (int i = 0; i < in.nch; ++i) {
+    const long w = (long)i + (long)in.nch * j;
+    const int t = b.tab ? b.tab[w] : 0;
+    if (!(brdf_exact(b.kw + 3 * w, b.tpar[2 * t], b.tpar[2 * t + 1], in.sza[j], in.vza[j], in.raa[j]) < 0.0)) {
+      atomicMin(first, j);
+      return;
+    }
+  }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(32) k_brdf_setup(RtOptions opt, LambertInputs in, Quad q,
+                                                   const __grid_constant__ BrdfInputs b, void* scratch, int base,
+                                                   int count, double* rad, double* refl, int* nf, int* st,
+                                                   unsigned char* live) {
+  const ScratchLayout<NS> lay(in.km, false);
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < count; s += gridDim.x * blockDim.x) {
+    const SolveScratch<double> S = make_scratch<NS, double>(scratch, s, count, in.km, false);
+    SetupRecord r;
+    const bool ok = solve_setup<NS, double>(opt, in, base + s, q.tu, q.wu, S, rad, refl, nf, st, r, &b, s);
+    if (ok) r.store(S.D, lay.rec);
+    live[s] = ok ? 1 : 0;
+  }
+}
+
+template <int NS, int WPB>
+__global__ void __launch_bounds__(32 * WPB, 1)
+    k_brdf_series(RtOptions opt, LambertInputs in, Quad q, const __grid_constant__ BrdfInputs b, void* scratch,
+                  int base, int count, int* counter, const unsigned char* live, double* rad, double* refl, int* nf,
+                  int* st) {
+  extern __shared__ __align__(16) unsigned char team_smem[];
+  const int lane = threadIdx.x & 31;
+  TeamMem<NS, double>& M = reinterpret_cast<TeamMem<NS, double>*>(team_smem)[threadIdx.x >> 5];
+  const ScratchLayout<NS> lay(in.km, false);
+  const Team tm{lane, nullptr, nullptr};
+  for (;;) {
+    int s = 0;
+    if (lane == 0) s = atomicAdd(counter, 1);
+    s = __shfl_sync(0xffffffffu, s, 0);
+    if (s >= count) break;
+    if (!live[s]) continue;
+    const SolveScratch<double> S = make_scratch<NS, double>(scratch, s, count, in.km, false);
+    SetupRecord r;
+    r.load(S.D, lay.rec);
+    team_fourier_series<NS, double, true>(tm, M, opt, in, r, q.qx, q.qw, S.W, lay, rad, refl, nf, st, Worklist(),
+                                          base + s, &b, s);
+  }
+}
+
+// Per call: kw (3, nch, nobs) on the device; ntab Li-sparse (h/b, b/r) pairs
+// tpar_host and the table of every solve tab_host (nch x nobs, null when
+// ntab == 1), both on the host; br (nobs, nch) output on the device.
+template <int NS>
+int launch_scalar_landmodis(Context& c, const RtOptions& opt, const LambertInputs& in, const double* kw,
+                            const int* tab_host, const double* tpar_host, int ntab, double* rad, double* refl,
+                            double* br, int* nf, int* st, cudaStream_t s) {
+  constexpr int WPB = 2;
+  const int nsolve = in.nobs * in.nch;
+  if (nsolve == 0) return 0;
+  Quad q;
+  std::memset(&q, 0, sizeof(q));
+  gauss_legendre01(NS, q.qx, q.qw);
+  if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
+  BrdfInputs b;
+  std::memset(&b, 0, sizeof(b));
+  {
+    double x[kBrdfAzimuth], w[kBrdfAzimuth];
+    gauss_legendre01(kBrdfAzimuth, x, w);
+    for (int k = 0; k < kBrdfAzimuth; ++k) {
+      b.q.phi[k] = kPIE * x[k];
+      b.q.a[k] = w[k];
+      b.q.c[k] = std::cos(b.q.phi[k]);
+      b.q.s[k] = std::sin(b.q.phi[k]);
+    }
+  }
+  for (int k = 0; k < NS; ++k) b.qx[k] = q.qx[k];
+  // quadrature-to-quadrature tables: Ross-thick, then Li-sparse per parameter pair
+  const size_t tab_elems = (size_t)2 * NS * NS * NS;
+  std::vector<double> qq((size_t)(1 + ntab) * tab_elems);
+  brdf_qq_table(NS, q.qx, b.q, false, 0.0, 0.0, qq.data());
+  for (int t = 0; t < ntab; ++t)
+    brdf_qq_table(NS, q.qx, b.q, true, tpar_host[2 * t], tpar_host[2 * t + 1], qq.data() + (1 + t) * tab_elems);
+  int per_sm = 0;
+  {
+    const size_t smem = sizeof(TeamMem<NS, double>) * WPB;
+    CUDA_TRY(cudaFuncSetAttribute(k_brdf_series<NS, WPB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_brdf_series<NS, WPB>, 32 * WPB, smem));
+    if (per_sm < 1) return set_error(AERORT_RC_CUDA, "BRDF team kernel does not fit on an SM");
+  }
+  const int slice = nsolve < kSetupSlice ? nsolve : kSetupSlice;
+  long nblocks = (long)per_sm * c.num_sms;
+  if (nblocks > (slice + WPB - 1) / WPB) nblocks = (slice + WPB - 1) / WPB;
+  const ScratchLayout<NS> lay(in.km, false);
+  auto up256 = [](size_t v) { return (v + 255) / 256 * 256; };
+  const size_t live_off = up256((size_t)lay.template bytes<double>() * slice);
+  const size_t terms_off = live_off + up256((size_t)slice);
+  const size_t qq_off = terms_off + up256(sizeof(double) * (size_t)BrdfBlock<NS>::total * slice);
+  const size_t tpar_off = qq_off + up256(sizeof(double) * qq.size());
+  const size_t tab_off = tpar_off + up256(sizeof(double) * 2 * (size_t)ntab);
+  const size_t total = tab_off + (tab_host ? up256(sizeof(int) * (size_t)nsolve) : 0);
+  if (int rc = c.pad->scratch.ensure(total)) return rc;
+  if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
+  char* base = (char*)c.pad->scratch.p;
+  // pageable-memory copies: the host buffers may go once the calls return
+  CUDA_TRY(cudaMemcpyAsync(base + qq_off, qq.data(), sizeof(double) * qq.size(), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(base + tpar_off, tpar_host, sizeof(double) * 2 * (size_t)ntab, cudaMemcpyHostToDevice,
+                           s));
+  if (tab_host)
+    CUDA_TRY(cudaMemcpyAsync(base + tab_off, tab_host, sizeof(int) * (size_t)nsolve, cudaMemcpyHostToDevice, s));
+  b.kw = kw;
+  b.tab = tab_host ? (const int*)(base + tab_off) : nullptr;
+  b.tpar = (const double*)(base + tpar_off);
+  b.qq = (const double*)(base + qq_off);
+  b.br = br;
+  b.terms = (double*)(base + terms_off);
+  b.stride = slice;
+  int* counter = (int*)c.pad->counter.p;
+  int* first = counter + 1;
+  k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, nullptr);
+  k_brdf_nadir_first<NS><<<(in.nobs + 127) / 128, 128, 0, s>>>(in, b, first);
+  CUDA_TRY(cudaGetLastError());
+  count_launches(2);
+  LambertInputs in2 = in;
+  in2.nadir_first = first;
+  const size_t smem = sizeof(TeamMem<NS, double>) * WPB;
+  for (int b0 = 0; b0 < nsolve; b0 += slice) {
+    const int cnt = nsolve - b0 < slice ? nsolve - b0 : slice;
+    if (b0 > 0) CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), s));
+    k_brdf_setup<NS><<<(unsigned)((cnt + 31) / 32), 32, 0, s>>>(opt, in2, q, b, base, b0, cnt, rad, refl, nf, st,
+                                                                 (unsigned char*)(base + live_off));
+    k_brdf_series<NS, WPB><<<(unsigned)nblocks, 32 * WPB, smem, s>>>(
+        opt, in2, q, b, base, b0, cnt, counter, (const unsigned char*)(base + live_off), rad, refl, nf, st);
+    CUDA_TRY(cudaGetLastError());
+    count_launches(2);
+  }
+  return 0;
+}
+
 }  // namespace aerort_internal
 
 #define AERORT_INSTANTIATE_RT(NS)                                                                             \
@@ -431,4 +589,7 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
       const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t, const aerort::Worklist&);                            \
   template int aerort_internal::launch_scalar_lambert_fixed<NS, float>(                                        \
       const aerort::RtOptions&, const aerort::LambertInputs&, void*, size_t, int*, int,                         \
-      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t, const aerort::Worklist&);
+      const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t, const aerort::Worklist&); \
+  template int aerort_internal::launch_scalar_landmodis<NS>(                                                   \
+      aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, const double*,          \
+      const int*, const double*, int, double*, double*, double*, int*, int*, cudaStream_t);

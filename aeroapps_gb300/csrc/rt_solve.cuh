@@ -10,6 +10,7 @@
 // uses an algebraically equal form built on expm1; the double instantiation
 // keeps the reference's formulas.
 #pragma once
+#include "rt_brdf.cuh"
 #include "rt_scalar.cuh"
 
 namespace aerort {
@@ -1167,10 +1168,15 @@ RT_HD void solve_finish(const RtOptions& opt, const LambertInputs& in, const Set
 // first-order single scatter, beam attenuation.  Leaves the per-layer inputs of
 // the Fourier series in scratch and fills r.  Returns false when the pixel is
 // finished already (MISSING inputs or a bad layer: outputs written).
+// With `brdf` (VLIDORT_Scalar_LandMODIS, VLIDORT_BRDF_MODIS.F90:113-185) the
+// surface is the RTLS BRDF instead of the albedo: its exact direct-bounce
+// value BR feeds the first-order correction and the BR output (a negative BR
+// gives -500 in radiance, reflectance and BR and no solve), and the solve's
+// beam and view Fourier terms go to block `bidx` of brdf->terms.
 template <int NS, typename T>
 RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, const double* tu, const double* wu,
                        const SolveScratch<T>& SS, double* radiance, double* reflectance, int* nfourier,
-                       int* status, SetupRecord& r) {
+                       int* status, SetupRecord& r, const BrdfInputs* brdf = nullptr, long bidx = 0) {
   const Scratch& S = SS.D;
   const ScratchT<T>& W = SS.W;
   const int nch = in.nch, j = sidx / nch, i = sidx % nch;
@@ -1178,18 +1184,36 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
   const int L = in.nlay ? in.nlay[j] : in.km, ngreek = in.nmom;
   const ScratchLayout<NS> lay(in.km);
   auto is_missing = [&](double x) { return fabs(x / in.missing - 1.0) < 0.001; };
-  const double sza = in.sza[j], vza = in.vza[j], raa = in.raa[j], alb = in.albedo[o];
+  const double sza = in.sza[j], vza = in.vza[j], raa = in.raa[j], alb = brdf ? 0.0 : in.albedo[o];
   if (nfourier) nfourier[o] = -1;
   if (status) status[o] = RT_OK;
-  if (is_missing(sza) || is_missing(vza) || is_missing(raa) || is_missing(alb)) {
+  if (is_missing(sza) || is_missing(vza) || is_missing(raa) || (!brdf && is_missing(alb))) {
     radiance[o] = in.missing; reflectance[o] = in.missing;
+    if (brdf) brdf->br[o] = in.missing;
     return false;
+  }
+  double refl_db = alb;  // surface reflectance of the direct bounce
+  if (brdf) {
+    const long w = (long)i + (long)nch * j;
+    const double* kw = brdf->kw + 3 * w;
+    const int t = brdf->tab ? brdf->tab[w] : 0;
+    const double hb = brdf->tpar[2 * t], br = brdf->tpar[2 * t + 1];
+    const double b = brdf_exact(kw, hb, br, sza, vza, raa);
+    brdf->br[o] = b < 0.0 ? -500.0 : b;
+    if (b < 0.0) {
+      radiance[o] = -500.0; reflectance[o] = -500.0;
+      return false;
+    }
+    refl_db = b;
+    const Scratch B{brdf->terms + bidx, brdf->stride};
+    brdf_solve_terms<NS>(brdf->q, brdf->qx, kw, hb, br, sza, vza, B);
+    B[BrdfBlock<NS>::w + 3] = (double)t;
   }
   r.o = o;
   r.L = L;
   r.NM = (2 * NS - 1 < ngreek) ? 2 * NS - 1 : ngreek;
   r.msmode = opt.do_focorr != 0;
-  r.albedo = alb;
+  r.albedo = brdf ? 1.0 : alb;  // a BRDF surface reflects in every Fourier term
   r.raa = raa;
   r.sza = sza;
   const double mu_u = cos(kDTR * vza), cos_sza = cos(sza * kDTR);
@@ -1310,15 +1334,15 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
       if (enhanced) {
         for (int k = 0; k <= L; ++k) W[lay.wh + k] = (float)S[lay.hgt + k];
         for (int k = 0; k < L; ++k) W[lay.we + k] = (float)S[lay.ext + k];
-        fo_enhanced_f32(opt, L, sza, vza, phi, alb, tu, wu, W, lay.wh, lay.we, S, lay.hgt, lay.ext, lay.escat, &ss,
+        fo_enhanced_f32(opt, L, sza, vza, phi, refl_db, tu, wu, W, lay.wh, lay.we, S, lay.hgt, lay.ext, lay.escat, &ss,
                         &db);
       } else {
-        fo_single_scatter_chord(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat,
+        fo_single_scatter_chord(opt, enhanced, L, sza, vza, phi, refl_db, tu, wu, S, lay.hgt, lay.ext, lay.escat,
                                 lay.dts, &ss, &db);
       }
     }
     else
-      fo_single_scatter_ref(opt, enhanced, L, sza, vza, phi, alb, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts,
+      fo_single_scatter_ref(opt, enhanced, L, sza, vza, phi, refl_db, tu, wu, S, lay.hgt, lay.ext, lay.escat, lay.dts,
                             &ss, &db);
   }
   // ---------------------------------------------------------------- beam attenuation

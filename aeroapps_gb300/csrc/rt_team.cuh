@@ -788,21 +788,33 @@ RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<
 // with cum_L the surface term.  Nothing per layer is stored, so the term's
 // memory traffic is its inputs W alone.  Every lane returns the same status
 // and *out.
-template <int NS, typename T>
+//
+// BRDF = true (the RTLS surface of VLIDORT_Scalar_LandMODIS, FP64): the
+// surface reflects in every term, with the Fourier components of rt_brdf.cuh
+// in place of the albedo -- BVP rows R2_HOMP/R2_HOMM and R2_BEAM with
+// QUAD_STRMWTS(j) BRDF_F(m, i, j) (vlidort_bvproblem.f90:558-614, 1680-1736),
+// direct beam ATTN BRDF_F_0(m, i) per stream (vlidort_miscsetups.f90:1517-1545),
+// and the view-angle surface source sum_j STOKES_DOWNSURF(j) USER_BRDF_F(m, j)
+// (vlidort_intensity.f90:1378-1396).  `brdf` holds the launch's tables and
+// `bidx` is this solve's block.
+template <int NS, typename T, bool BRDF = false>
 RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& c, const RtOptions& opt, int m,
-                            const ScratchT<T>& W, const ScratchLayout<NS>& lay, T* out) {
+                            const ScratchT<T>& W, const ScratchLayout<NS>& lay, T* out,
+                            const BrdfInputs* brdf = nullptr, long bidx = 0) {
+  static_assert(!BRDF || sizeof(T) == sizeof(double), "the BRDF surface runs in FP64");
   constexpr int LD = TeamMem<NS, T>::LD;
   constexpr int LR = TeamMem<NS, T>::LR;
   const int N = NS, NM = c.NM, L = c.L;
-  const bool incl_surface = (m == 0) && (c.albedo != (T)0);
+  const bool incl_surface = BRDF ? true : ((m == 0) && (c.albedo != (T)0));
   const T surface_factor = (m == 0) ? (T)2 : (T)1;
   const T delta_factor = (m == 0) ? (T)1 : (T)2;
   const bool localbeam = incl_surface && c.refl_directbeam;
-  T direct_beam = 0;
+  T direct_beam = 0, beam_attn = 0;
   if (localbeam) {
     T x0 = (T)4 * c.cos_sza / delta_factor;
     x0 = (T)opt.flux_factor * x0 / (T)kPI4;
-    direct_beam = x0 * c.trans_solar_beam * c.albedo;
+    beam_attn = x0 * c.trans_solar_beam;
+    direct_beam = beam_attn * c.albedo;
   }
   team_legendre<NS, T>(tm, M, c, m);
   T* K = M.work;  // interface systems, row-major (team_lu_solve)
@@ -927,34 +939,87 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
   // surface closure on the bottom layer (slot prev)
   const int bl = prev;
   const T kmult = incl_surface ? surface_factor * c.albedo : (T)0;
-  if (tm.lane < N) {
-    const int k = tm.lane;
-    T sp = 0, sm = 0;
-    for (int j = 0; j < N; ++j) {
-      sp += M.cqx[j] * M.cqw[j] * M.P[bl][j + LD * k];
-      sm += M.cqx[j] * M.cqw[j] * M.Q[bl][j + LD * k];
-    }
-    M.dpi[k] = sp * kmult;   // r2p
-    M.dmi[k] = sm * kmult;   // r2m
-  }
-  T r2b = 0;
-  for (int j = 0; j < N; ++j) r2b += M.cqx[j] * M.cqw[j] * M.wb[bl][j];
-  r2b *= kmult;
-  tm.sync();
   const int nbc = rhs_col(N);
-  for (int e = tm.lane; e < N * N; e += kTeam) {
-    const int j = e % N, i = e / N;
-    T s = M.P[bl][i + LD * j] - M.dmi[j];
-    for (int k = 0; k < N; ++k) s += (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.F[k + LD * j];
-    K[LR * i + j] = s;
+  Scratch Bb{nullptr, 0};
+  if constexpr (BRDF) {
+    // R(i, l) = BRDF_F(m, i, l) in M.Vp, R2P / R2M in the free layer slot,
+    // R2_BEAM(i) in M.dpi, DIRECT_BEAM(i) in M.dmi
+    const int fr = 1 - bl;
+    using BB = BrdfBlock<NS>;
+    Bb = Scratch{brdf->terms + bidx, brdf->stride};
+    const double fiso = Bb[BB::w], fvol = Bb[BB::w + 1], fgeo = Bb[BB::w + 2];
+    const int t = (int)Bb[BB::w + 3];
+    const double* qv = brdf->qq + (long)m * NS * NS;
+    const double* qg = brdf->qq + ((long)(1 + t) * 2 * NS + m) * NS * NS;
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e / N, l = e % N;
+      double r = (m == 0) ? fiso : 0.0;
+      r += fvol * qv[i * NS + l];
+      r += fgeo * qg[i * NS + l];
+      M.Vp[i + LD * l] = (T)r;
+    }
+    tm.sync();
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int i = e % N, k = e / N;
+      T sp = 0, sm = 0;
+      for (int l = 0; l < N; ++l) {
+        const T ax = M.cqx[l] * M.cqw[l] * M.Vp[i + LD * l];
+        sp += ax * M.P[bl][l + LD * k];
+        sm += ax * M.Q[bl][l + LD * k];
+      }
+      M.P[fr][i + LD * k] = surface_factor * sp;
+      M.Q[fr][i + LD * k] = surface_factor * sm;
+    }
+    if (tm.lane < N) {
+      const int i = tm.lane;
+      T s = 0;
+      for (int l = 0; l < N; ++l) s += M.cqx[l] * M.cqw[l] * M.Vp[i + LD * l] * M.wb[bl][l];
+      M.dpi[i] = surface_factor * s;
+      M.dmi[i] = localbeam ? beam_attn * (T)Bb[BB::r0 + (long)m * NS + i] : (T)0;
+    }
+    tm.sync();
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int j = e % N, i = e / N;
+      T s = M.P[bl][i + LD * j] - M.Q[fr][i + LD * j];
+      for (int k = 0; k < N; ++k) s += (M.Q[bl][i + LD * k] - M.P[fr][i + LD * k]) * M.t[bl][k] * M.F[k + LD * j];
+      K[LR * i + j] = s;
+    }
+    if (tm.lane < N) {
+      const int i = tm.lane;
+      T s = -M.wb[bl][N + i] + M.dpi[i] + M.dmi[i];
+      for (int k = 0; k < N; ++k) s -= (M.Q[bl][i + LD * k] - M.P[fr][i + LD * k]) * M.t[bl][k] * M.f[k];
+      K[LR * i + nbc] = s;
+    }
+    tm.sync();
+  } else {
+    if (tm.lane < N) {
+      const int k = tm.lane;
+      T sp = 0, sm = 0;
+      for (int j = 0; j < N; ++j) {
+        sp += M.cqx[j] * M.cqw[j] * M.P[bl][j + LD * k];
+        sm += M.cqx[j] * M.cqw[j] * M.Q[bl][j + LD * k];
+      }
+      M.dpi[k] = sp * kmult;   // r2p
+      M.dmi[k] = sm * kmult;   // r2m
+    }
+    T r2b = 0;
+    for (int j = 0; j < N; ++j) r2b += M.cqx[j] * M.cqw[j] * M.wb[bl][j];
+    r2b *= kmult;
+    tm.sync();
+    for (int e = tm.lane; e < N * N; e += kTeam) {
+      const int j = e % N, i = e / N;
+      T s = M.P[bl][i + LD * j] - M.dmi[j];
+      for (int k = 0; k < N; ++k) s += (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.F[k + LD * j];
+      K[LR * i + j] = s;
+    }
+    if (tm.lane < N) {
+      const int i = tm.lane;
+      T s = -M.wb[bl][N + i] + r2b + (localbeam ? direct_beam : (T)0);
+      for (int k = 0; k < N; ++k) s -= (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.f[k];
+      K[LR * i + nbc] = s;
+    }
+    tm.sync();
   }
-  if (tm.lane < N) {
-    const int i = tm.lane;
-    T s = -M.wb[bl][N + i] + r2b + (localbeam ? direct_beam : (T)0);
-    for (int k = 0; k < N; ++k) s -= (M.Q[bl][i + LD * k] - M.dpi[k]) * M.t[bl][k] * M.f[k];
-    K[LR * i + nbc] = s;
-  }
-  tm.sync();
   if (!team_lu_solve<LR>(tm, N, K, 1, M.red)) return RT_BVP_SINGULAR;
   // M_{L-1} (Mc) from the solved right-hand side, L_{L-1} (Lc) in M.gup
   T* Mc = M.hm1;
@@ -978,10 +1043,17 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
     }
     tm.sync();
     T s = 0;
-    for (int i = 0; i < N; ++i) s += M.red[i];
-    cum = kmult * s;
     const bool incl_directrf = localbeam && !opt.do_focorr && !c.msmode;
-    if (incl_directrf) cum += direct_beam;
+    if constexpr (BRDF) {
+      using BB = BrdfBlock<NS>;
+      for (int i = 0; i < N; ++i) s += M.red[i] * (T)Bb[BB::ur + (long)m * NS + i];
+      cum = surface_factor * s;
+      if (incl_directrf) cum += beam_attn * (T)Bb[BB::ur0 + m];
+    } else {
+      for (int i = 0; i < N; ++i) s += M.red[i];
+      cum = kmult * s;
+      if (incl_directrf) cum += direct_beam;
+    }
     tm.sync();
   }
   T d = 0;
@@ -994,11 +1066,12 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
 
 // The Fourier series of one set-up solve, run by the whole team; lane 0 writes
 // the outputs.
-template <int NS, typename T>
+template <int NS, typename T, bool BRDF = false>
 RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOptions& opt, const LambertInputs& in,
                                const SetupRecord& r, const double* qx, const double* qw, const ScratchT<T>& W,
                                const ScratchLayout<NS>& lay, double* radiance, double* reflectance,
-                               int* nfourier, int* status, const Worklist& wl = Worklist(), int sidx = 0) {
+                               int* nfourier, int* status, const Worklist& wl = Worklist(), int sidx = 0,
+                               const BrdfInputs* brdf = nullptr, long bidx = 0) {
   SolveCtx<NS, T> c;
   make_ctx<NS, T>(r, qx, qw, c);
   if (tm.lane < NS) {
@@ -1015,7 +1088,7 @@ RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOption
   int m = 0, st = RT_OK;
   for (m = 0; m <= r.n_fouriers; ++m) {
     T sf = 0;
-    st = team_fourier_term<NS, T>(tm, M, c, opt, m, W, lay, &sf);
+    st = team_fourier_term<NS, T, BRDF>(tm, M, c, opt, m, W, lay, &sf, brdf, bidx);
     if (st != RT_OK || sum.add(opt, r, m, (double)sf)) break;
   }
   if (tm.lane == 0) {

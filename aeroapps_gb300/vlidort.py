@@ -50,6 +50,41 @@ def vlidort_scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nM
     return rad, refl, rc
 
 
+def vlidort_scalar_landmodis(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g,
+                             pmom, pe, he, te, kernel_wt, param, solar_zenith, relat_azymuth, sensor_zenith,
+                             MISSING=MISSING, verbose=0, diagnostics=False):
+    """VLIDORT_Scalar_LandMODIS: scalar TOA radiance/reflectance over the MODIS
+    RTLS BRDF (geo_vlidort/VLIDORT_BRDF_MODIS.F90:34-200).
+
+    As vlidort_scalar_lambert with the albedo replaced by kernel_wt(3,nch,nobs)
+    (fiso, fvol, fgeo) and param(2,nch,nobs) (Li-sparse h/b, b/r).  Returns
+    (radiance, reflectance, BR, rc), plus (nfourier, status) with
+    diagnostics=True; BR(nobs,nch) is the exact direct-bounce BRDF (-500 where
+    the kernel combination is negative, as the reference)."""
+    arrs = [_f64(channels), _f64(ROT), _f64(depol), _f64(tau), _f64(ssa), _f64(g), _f64(pmom), _f64(pe), _f64(he),
+            _f64(te), _f64(kernel_wt), _f64(param), _f64(solar_zenith), _f64(relat_azymuth), _f64(sensor_zenith)]
+    ch, ROT, depol, tau, ssa, g, pmom, pe, he, te, kw, par, sza, raa, vza = arrs
+    if ROT.shape != (km, nobs, nch) or tau.shape != (km, nch, nobs) or he.shape != (km + 1, nobs):
+        raise ValueError("array shapes do not match (km, nch, nobs) = (%d, %d, %d)" % (km, nch, nobs))
+    if kw.shape != (3, nch, nobs) or par.shape != (2, nch, nobs):
+        raise ValueError("kernel_wt must have shape (3, nch, nobs) and param (2, nch, nobs)")
+    rad = np.zeros((nobs, nch), np.float64, order="F")
+    refl = np.zeros_like(rad)
+    br = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    P = lambda a: _lib.ptr(a, _lib.P_d)
+    rc = _lib.lib().aerort_vlidort_scalar_landmodis_ex(
+        km, nch, nobs, P(ch), nstreams, int(bool(plane_parallel)), nMom, nPol, P(ROT), P(depol), P(tau), P(ssa), P(g),
+        P(pmom), P(pe), P(he), P(te), P(kw), P(par), P(sza), P(raa), P(vza), float(MISSING), int(verbose), P(rad),
+        P(refl), P(br), _lib.ptr(nf, _lib.P_i), _lib.ptr(st, _lib.P_i))
+    if rc >= 1000:
+        raise RuntimeError("aerort_vlidort_scalar_landmodis rc=%d: %s" % (rc, _lib.last_error()))
+    if diagnostics:
+        return rad, refl, br, rc, nf, st
+    return rad, refl, br, rc
+
+
 def vlidort_scalar_lambert_dev(km, nch, nobs, nstreams, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith,
                                relat_azymuth, sensor_zenith, radiance, reflectance, nfourier=None, status=None,
                                MISSING=MISSING, plane_parallel=False, stream=0):

@@ -257,6 +257,51 @@ int aerort_vlidort_vector_lambert_batch_dev(int km, int nch, int nobs, int nstre
                                             double* radiance_VL, double* reflectance_VL, double* Q, double* U,
                                             int* nfourier, int* status, void* stream);
 
+/* VLIDORT_Scalar_LandMODIS (geo_vlidort/VLIDORT_BRDF_MODIS.F90:34-200): the
+ * scalar solve of aerort_vlidort_scalar_lambert over the MODIS RTLS BRDF of
+ * VLIDORT_LANDMODIS_SingleGeom (RTSI/VLIDORT2p8p3/VLIDORT_SurfaceMod.F90
+ * :1376-1596) -- Lambertian, Ross-thick and Li-sparse kernels with amplitudes
+ * kernel_wt(3, nch, nobs) = (fiso, fvol, fgeo) and Li-sparse parameters
+ * param(2, nch, nobs) = (h/b, b/r), 50 azimuth streams -- in place of the
+ * albedo; same argument list as the reference (BR(nobs, nch): the exact
+ * direct-bounce BRDF of each pixel and channel).  A pixel with MISSING angles
+ * gets MISSING radiance, reflectance and BR; a negative BR gives -500 in all
+ * three and no solve (as the reference).  The reference's MISSING checks of
+ * kernel_wt and param never skip a pixel (their CYCLE ends only their own
+ * loop), so none is made here either.  FP64; at most 256 distinct param pairs
+ * per call (AERORT_RC_ARG beyond).  rc as aerort_vlidort_scalar_lambert. */
+int aerort_vlidort_scalar_landmodis(int km, int nch, int nobs, const double* channels, int nstreams,
+                                    int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                    const double* tau, const double* ssa, const double* g, const double* pmom,
+                                    const double* pe, const double* he, const double* te, const double* kernel_wt,
+                                    const double* param, const double* solar_zenith, const double* relat_azymuth,
+                                    const double* sensor_zenith, double MISSING, int verbose,
+                                    double* radiance_VL_SURF, double* reflectance_VL_SURF, double* BR);
+/* Same, plus nfourier(nobs,nch) and status(nobs,nch) (either may be NULL). */
+int aerort_vlidort_scalar_landmodis_ex(int km, int nch, int nobs, const double* channels, int nstreams,
+                                       int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                       const double* tau, const double* ssa, const double* g, const double* pmom,
+                                       const double* pe, const double* he, const double* te, const double* kernel_wt,
+                                       const double* param, const double* solar_zenith, const double* relat_azymuth,
+                                       const double* sensor_zenith, double MISSING, int verbose,
+                                       double* radiance_VL_SURF, double* reflectance_VL_SURF, double* BR,
+                                       int* nfourier, int* status);
+/* Batched device form (no counterpart routine in the reference): arrays on
+ * the device as aerort_vlidort_scalar_lambert_batch_dev (nlay and FP32
+ * optics optional), kernel_wt(3, nch, nobs) on the device, param_host(2, nch,
+ * nobs) on the HOST (the launch builds one Fourier table per distinct pair),
+ * BR(nobs, nch) out on the device.  Enqueued on `stream`; the table upload
+ * is a pageable-memory copy, so this call does not belong in a stream capture. */
+int aerort_vlidort_scalar_landmodis_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                              const int* nlay, const double* ROT, const double* depol,
+                                              const double* tau, const double* ssa, const double* pmom,
+                                              const float* tau_f, const float* ssa_f, const float* pmom_f,
+                                              const double* he, const double* kernel_wt, const double* param_host,
+                                              const double* solar_zenith, const double* relat_azymuth,
+                                              const double* sensor_zenith, double MISSING, double* radiance_VL_SURF,
+                                              double* reflectance_VL_SURF, double* BR, int* nfourier, int* status,
+                                              void* stream);
+
 /* Edge pressure pe (Pa), height above the surface ze (m) and temperature te
  * (K), each (km+1,nobs), from layer air density airdens (kg m-3) and pressure
  * thickness delp (Pa), each (km,nobs), and the top pressure ptop (Pa).

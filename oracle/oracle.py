@@ -35,6 +35,7 @@ def lib():
         _lib.oracle_vlidort_vector_solve.restype = ctypes.c_int
         _lib.oracle_vector_lambert.restype = ctypes.c_int
         _lib.oracle_scalar_lambert.restype = ctypes.c_int
+        _lib.oracle_scalar_landmodis.restype = ctypes.c_int
         _lib.oracle_get_aop_vector.restype = ctypes.c_int
         _lib.oracle_set_asymtx_tol.restype = None
         _lib.oracle_rot_calc.restype = ctypes.c_int
@@ -145,6 +146,26 @@ def scalar_lambert(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol
                                      _p(nf, P_i), _p(st, P_i),
                                      None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
     return rad, refl, rc, nf, st
+
+
+def scalar_landmodis(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g, pmom,
+                     pe, he, te, kernel_wt, param, solar_zenith, relat_azymuth, sensor_zenith, MISSING, verbose=0,
+                     nlay=None):
+    """Oracle VLIDORT_Scalar_LandMODIS; kernel_wt (3, nch, nobs), param (2, nch, nobs).
+    Returns (radiance, reflectance, BR, rc, nfourier, status)."""
+    F = lambda a: np.asfortranarray(a, np.float64)
+    arr = [F(x) for x in (channels, ROT, depol, tau, ssa, g, pmom, pe, he, te, kernel_wt, param, solar_zenith,
+                          relat_azymuth, sensor_zenith)]
+    rad = np.zeros((nobs, nch), order="F")
+    refl = np.zeros_like(rad)
+    br = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    rc = lib().oracle_scalar_landmodis(km, nch, nobs, _p(arr[0], P_d), nstreams, int(plane_parallel), nMom, nPol,
+                                       *[_p(a, P_d) for a in arr[1:]], ctypes.c_double(MISSING), int(verbose),
+                                       _p(rad, P_d), _p(refl, P_d), _p(br, P_d), _p(nf, P_i), _p(st, P_i),
+                                       None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
+    return rad, refl, br, rc, nf, st
 
 
 def vector_lambert(km, nch, nobs, nstreams, plane_parallel, nMom, ROT, depol, alpha, tau, ssa, pmom, he, albedo,

@@ -63,4 +63,14 @@ void fo_geometry(const OracleOpts* o, int L, const double* heights, const std::v
                  const std::vector<double>& ext, const std::vector<double>& dts, double sza, double vza,
                  double raa, FoGeom& G);
 
+// One VBRDF kernel value (brdf_oracle.cpp): incident (xi, sxi), reflected
+// (xj, sxj), azimuth cosine/sine; `which` as vlidort_pars.f90:466-474.
+double brdf_kernel(int which, const double* pars, double xi, double sxi, double xj, double sxj, double cphi,
+                   double sphi);
+
 }  // namespace orc
+
+extern "C" int oracle_brdf_supplement(int nk, const int* which, const double* factors, const double* pars_in,
+                                      int do_shadow, int nstreams_brdf, int N, int nmom, double sza, int nvza,
+                                      const double* vza, int nraa, const double* raa, double* f, double* f0,
+                                      double* uf, double* uf0, double* exactdb);

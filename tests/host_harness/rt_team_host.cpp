@@ -79,3 +79,75 @@ extern "C" int team_scalar_lambert_mixed(int km, int nch, int nobs, int nstreams
   return dispatch<float>(km, nch, nobs, nstreams, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nadir,
                          missing, max_fourier, rad, refl, nf, st);
 }
+
+// The RTLS BRDF surface (VLIDORT_Scalar_LandMODIS) through the same team
+// solve: Fourier tables and per-solve blocks built as the CUDA entry point
+// builds them, one solve at a time.  kw (3, nch, nobs), param (2, nch, nobs).
+template <int NS>
+static int run_brdf(const RtOptions& opt, const LambertInputs& in, const double* kw, const double* param,
+                    double* rad, double* refl, double* br, int* nf, int* st) {
+  double qx[NS], qw[NS], tu[4], wu[4];
+  gl(NS, qx, qw);
+  gl(opt.nfine > 0 ? opt.nfine : 1, tu, wu);
+  BrdfInputs b{};
+  double ax[kBrdfAzimuth], aw[kBrdfAzimuth];
+  gl(kBrdfAzimuth, ax, aw);
+  for (int k = 0; k < kBrdfAzimuth; ++k) {
+    b.q.phi[k] = kPIE * ax[k];
+    b.q.a[k] = aw[k];
+    b.q.c[k] = std::cos(b.q.phi[k]);
+    b.q.s[k] = std::sin(b.q.phi[k]);
+  }
+  for (int q = 0; q < NS; ++q) b.qx[q] = qx[q];
+  // one Li-sparse table per (pixel, channel): tab[w] = w
+  const int nsolve = in.nobs * in.nch;
+  std::vector<double> tpar(2 * nsolve), qq((size_t)(1 + nsolve) * 2 * NS * NS * NS);
+  std::vector<int> tab(nsolve);
+  brdf_qq_table(NS, qx, b.q, false, 0.0, 0.0, qq.data());
+  for (int w = 0; w < nsolve; ++w) {
+    tab[w] = w;
+    tpar[2 * w] = param[2 * w];
+    tpar[2 * w + 1] = param[2 * w + 1];
+    brdf_qq_table(NS, qx, b.q, true, tpar[2 * w], tpar[2 * w + 1], qq.data() + (size_t)(1 + w) * 2 * NS * NS * NS);
+  }
+  std::vector<double> terms(BrdfBlock<NS>::total);
+  b.kw = kw; b.tab = tab.data(); b.tpar = tpar.data(); b.qq = qq.data(); b.br = br;
+  b.terms = terms.data(); b.stride = 1;
+  ScratchLayout<NS> lay(in.km, false);
+  std::vector<double> scr((lay.template bytes<double>() + 7) / 8);
+  auto M = std::make_unique<TeamMem<NS, double>>();
+  const SolveScratch<double> S = make_scratch<NS, double>(scr.data(), 0, 1, in.km, false);
+  for (int s = 0; s < nsolve; ++s) {
+    SetupRecord r;
+    if (!solve_setup<NS, double>(opt, in, s, tu, wu, S, rad, refl, nf, st, r, &b, 0)) continue;
+    r.store(S.D, lay.rec);
+    SetupRecord rb;
+    rb.load(S.D, lay.rec);
+    std::barrier<> bar(kTeam);
+    std::vector<std::thread> th;
+    for (int lane = 0; lane < kTeam; ++lane)
+      th.emplace_back([&, lane] {
+        const Team tm{lane, bar_sync, &bar};
+        team_fourier_series<NS, double, true>(tm, *M, opt, in, rb, qx, qw, S.W, lay, rad, refl, nf, st, Worklist(), 0,
+                                              &b, 0);
+      });
+    for (auto& t : th) t.join();
+  }
+  return 0;
+}
+extern "C" int team_scalar_landmodis(int km, int nch, int nobs, int nstreams, int nmom, const double* rot,
+    const double* depol, const double* tau, const double* ssa, const double* pmom, const double* he,
+    const double* kw, const double* param, const double* sza, const double* raa, const double* vza,
+    const int* nadir, double missing, double* rad, double* refl, double* br, int* nf, int* st) {
+  RtOptions opt{1, 1, g_plane_parallel, 1, 3, 3, kAccuracySingle, 6371.0, 1.0, -1};
+  LambertInputs in{km, nch, nobs, nmom, rot, depol, tau, ssa, pmom, he, nullptr, sza, raa, vza, nullptr, nullptr,
+                   nullptr, nullptr, nadir, missing};
+  switch (nstreams) {
+    case 4: return run_brdf<4>(opt, in, kw, param, rad, refl, br, nf, st);
+    case 6: return run_brdf<6>(opt, in, kw, param, rad, refl, br, nf, st);
+    case 8: return run_brdf<8>(opt, in, kw, param, rad, refl, br, nf, st);
+    case 12: return run_brdf<12>(opt, in, kw, param, rad, refl, br, nf, st);
+    case 16: return run_brdf<16>(opt, in, kw, param, rad, refl, br, nf, st);
+  }
+  return -1;
+}

@@ -128,3 +128,43 @@ def test_plane_parallel_flag(host_lib, team_lib, nstreams, km):
     assert np.max(np.abs(rad / orad - 1)) < 1e-9
     assert np.max(np.abs(mrad / orad - 1)) < 1e-4
     assert np.array_equal(tnf, nf1) and np.all(tst == 0) and np.max(np.abs(trad / rad1 - 1)) < 1e-12
+
+
+def _host_brdf(lib, c, nstreams, kw, par):
+    P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    keep = [np.asfortranarray(c[k], np.float64) for k in ("ROT", "depol", "tau", "ssa", "pmom", "he")]
+    kwf, parf = np.asfortranarray(kw, np.float64), np.asfortranarray(par, np.float64)
+    ang = [np.ascontiguousarray(c[k], np.float64) for k in ("sza", "raa", "vza")]
+    nobs, nch = c["ncol"], c["nch"]
+    rad = np.zeros((nobs, nch), order="F")
+    refl = np.zeros_like(rad)
+    br = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    first = np.array([nobs], np.int32)
+    Ip = ctypes.POINTER(ctypes.c_int)
+    lib.team_scalar_landmodis(c["km"], nch, nobs, nstreams, c["nmom"], *[P(a) for a in keep], P(kwf), P(parf),
+                              *[P(a) for a in ang], first.ctypes.data_as(Ip), ctypes.c_double(MISSING), P(rad),
+                              P(refl), P(br), nf.ctypes.data_as(Ip), st.ctypes.data_as(Ip))
+    return rad, refl, br, nf, st
+
+
+@pytest.mark.parametrize("nstreams,km", [(4, 10), (8, 6)])
+def test_team_solver_over_modis_brdf_matches_oracle(team_lib, nstreams, km):
+    # the RTLS surface of VLIDORT_Scalar_LandMODIS through the team solve
+    # (one std::thread per lane): same Fourier terms, radiance within 1e-9,
+    # BR exact; one (pixel, channel) with an unphysical kernel set gives -500
+    from rt_cases import modis_brdf
+    c = random_aop_case(nstreams, km, nobs=3, nch=2, seed=km + 5 * nstreams)
+    kw, par = modis_brdf(3, 2, seed=nstreams, negative=[(1, 0)])
+    rad, refl, br, nf, st = _host_brdf(team_lib, c, nstreams, kw, par)
+    a = rt_args(c, nstreams)
+    orad, orefl, obr, orc, onf, ost = oracle.scalar_landmodis(*a[:17], kw, par, c["sza"], c["raa"], c["vza"],
+                                                              MISSING)
+    assert orc == 0
+    assert obr[1, 0] == -500.0 and br[1, 0] == -500.0 and rad[1, 0] == -500.0 and orad[1, 0] == -500.0
+    ok = obr != -500.0
+    assert np.max(np.abs(br[ok] - obr[ok])) < 1e-14
+    assert np.array_equal(nf[ok], onf[ok]) and np.all(st == 0)
+    assert np.max(np.abs(rad[ok] / orad[ok] - 1)) < 1e-9
+    assert np.max(np.abs(refl[ok] / orefl[ok] - 1)) < 1e-9
