@@ -66,7 +66,7 @@ RT_HD double brdf_li_sparse(double hb, double br, double xi, double sxi, double 
 
 // BRDF inputs of a launch.
 struct BrdfInputs {
-  const double* kw;    // (3, nch, nobs) kernel amplitudes fiso, fvol, fgeo
+  const double* kw;    // (3, nch, nobs) kernel amplitudes fiso, fgeo, fvol (the reference's kernel_wt order)
   const int* tab;      // (nch, nobs) Li-sparse parameter table of each solve
   const double* tpar;  // (2, ntab) h/b, b/r of each table
   const double* qq;    // Fourier tables: Ross-thick [m][i][j], then Li-sparse [t][m][i][j], m < 2N
@@ -92,9 +92,9 @@ RT_HD double brdf_exact(const double* kw, double hb, double br, double sza, doub
   const double mu0 = cos(sza * kDTR), s0 = sqrt(1.0 - mu0 * mu0);
   const double mu = cos(vza * kDTR), su = sqrt(1.0 - mu * mu);
   const double phi = raa * kDTR, cp = cos(phi), sp = sin(phi);
-  double b = kw[0] * 1.0;
-  b += kw[1] * brdf_ross_thick(mu0, s0, mu, su, cp);
-  b += kw[2] * brdf_li_sparse(hb, br, mu0, s0, mu, su, cp, sp);
+  double b = kw[0] * 1.0;  // Lambertian (fiso), Ross-thick (fvol), Li-sparse (fgeo), the supplement's order
+  b += kw[2] * brdf_ross_thick(mu0, s0, mu, su, cp);
+  b += kw[1] * brdf_li_sparse(hb, br, mu0, s0, mu, su, cp, sp);
   return b;
 }
 
@@ -129,15 +129,15 @@ RT_HD void brdf_solve_terms(const BrdfQuad& q, const double* qx, const double* k
       }
       const double help = (m == 0) ? 1.0 : 2.0;
       double v = (m == 0) ? kw[0] : 0.0;
-      v += kw[1] * (help * sv);
-      v += kw[2] * (help * sg);
+      v += kw[2] * (help * sv);
+      v += kw[1] * (help * sg);
       const long e = p < NS ? BB::r0 + (long)m * NS + p : (p < 2 * NS ? BB::ur + (long)m * NS + (p - NS) : BB::ur0 + m);
       B[e] = v;
     }
   }
-  B[BB::w] = kw[0];
-  B[BB::w + 1] = kw[1];
-  B[BB::w + 2] = kw[2];
+  B[BB::w] = kw[0];      // fiso
+  B[BB::w + 1] = kw[2];  // fvol
+  B[BB::w + 2] = kw[1];  // fgeo
 }
 
 // Host: the quadrature-to-quadrature Fourier table of one kernel (Ross-thick

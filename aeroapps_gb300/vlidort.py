@@ -57,7 +57,7 @@ def vlidort_scalar_landmodis(km, nch, nobs, channels, nstreams, plane_parallel, 
     RTLS BRDF (geo_vlidort/VLIDORT_BRDF_MODIS.F90:34-200).
 
     As vlidort_scalar_lambert with the albedo replaced by kernel_wt(3,nch,nobs)
-    (fiso, fvol, fgeo) and param(2,nch,nobs) (Li-sparse h/b, b/r).  Returns
+    (fiso, fgeo, fvol) and param(2,nch,nobs) (Li-sparse h/b, b/r).  Returns
     (radiance, reflectance, BR, rc), plus (nfourier, status) with
     diagnostics=True; BR(nobs,nch) is the exact direct-bounce BRDF (-500 where
     the kernel combination is negative, as the reference)."""

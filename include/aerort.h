@@ -261,7 +261,7 @@ int aerort_vlidort_vector_lambert_batch_dev(int km, int nch, int nobs, int nstre
  * scalar solve of aerort_vlidort_scalar_lambert over the MODIS RTLS BRDF of
  * VLIDORT_LANDMODIS_SingleGeom (RTSI/VLIDORT2p8p3/VLIDORT_SurfaceMod.F90
  * :1376-1596) -- Lambertian, Ross-thick and Li-sparse kernels with amplitudes
- * kernel_wt(3, nch, nobs) = (fiso, fvol, fgeo) and Li-sparse parameters
+ * kernel_wt(3, nch, nobs) = (fiso, fgeo, fvol) and Li-sparse parameters
  * param(2, nch, nobs) = (h/b, b/r), 50 azimuth streams -- in place of the
  * albedo; same argument list as the reference (BR(nobs, nch): the exact
  * direct-bounce BRDF of each pixel and channel).  A pixel with MISSING angles

@@ -1519,8 +1519,8 @@ extern "C" int oracle_scalar_lambert(int km, int nch, int nobs, const double* ch
 // scalar solve of VLIDORT_Scalar_Lambert (same layer mixing and
 // VLIDORT_Init settings) over the MODIS RTLS surface of
 // VLIDORT_LANDMODIS_SingleGeom (VLIDORT_SurfaceMod.F90:1376-1596):
-// kernel_wt(3, nch, nobs) = (fiso, fvol, fgeo) on the Lambertian, Ross-thick
-// and Li-sparse kernels, param(2, nch, nobs) = Li-sparse (h/b, b/r), 50
+// kernel_wt(3, nch, nobs) = (fiso, fgeo, fvol) on the Lambertian, Li-sparse
+// and Ross-thick kernels, param(2, nch, nobs) = Li-sparse (h/b, b/r), 50
 // azimuth streams, observation geometry.  BR(nobs, nch) is the exact
 // direct-bounce BRDF (BS_DBOUNCE_BRDFUNC); a negative one gives -500 in the
 // three outputs and skips the solve (:168-174).  The reference's checks of
@@ -1545,8 +1545,11 @@ extern "C" int oracle_scalar_landmodis(int km, int nch, int nobs, const double* 
   };
   auto kernels = [&](int j, int i, int* which, double* fac, double* pars) {
     const size_t w = 3 * ((size_t)i + (size_t)nch * j), q = 2 * ((size_t)i + (size_t)nch * j);
+    // kernel_wt = (fiso, fgeo, fvol) (VLIDORT_BRDF_MODIS.F90:152-156 into
+    // VLIDORT_LANDMODIS(..., fiso, fgeo, fvol, ...)); the supplement sums the
+    // kernels as Lambertian (fiso), Ross-thick (fvol), Li-sparse (fgeo)
     which[0] = 1; which[1] = 3; which[2] = 4;
-    for (int n = 0; n < 3; ++n) fac[n] = kernel_wt[w + n];
+    fac[0] = kernel_wt[w]; fac[1] = kernel_wt[w + 2]; fac[2] = kernel_wt[w + 1];
     for (int n = 0; n < 9; ++n) pars[n] = 0.0;
     pars[6] = param[q]; pars[7] = param[q + 1];
   };

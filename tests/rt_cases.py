@@ -56,14 +56,14 @@ def vector_mie_case(nstreams, nobs, nch=2, seed=0, nlayers=72, chem_channels=(47
 
 
 def modis_brdf(nobs, nch, seed=0, negative=()):
-    """MODIS RTLS kernel amplitudes kernel_wt(3, nch, nobs) = (fiso, fvol, fgeo)
+    """MODIS RTLS kernel amplitudes kernel_wt(3, nch, nobs) = (fiso, fgeo, fvol)
     and Li-sparse parameters param(2, nch, nobs) = (h/b, b/r) = (2, 1) as
     geo_vlidort.F90:543 sets them; `negative` lists (pixel, channel) pairs
     given a strongly negative fgeo (an unphysical combination, BR < 0)."""
     rng = np.random.default_rng(seed)
-    kw = np.stack([rng.uniform(0.02, 0.35, (nch, nobs)), rng.uniform(0.0, 0.15, (nch, nobs)),
-                   rng.uniform(0.0, 0.06, (nch, nobs))])
+    kw = np.stack([rng.uniform(0.02, 0.35, (nch, nobs)), rng.uniform(0.0, 0.06, (nch, nobs)),
+                   rng.uniform(0.0, 0.15, (nch, nobs))])
     for j, i in negative:
-        kw[:, i, j] = (0.01, 0.0, 5.0)
+        kw[:, i, j] = (0.01, 5.0, 0.0)
     par = np.stack([np.full((nch, nobs), 2.0), np.full((nch, nobs), 1.0)])
     return np.asfortranarray(kw), np.asfortranarray(par)

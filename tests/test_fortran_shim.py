@@ -66,5 +66,9 @@ def test_drop_ins_keep_the_reference_argument_lists():
     ref_edge = "km nobs airdens delp ptop pe ze te rc".split()
     assert _subroutine_args("VLIDORT_Scalar_Lambert_GPU", shim) == ref_scalar
     assert _subroutine_args("VLIDORT_Vector_Lambert_GPU", shim) == ref_vector
+    ref_modis = ("km nch nobs channels nstreams plane_parallel nmom npol rot depol tau ssa g pmom pe he te kernel_wt "
+                 "param solar_zenith relat_azymuth sensor_zenith missing verbose radiance_vl_surf "
+                 "reflectance_vl_surf br rc").split()
+    assert _subroutine_args("VLIDORT_Scalar_LandMODIS_GPU", shim) == ref_modis
     assert _subroutine_args("VLIDORT_ROT_CALC_GPU", shim) == ref_rot
     assert _subroutine_args("getEdgeVars_GPU", shim) == ref_edge
