@@ -172,6 +172,47 @@ RT_HD bool team_eigen(const Team& tm, int n, int ld, double* H, double* Zm, doub
       its = 0;
       continue;
     }
+    if (lo == hi - 1) {
+      // an isolated 2 x 2 block: both eigenvalues at once, as ASYMTX's
+      // "two eigenvalues found" step (vlidort_aux.f90 ASYMTX): with
+      // p = (y - x) / 2, q = p^2 + w, the eigenvalues x + z and x - w / z for
+      // z = p + sign(p) sqrt(|q|) -- real even when rounding leaves a nearly
+      // degenerate pair complex (q < 0), where a real QR step would never
+      // split the block -- and the rotation by the eigenvector (z, c) / r.
+      const double xd = A(hi, hi), yd = A(hi - 1, hi - 1), cd = A(hi, hi - 1), wd = cd * A(hi - 1, hi);
+      const double pd = 0.5 * (yd - xd), qd = pd * pd + wd;
+      const double zd = pd + copysign(sqrt(fabs(qd)), pd);
+      const double l1 = xd + zd, l2 = (zd != 0.0) ? xd - wd / zd : l1;
+      const double rd = sqrt(cd * cd + zd * zd);
+      const double cp = rd > 0.0 ? cd / rd : 0.0, cq = rd > 0.0 ? zd / rd : 1.0;
+      tm.sync();
+      for (int j = hi - 1 + tm.lane; j < n; j += kTeam) {
+        const double a1 = A(hi - 1, j), a2 = A(hi, j);
+        A(hi - 1, j) = cq * a1 + cp * a2;
+        A(hi, j) = cq * a2 - cp * a1;
+      }
+      tm.sync();
+      for (int i = tm.lane; i < n; i += kTeam) {
+        if (i <= hi) {
+          const double a1 = A(i, hi - 1), a2 = A(i, hi);
+          A(i, hi - 1) = cq * a1 + cp * a2;
+          A(i, hi) = cq * a2 - cp * a1;
+        }
+        const double z1 = Zz(i, hi - 1), z2 = Zz(i, hi);
+        Zz(i, hi - 1) = cq * z1 + cp * z2;
+        Zz(i, hi) = cq * z2 - cp * z1;
+      }
+      tm.sync();
+      if (tm.lane == 0) {
+        A(hi, hi - 1) = 0.0;
+        A(hi - 1, hi - 1) = l1;
+        A(hi, hi) = l2;
+      }
+      tm.sync();
+      hi -= 2;
+      its = 0;
+      continue;
+    }
     if (++total > 60 * n) return false;
     ++its;
     // Wilkinson shift from the trailing 2x2 block (real part if complex);

@@ -48,6 +48,10 @@ WORKLOAD = ("batching config: 262,144 columns x 4 wavelengths (470, 550, 670, 86
             "72-level grid, top layers merged), streams {4,6,8,12,16}, moments 2x streams; Mie AOP (FP32) + scalar "
             "Lambertian RT per stream group")
 SEED = 20261204
+# DRAM bytes (read + write) per solve of the 16-stream FP32 series kernel,
+# from one ncu capture (profiles/k_team_series_16_float_cols8192.md); None
+# until captured
+TEAM16_DRAM_BYTES_PER_SOLVE = None
 
 
 def parse(argv=None):
@@ -64,7 +68,7 @@ def parse(argv=None):
     ap.add_argument("--stress-cols", type=int, default=96, help="columns per stream count of the SSA stress set")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-config0", action="store_true")
-    ap.add_argument("--config3-cols", type=int, default=8192, help="columns of the polarized sample (0 = skip)")
+    ap.add_argument("--config3-cols", type=int, default=2048, help="columns of the polarized sample (0 = skip)")
     ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=2000.0, help="Poisson arrival rate [requests/s]")
     ap.add_argument("--serve-max-cols", type=int, default=16384, help="largest swath of the serving run")
@@ -443,6 +447,11 @@ def config0(torch, L, fp64_peak, ftab, cpu=True):
     stream = torch.cuda.current_stream().cuda_stream
     ch32 = np.array(ch, np.float32)
     P = lambda t: t.data_ptr()
+    # the library's own kernel choice for this batch size (1,024 solves: the
+    # team kernel, one warp per solve); the shipped table's 8-stream FP64
+    # entry was tuned on 8,192-column buckets
+    L.aerort_set_kernel(N, _lib.PREC_FP64, _lib.KERNEL_AUTO)
+    L.aerort_set_schedule(N, _lib.PREC_FP64, 32, 0)
 
     def run():
         rc = L.aerort_get_aop_vector_dev(chem.handle, km, ncol, 1, 20, _lib.ptr(ch32, _lib.P_f), _lib.ptr(qt, _lib.P_i),
@@ -498,7 +507,7 @@ def config3(torch, L, ncols, ocols=32, cpu=True):
     wavelengths (SERVE_CHANNELS), Lambertian albedo U(0.02, 0.40).  A bounded
     sample of the 65,536-column workload: `ncols` columns at every wavelength
     in one AOP + vector RT launch pair (FP32 optics straight into the FP64
-    polarized solve), 1 warm-up + 2 timed launches with CUDA events.  I, Q, U
+    polarized solve), 1 warm-up + 1 timed launch with CUDA events.  I, Q, U
     of the first `ocols` columns against the polarized FP64 oracle (I
     relative; Q and U relative to I, as they pass through zero), and the
     oracle's own rate on the host cores."""
@@ -541,7 +550,7 @@ def config3(torch, L, ncols, ocols=32, cpu=True):
     run()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 2
+    reps = 1
     e0.record()
     for _ in range(reps):
         run()
@@ -869,6 +878,19 @@ def main():
         rt_ms_d += timed_step(_lib.PREC_FP64) / args.plain_steps
     plain_value = total_solves / (rt_ms_d * 1e-3)
 
+    # ---------------------------------------------------------------- the dominant kernel
+    # every group's mixed RT launches alone on the main stream (serial, CUDA
+    # events), for the roofline of the costliest one
+    group_ms = []
+    for d in groups:
+        g0, g1 = ev(), ev()
+        g0.record()
+        run_group(d, _lib.PREC_MIXED, stream)
+        g1.record()
+        torch.cuda.synchronize()
+        group_ms.append(g0.elapsed_time(g1))
+    dom = int(np.argmax(group_ms))
+
     # ---------------------------------------------------------------- results, flops
     rad_m = np.zeros((my_cols, nch))
     rad_d = np.zeros((my_cols, nch))
@@ -899,14 +921,28 @@ def main():
     fp64_peak, fp32_peak, dgemm = pipe_peaks(torch, L, stream)
     ach_m = flops / (rt_ms_m * 1e-3) / 1e12
     ach_d = flops / (rt_ms_d * 1e-3) / 1e12
-    roofline = {"bound": "fp32", "achieved": ach_m, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach_m / fp32_peak,
-                "traffic": None, "kernel": "k_team_setup + k_team_series<NS, float> / k_scalar_lambert<NS, float> "
-                                           "(mixed; all stream counts)",
-                "kernel_ms_per_step": rt_ms_m,
-                "kernel_time": "span of one eager step's launches (all stream groups, AOP kernels included at <1%)",
+    dg = groups[dom]
+    dom_nf = dg["nfm"].cpu().numpy().reshape(dg["n"], nch, order="F")
+    dom_flops = float(ftab[dg["N"]][dg["host"]["nlayers"][:, None], np.clip(dom_nf, 0, 63)].sum())
+    dom_solves = int((dom_nf >= 0).sum())
+    ach_dom = dom_flops / (group_ms[dom] * 1e-3) / 1e12
+    traffic = None
+    if dg["N"] == 16 and TEAM16_DRAM_BYTES_PER_SOLVE:
+        traffic = TEAM16_DRAM_BYTES_PER_SOLVE * dom_solves
+    roofline = {"bound": "fp32", "achieved": ach_dom, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": ach_dom / fp32_peak, "traffic": traffic,
+                "kernel": "k_team_setup + k_team_series<%d, float> (+ the FP64 refinement launch) of the %d-stream "
+                          "group with %d-%d layers" % (dg["N"], dg["N"], int(dg["host"]["nlayers"].min()),
+                                                        int(dg["host"]["nlayers"].max())),
+                "kernel_ms": group_ms[dom], "solves": dom_solves,
+                "kernel_time": "the group's RT launches alone on one stream, CUDA events",
+                "traffic_source": "DRAM bytes per solve of k_team_series<16, float> from one ncu capture "
+                                  "(profiles/k_team_series_16_float_cols8192.md) x the group's solves",
                 "peak_source": "measured live: FFMA issue-rate probe (8 FMA chains/thread), of measured",
                 "note": "achieved = reference-algorithm flops (banded-LU BVP, nonsymmetric eigen-solve) of the solves "
-                        "/ kernel time; the kernel executes a different, mostly FP32 operation mix"}
+                        "/ kernel time; the kernel executes a different, mostly FP32 operation mix",
+                "whole_step": {"achieved": ach_m, "frac": ach_m / fp32_peak, "kernel_ms_per_step": rt_ms_m,
+                               "group_ms": {"N%d|L%d" % (d["N"], d["km"]): ms for d, ms in zip(groups, group_ms)}}}
     roofline_plain = {"bound": "fp64", "achieved": ach_d, "peak": fp64_peak, "unit": "TFLOP/s",
                       "frac": ach_d / fp64_peak, "kernel": "k_team_series<NS, double> / k_scalar_lambert<NS, double>",
                       "kernel_ms_per_step": rt_ms_d,
