@@ -78,6 +78,8 @@ _SIGNATURES = {
     "aerort_set_kernel": (c_int, [c_int, c_int, c_int]),
     "aerort_refined_count": (c_int, [c_void_p, P_i]),
     "aerort_get_kernel": (c_int, [c_int, c_int]),
+    "aerort_set_moment_contraction": (c_int, [c_int]),
+    "aerort_get_moment_contraction": (c_int, []),
     "aerort_probe_dfma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_probe_ffma": (c_int, [c_int, c_int, c_int, c_void_p, c_void_p]),
     "aerort_last_error": (ctypes.c_char_p, []),
@@ -96,6 +98,8 @@ PREC_MIXED = 1
 KERNEL_THREAD = 0
 KERNEL_TEAM = 1
 KERNEL_AUTO = 2
+CONTRACT_FMA = 0
+CONTRACT_TF32X3 = 1
 
 
 def library_path():

@@ -333,6 +333,174 @@ __global__ void __launch_bounds__(256) k_aop(const DevMieTable* __restrict__ tab
   }
 }
 
+// The same computation with the Mie-table rows staged in shared memory.
+// Block (x, n) handles elements e0..e0 + 256*EPT of channel n (e = k + km i,
+// layer fastest, so qm, rh reads and output stores stay coalesced).  The
+// block first copies, for every tracer, the bext, bsca and g rows of its
+// table and size bin at this channel (all RH nodes, row stride R), then for
+// each chunk of MC moments and each element group the moment rows; the
+// per-element lerps read them from shared memory instead of gathering them
+// from L1/L2.  Operations and their order are those of k_aop, so the bits
+// are too.  Shared memory: nq (3 + P MC) R + 256 EPT floats, P = 2 for
+// nPol = 6 (paired elements), else 1.
+template <int MC, int EPT>
+__global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restrict__ tabs, int km, int nobs, int nch,
+                                                    int nq, const AopMeta meta, const float* __restrict__ qm,
+                                                    const float* __restrict__ rh, int nMom, int nPol, int R,
+                                                    float* __restrict__ tau, float* __restrict__ ssa,
+                                                    float* __restrict__ g, float* __restrict__ pmom) {
+  extern __shared__ float aop_smem[];
+  const int n = blockIdx.y;
+  const int ich = meta.idxch[n];
+  const long nel = (long)km * nobs;
+  const long e0 = (long)blockIdx.x * (256L * EPT);
+  if (e0 >= nel) return;
+  const long e1 = nel < e0 + 256L * EPT ? nel : e0 + 256L * EPT;
+  const int P = nPol == 6 ? 2 : 1;
+  float* s_sc = aop_smem;                   // [q][3][R]: bext, bsca, g rows
+  float* s_st = s_sc + (long)nq * 3 * R;    // [256 EPT]: ssa_out * tau_out of each element
+  float* s_mo = s_st + 256L * EPT;          // [q][P][MC][R]: moment rows of the current chunk
+  for (int x = threadIdx.x; x < nq * 3 * R; x += blockDim.x) {
+    const int r = x % R, qty = (x / R) % 3, q = x / (3 * R);
+    const int tb = meta.q_table[q];
+    float v = 0.0f;
+    if (tb >= 0) {
+      const DevMieTable& T = tabs[tb];
+      if (r < T.nrh) {
+        const long row = r + (long)T.nrh * (ich + (long)T.nch * meta.q_bin[q]);
+        v = (qty == 0 ? T.bext : (qty == 1 ? T.bsca : T.g))[row];
+      }
+    }
+    s_sc[x] = v;
+  }
+  __syncthreads();
+  const long total = (long)km * nch * nobs;
+  auto snap = [&](int k, int i) {
+    const float rhUse = fminf(rh[k + (long)km * i], 0.99f);
+    int isnap = (int)__fmul_rn(__fadd_rn(rhUse, 0.001f), 1000.0f);
+    return isnap < 1 ? 1 : isnap;
+  };
+  // a tracer's RH rows (staged indices), weights, tau and ssa at one element
+  struct Row { int r0, r1; float arh, w0, tau, ssa; };
+  auto row_of = [&](int iq, int isnap, float qmv, Row& w) -> bool {
+    const int tb = meta.q_table[iq];
+    if (tb < 0) return false;
+    const DevMieTable& T = tabs[tb];
+    w.arh = T.rha[isnap - 1];
+    const int irh = T.rhi[isnap - 1];
+    const int irhp1 = irh + 1 > T.nrh ? T.nrh : irh + 1;
+    w.r0 = irh - 1;
+    w.r1 = irhp1 - 1;
+    w.w0 = __fsub_rn(1.0f, w.arh);
+    const float* sc = s_sc + (long)iq * 3 * R;
+    const float bext = lerp_ref(sc[w.r0], sc[w.r1], w.w0, w.arh);
+    const float bsca = lerp_ref(sc[R + w.r0], sc[R + w.r1], w.w0, w.arh);
+    w.tau = __fmul_rn(bext, qmv);
+    w.ssa = __fdiv_rn(bsca, bext);
+    return true;
+  };
+  for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int k = (int)(e % km), i = (int)(e / km);
+    const int isnap = snap(k, i);
+    const float* qcol = qm + k + (long)km * (long)nq * i;
+    float ts = 0.0f, ss = 0.0f, gs = 0.0f;
+    for (int iq = 0; iq < nq; ++iq) {
+      Row w;
+      if (!row_of(iq, isnap, qcol[(long)km * iq], w)) continue;
+      const float* sc = s_sc + (long)iq * 3 * R;
+      const float gg = lerp_ref(sc[2 * R + w.r0], sc[2 * R + w.r1], w.w0, w.arh);
+      ts = __fadd_rn(ts, w.tau);
+      ss = __fadd_rn(ss, __fmul_rn(w.ssa, w.tau));
+      gs = __fadd_rn(gs, __fmul_rn(__fmul_rn(gg, w.ssa), w.tau));
+    }
+    const float ssa_out = ts > 0.0f ? __fdiv_rn(ss, ts) : ss;
+    const float st = __fmul_rn(ssa_out, ts);
+    const float g_out = st > 0.0f ? __fdiv_rn(gs, st) : gs;
+    const long o = k + (long)km * (n + (long)nch * i);
+    tau[o] = ts;
+    ssa[o] = ssa_out;
+    g[o] = g_out;
+    s_st[e - e0] = st;
+  }
+  const int ngroups = nPol == 6 ? 4 : nPol;
+  for (int grp = 0; grp < ngroups; ++grp) {
+    const int ea = grp;
+    const int eb = nPol == 6 ? (grp == 0 ? 4 : (grp == 2 ? 5 : -1)) : -1;
+    for (int m0 = 0; m0 < nMom; m0 += MC) {
+      const int mc = nMom - m0 < MC ? nMom - m0 : MC;
+      __syncthreads();  // the previous chunk's readers are done
+      for (int x = threadIdx.x; x < nq * P * MC * R; x += blockDim.x) {
+        const int r = x % R, j = (x / R) % MC, p = (x / (R * MC)) % P, q = x / (R * MC * P);
+        const int tb = meta.q_table[q];
+        float v = 0.0f;
+        const int ip = p == 0 ? ea : eb;
+        if (tb >= 0 && j < mc && ip >= 0) {
+          const DevMieTable& T = tabs[tb];
+          const bool sph = (nPol == 6 && T.npol == 4);
+          if (r < T.nrh && !(p == 1 && sph)) {
+            const long s = (long)T.nrh * T.nch * T.nbin;
+            const long row = r + (long)T.nrh * (ich + (long)T.nch * meta.q_bin[q]);
+            v = T.pmom[(long)(m0 + j + T.nmom * ip) * s + row];
+          }
+        }
+        s_mo[x] = v;
+      }
+      __syncthreads();
+      for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        const int k = (int)(e % km), i = (int)(e / km);
+        const int isnap = snap(k, i);
+        const float* qcol = qm + k + (long)km * (long)nq * i;
+        float a[MC], b[MC];
+#pragma unroll
+        for (int j = 0; j < MC; ++j) { a[j] = 0.0f; b[j] = 0.0f; }
+        for (int iq = 0; iq < nq; ++iq) {
+          Row w;
+          if (!row_of(iq, isnap, qcol[(long)km * iq], w)) continue;
+          const bool sph = (nPol == 6 && tabs[meta.q_table[iq]].npol == 4);
+          const float* pa = s_mo + (long)iq * P * MC * R;
+#pragma unroll
+          for (int j = 0; j < MC; ++j) {
+            if (j < mc) {
+              const float pv = lerp_ref(pa[j * R + w.r0], pa[j * R + w.r1], w.w0, w.arh);
+              a[j] = __fadd_rn(a[j], __fmul_rn(__fmul_rn(pv, w.ssa), w.tau));
+            }
+          }
+          if (eb >= 0) {
+            if (sph) {
+#pragma unroll
+              for (int j = 0; j < MC; ++j) b[j] = a[j];
+            } else {
+              const float* pb = pa + MC * R;
+#pragma unroll
+              for (int j = 0; j < MC; ++j) {
+                if (j < mc) {
+                  const float pv = lerp_ref(pb[j * R + w.r0], pb[j * R + w.r1], w.w0, w.arh);
+                  b[j] = __fadd_rn(b[j], __fmul_rn(__fmul_rn(pv, w.ssa), w.tau));
+                }
+              }
+            }
+          }
+        }
+        const float st = s_st[e - e0];
+        const long o = k + (long)km * (n + (long)nch * i);
+#pragma unroll
+        for (int j = 0; j < MC; ++j) {
+          if (j < mc) {
+            float v = a[j];
+            if (st > 0.0f) v = __fdiv_rn(v, st);
+            pmom[o + total * (m0 + j + (long)nMom * ea)] = v;
+            if (eb >= 0) {
+              float u = b[j];
+              if (st > 0.0f) u = __fdiv_rn(u, st);
+              pmom[o + total * (m0 + j + (long)nMom * eb)] = u;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
 // Chem_MieTableMod.F90:612-627 in single precision.
 void rh_map(int nrh, const float* rh, int* rhi, float* rha) {
   for (int j = 1; j <= 991; ++j) {
@@ -450,10 +618,29 @@ int aop_launch(aerort_mie* mie, int km, int nobs, int nch, int nq, const std::ve
   for (int q = 0; q < nq; ++q) { meta.q_table[q] = q_table[q]; meta.q_bin[q] = q_bin[q]; }
   long total = (long)km * nch * nobs;
   if (total == 0) return 0;
-  const int bs = 256;
-  const long nb = (total + bs - 1) / bs;
-  k_aop<16><<<(unsigned)nb, bs, 0, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, tau, ssa, g,
-                                        pmom);
+  // table rows staged in shared memory when they fit (k_aop_staged), else gathered (k_aop)
+  constexpr int kMC = 8, kEPT = 16;
+  int R = 1;
+  for (int q = 0; q < nq; ++q)
+    if (q_table[q] >= 0 && mie->host_desc[q_table[q]].nrh > R) R = mie->host_desc[q_table[q]].nrh;
+  const int P = nPol == 6 ? 2 : 1;
+  const size_t smem = sizeof(float) * ((size_t)nq * (3 + P * kMC) * R + 256 * kEPT);
+  if (nq > 0 && smem <= 96 * 1024) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      CUDA_TRY(cudaFuncSetAttribute(k_aop_staged<kMC, kEPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+      attr_set = true;
+    }
+    const long nel = (long)km * nobs;
+    const dim3 grid((unsigned)((nel + 256L * kEPT - 1) / (256L * kEPT)), (unsigned)nch);
+    k_aop_staged<kMC, kEPT><<<grid, 256, smem, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, R,
+                                                    tau, ssa, g, pmom);
+  } else {
+    const int bs = 256;
+    const long nb = (total + bs - 1) / bs;
+    k_aop<16><<<(unsigned)nb, bs, 0, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, tau, ssa, g,
+                                          pmom);
+  }
   CUDA_TRY(cudaGetLastError());
   count_launches(1);
   return 0;
@@ -551,8 +738,12 @@ __global__ void k_init_sched(int* counter, int* first, int nobs, int* zero) {
 
 namespace {
 
+// AERORT_CONTRACT_* of the FP32 team solve (aerort_set_moment_contraction)
+std::atomic<int> g_moment_contraction{AERORT_CONTRACT_FMA};
+
 RtOptions lambert_options(int plane_parallel) {
   RtOptions o;
+  o.moment_contraction = g_moment_contraction.load();
   o.do_focorr = 1;            // VLIDORT_Mod.F90: DO_FOCORR / DO_FOCORR_OUTGOING
   o.do_deltam = 1;            // DO_DELTAM_SCALING
   o.do_plane_parallel = plane_parallel ? 1 : 0;
@@ -743,6 +934,15 @@ extern "C" int aerort_set_kernel(int nstreams, int precision, int kernel) {
   c.sched[precision][si].kernel = kernel;
   return AERORT_OK;
 }
+
+extern "C" int aerort_set_moment_contraction(int mode) {
+  if (mode != AERORT_CONTRACT_FMA && mode != AERORT_CONTRACT_TF32X3)
+    return set_error(AERORT_RC_ARG, "set_moment_contraction: mode must be AERORT_CONTRACT_FMA or _TF32X3");
+  g_moment_contraction.store(mode);
+  return AERORT_OK;
+}
+
+extern "C" int aerort_get_moment_contraction(void) { return g_moment_contraction.load(); }
 
 extern "C" int aerort_get_kernel(int nstreams, int precision) {
   const int si = stream_index(nstreams);

@@ -73,6 +73,7 @@ struct RtOptions {
   double earth_radius;     // km
   double flux_factor;      // solar flux
   int max_fourier;         // -1: up to NMOMENTS (reference); otherwise cap (testing)
+  int moment_contraction = 0;  // FP32 team solve: 0 CUDA-core FMA, 1 tensor cores (3xTF32 mma.sync)
 };
 
 // Strided per-thread view of a global scratch buffer (element e of this

@@ -1094,6 +1094,7 @@ RT_HD void make_ctx(const SetupRecord& r, const double* qx, const double* qw, So
 struct FourierSum {
   double stokes = 0.0;
   double sumabs = 0.0;  // sum of |contributions|: |stokes| / sumabs measures the cancellation
+  double edge = 1e300;  // smallest | |term / sum| / accuracy - 1 | over the convergence tests
   int testconv = 0;
   RT_HD bool add(const RtOptions& opt, const SetupRecord& r, int m, double sf) {
     if (m == 0) {
@@ -1108,7 +1109,13 @@ struct FourierSum {
     double tazm = cos(r.raa * (double)m * kDTR) * sf;
     sumabs += fabs(tazm);
     double tnew = stokes + tazm;
-    bool conv = (tazm != 0.0) ? (fabs(tazm / tnew) < opt.accuracy) : true;
+    bool conv = true;
+    if (tazm != 0.0) {
+      const double q = fabs(tazm / tnew);
+      conv = q < opt.accuracy;
+      const double d = fabs(q / opt.accuracy - 1.0);
+      if (d < edge) edge = d;
+    }
     stokes = tnew;
     if (conv) {
       ++testconv;
@@ -1120,12 +1127,23 @@ struct FourierSum {
   }
 };
 
+// Relative distance of a convergence test's |term / sum| from the accuracy
+// threshold below which a mixed-method solve is re-solved in FP64: the FP32
+// terms were measured within 2e-4 (relative) of the FP64 terms on the
+// solves whose test decided the other way.
+constexpr double kConvEdge = 1.0e-3;
+
 // Which solves a launch runs and which it hands on.  in_list (device, length
 // *in_count): run only these solve indices (the FP64 refinement pass);
-// out_list: append every solve whose Fourier sum cancels by more than `ratio`
-// (sum |terms| > ratio |radiance|), so that the FP64 pass re-solves it.  The
-// mixed method's terms carry ~1e-6 relative FP32 error each; a radiance that
-// is a near-cancellation of much larger terms would inherit it amplified.
+// out_list: append every solve that the FP64 pass must re-solve: its Fourier
+// sum cancels by more than `ratio` (sum |terms| > ratio |radiance|), or one
+// of its convergence tests came within kConvEdge (relative) of the accuracy
+// threshold.  The mixed method's terms carry ~1e-6 relative FP32 error each:
+// a radiance that is a near-cancellation of much larger terms would inherit
+// it amplified, and a test that close to the threshold can decide the other
+// way than in FP64 -- the series then ends at another term, and the terms
+// that one solve keeps and the other drops are of order accuracy x radiance
+// each (up to 8e-4 relative in a slowly converging series).
 struct Worklist {
   const int* in_list = nullptr;
   const int* in_count = nullptr;
@@ -1135,7 +1153,7 @@ struct Worklist {
   RT_HD int count(int nsolve) const { return in_list ? *in_count : nsolve; }
   RT_HD int solve(int s) const { return in_list ? in_list[s] : s; }
   RT_HD void flag(const FourierSum& sum, int st, int sidx) const {
-    if (!out_list || st != RT_OK || !(sum.sumabs > ratio * fabs(sum.stokes))) return;
+    if (!out_list || st != RT_OK || !(sum.sumabs > ratio * fabs(sum.stokes) || sum.edge < kConvEdge)) return;
 #ifdef __CUDA_ARCH__
     const int pos = atomicAdd(out_count, 1);
 #else

@@ -357,10 +357,97 @@ RT_HD void team_legendre(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T
   tm.sync();
 }
 
+#ifdef __CUDA_ARCH__
+// The moment contraction of team_layer_eigen on the tensor cores, for the FP32
+// solve: mma.sync m16n8k8 with TF32 operands and FP32 accumulation, and the
+// 3xTF32 split x = hi + lo (hi = x rounded to TF32, lo = the remainder rounded
+// to TF32), x y ~ lo_x hi_y + hi_x lo_y + hi_x hi_y, which drops only lo_x lo_y
+// (below 2^-22 |x y|).  Per k-step of 8 moments l: A (16 x 8) = og_l P_l(mu_i)
+// for the rows i < N (zero above) and l of one parity (even, then odd l - m
+// into a second accumulator), B (8 x 8 per tile of columns j) = P_l(mu_j).
+// Fragments as the PTX ISA lays out m16n8k8 .tf32: lane = 4 g + t, A rows g
+// and g + 8 at columns t and t + 4, B rows t and t + 4 at column g, D rows g
+// and g + 8 at columns 2t and 2t + 1.  Writes the lower triangle of Sp
+// (mirrored) and of Bs as the CUDA-core loop does.
+__device__ __forceinline__ unsigned tf32_rna(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void tf32_split(float x, unsigned& hi, unsigned& lo) {
+  hi = tf32_rna(x);
+  lo = tf32_rna(x - __uint_as_float(hi));
+}
+
+__device__ __forceinline__ void mma_tf32_m16n8k8(float (&d)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <int NS>
+__device__ void team_contract_tf32x3(const Team& tm, TeamMem<NS, float>& M, int m, int NM, float* Sp, float* Bs) {
+  constexpr int LD = TeamMem<NS, float>::LD;
+  constexpr int NT = (NS + 7) / 8;
+  static_assert(NS <= 16, "one 16-row tile");
+  const int g = tm.lane >> 2, t4 = tm.lane & 3;
+  float ce[NT][4], co[NT][4];
+#pragma unroll
+  for (int jt = 0; jt < NT; ++jt)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) { ce[jt][r] = 0.0f; co[jt][r] = 0.0f; }
+  auto pq = [&](int i, int l) -> float { return (i < NS && l <= NM) ? M.piq[i][l] : 0.0f; };
+  for (int l0 = m & ~7; l0 <= NM; l0 += 8) {
+    const int la = l0 + t4, lb = la + 4;
+    const float oa = (la >= m && la <= NM) ? M.og[la] : 0.0f;
+    const float ob = (lb >= m && lb <= NM) ? M.og[lb] : 0.0f;
+    const bool eva = ((la - m) & 1) == 0, evb = ((lb - m) & 1) == 0;
+    const float x[4] = {oa * pq(g, la), oa * pq(g + 8, la), ob * pq(g, lb), ob * pq(g + 8, lb)};
+    const bool ev[4] = {eva, eva, evb, evb};
+    unsigned aeh[4], ael[4], aoh[4], aol[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      tf32_split(ev[r] ? x[r] : 0.0f, aeh[r], ael[r]);
+      tf32_split(ev[r] ? 0.0f : x[r], aoh[r], aol[r]);
+    }
+#pragma unroll
+    for (int jt = 0; jt < NT; ++jt) {
+      unsigned bh0, bl0, bh1, bl1;
+      tf32_split(pq(8 * jt + g, la), bh0, bl0);
+      tf32_split(pq(8 * jt + g, lb), bh1, bl1);
+      mma_tf32_m16n8k8(ce[jt], ael, bh0, bh1);
+      mma_tf32_m16n8k8(ce[jt], aeh, bl0, bl1);
+      mma_tf32_m16n8k8(ce[jt], aeh, bh0, bh1);
+      mma_tf32_m16n8k8(co[jt], aol, bh0, bh1);
+      mma_tf32_m16n8k8(co[jt], aoh, bl0, bl1);
+      mma_tf32_m16n8k8(co[jt], aoh, bh0, bh1);
+    }
+  }
+#pragma unroll
+  for (int jt = 0; jt < NT; ++jt)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int i = g + (r >= 2 ? 8 : 0), j = 8 * jt + 2 * t4 + (r & 1);
+      if (i < NS && j <= i) {
+        Sp[i + LD * j] = ce[jt][r];
+        Sp[j + LD * i] = ce[jt][r];
+        float b = -M.csqw[i] * M.csqw[j] * co[jt][r];
+        if (i == j) b += 1.0f;
+        Bs[i + LD * j] = b;
+      }
+    }
+}
+#endif
+
 // Eigen-solution of layer n for term m into P/Q/t of slot `cur`, with the
 // Green's-function norms and user-angle homogeneous solutions (layer_eigen).
+// tc: the FP32 solve forms the moment contraction on the tensor cores
+// (team_contract_tf32x3; device only).
 template <int NS, typename T>
-RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T>& c, int m, int cur) {
+RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T>& c, int m, int cur,
+                           bool tc = false) {
   constexpr int LD = TeamMem<NS, T>::LD;
   const int N = NS, NM = c.NM;
   T* Sp = M.work;
@@ -374,7 +461,16 @@ RT_HD int team_layer_eigen(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS,
   // diagonal only).  Element e of the folded triangle: row pairs (r, N-1-r)
   // hold N+1 elements together (N even).
   // Each lane keeps its U elements' sums in registers (U independent chains).
-  {
+#ifdef __CUDA_ARCH__
+  const bool use_tc = sizeof(T) == sizeof(float) && tc;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (use_tc) team_contract_tf32x3<NS>(tm, M, m, NM, Sp, Bs);
+  }
+#else
+  const bool use_tc = false;
+  (void)tc;
+#endif
+  if (!use_tc) {
     constexpr int NE = (NS / 2) * (NS + 1), U = (NE + kTeam - 1) / kTeam;
     int ii[U], jj[U];
     T se[U], so[U];
@@ -611,7 +707,7 @@ RT_HD int team_layer_solution(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<
                               int m, int n, bool laysc, int cur) {
   constexpr int LD = TeamMem<NS, T>::LD;
   const int N = NS, NM = c.NM;
-  int st = team_layer_eigen<NS, T>(tm, M, c, m, cur);
+  int st = team_layer_eigen<NS, T>(tm, M, c, m, cur, opt.moment_contraction != 0);
   if (st != RT_OK) return st;
   const T dtau = M.lsc[0], tuser = M.lsc[2], smu = c.sec_u;
   const int a = tm.lane;

@@ -48,10 +48,12 @@ WORKLOAD = ("batching config: 262,144 columns x 4 wavelengths (470, 550, 670, 86
             "72-level grid, top layers merged), streams {4,6,8,12,16}, moments 2x streams; Mie AOP (FP32) + scalar "
             "Lambertian RT per stream group")
 SEED = 20261204
-# DRAM bytes (read + write) per solve of the 16-stream FP32 series kernel,
-# from one ncu capture (profiles/k_team_series_16_float_cols8192.md); None
-# until captured
-TEAM16_DRAM_BYTES_PER_SOLVE = None
+# DRAM bytes (read + write) per solve-layer of the 16-stream FP32 series
+# kernel: 17,592,320 B in one ncu capture of a launch of 2,300 solves with
+# 104,216 solve-layers (the 8,192-column batch's 37-54-layer group;
+# profiles/k_team_series_16_float_cols8192.md).  Its inputs are per layer,
+# so the traffic of a launch scales with its solve-layers.
+TEAM16_DRAM_BYTES_PER_SOLVE_LAYER = 17592320 / 104216
 
 
 def parse(argv=None):
@@ -74,6 +76,8 @@ def parse(argv=None):
     ap.add_argument("--serve-max-cols", type=int, default=16384, help="largest swath of the serving run")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--tune", action="store_true", help="re-run the schedule autotuner before timing")
+    ap.add_argument("--contraction", default="fma", choices=["fma", "tf32x3"],
+                    help="moment contraction of the FP32 team solve for the whole run (aerort_set_moment_contraction)")
     ap.add_argument("--eager", action="store_true", help="launch the timed steps eagerly instead of replaying "
                     "the captured CUDA graph")
     ap.add_argument("--buckets", default="36,54,72", help="upper layer counts of the launch groups' layer buckets "
@@ -714,6 +718,8 @@ def main():
         dist.init_process_group("nccl")
     from aeroapps_gb300 import _lib, autotune, mie, synth
     L = _lib.lib()
+    run_contraction = _lib.CONTRACT_TF32X3 if args.contraction == "tf32x3" else _lib.CONTRACT_FMA
+    assert L.aerort_set_moment_contraction(run_contraction) == 0
     stream = torch.cuda.current_stream().cuda_stream
     dev_name = torch.cuda.get_device_name(local)
     tuned_src = autotune.apply_defaults(dev_name)
@@ -891,6 +897,41 @@ def main():
         group_ms.append(g0.elapsed_time(g1))
     dom = int(np.argmax(group_ms))
 
+    # ---------------------------------------------------------------- tensor-core contraction A/B
+    # the dominant group's mixed RT launches with the layer-matrix moment
+    # contraction on the tensor cores (3xTF32 mma.sync) and on the CUDA cores,
+    # the run's own choice last (so the group's results below are its own)
+    contraction_ab = None
+    dgab = groups[dom]
+    if dgab["N"] >= 8 and args.plain_steps > 0:
+        ab = {}
+        modes = [(_lib.CONTRACT_TF32X3, "tf32x3"), (_lib.CONTRACT_FMA, "fma")]
+        if run_contraction == _lib.CONTRACT_TF32X3:
+            modes = modes[::-1]
+        for mode, name in modes:
+            assert L.aerort_set_moment_contraction(mode) == 0
+            run_group(dgab, _lib.PREC_MIXED, stream)
+            torch.cuda.synchronize()
+            best = None
+            for _ in range(2):
+                g0, g1 = ev(), ev()
+                g0.record()
+                run_group(dgab, _lib.PREC_MIXED, stream)
+                g1.record()
+                torch.cuda.synchronize()
+                best = min(best or 1e30, g0.elapsed_time(g1))
+            cnt = ctypes.c_int(0)
+            L.aerort_refined_count(ctypes.c_void_p(stream), ctypes.byref(cnt))
+            rm, rd = dgab["radm"].cpu().numpy(), dgab["radd"].cpu().numpy()
+            ok = (rd != MISSING) & (dgab["stm"].cpu().numpy() == 0)
+            e = np.abs(rm[ok] / rd[ok] - 1.0)
+            ab[name] = {"ms": best, "max_rel_err_vs_fp64": float(e.max()), "median_rel_err_vs_fp64": float(np.median(e)),
+                        "refined": int(cnt.value)}
+        L.aerort_set_moment_contraction(run_contraction)
+        contraction_ab = {"group": "N%d|L%d" % (dgab["N"], dgab["km"]), "solves": int(dgab["n"]) * nch,
+                          "speedup_tf32x3": ab["fma"]["ms"] / ab["tf32x3"]["ms"], **ab,
+                          "time": "the group's mixed RT launches alone on one stream, best of 2, CUDA events"}
+
     # ---------------------------------------------------------------- results, flops
     rad_m = np.zeros((my_cols, nch))
     rad_d = np.zeros((my_cols, nch))
@@ -926,9 +967,11 @@ def main():
     dom_flops = float(ftab[dg["N"]][dg["host"]["nlayers"][:, None], np.clip(dom_nf, 0, 63)].sum())
     dom_solves = int((dom_nf >= 0).sum())
     ach_dom = dom_flops / (group_ms[dom] * 1e-3) / 1e12
+    # algorithmic bytes per solve-layer of the series: FP32 tau, ssa and 2N = 32
+    # moments (136 B), FP64 ROT and level height (16 B)
     traffic = None
-    if dg["N"] == 16 and TEAM16_DRAM_BYTES_PER_SOLVE:
-        traffic = TEAM16_DRAM_BYTES_PER_SOLVE * dom_solves
+    if dg["N"] == 16:
+        traffic = TEAM16_DRAM_BYTES_PER_SOLVE_LAYER * float((dg["host"]["nlayers"][:, None] * (dom_nf >= 0)).sum())
     roofline = {"bound": "fp32", "achieved": ach_dom, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": ach_dom / fp32_peak, "traffic": traffic,
                 "kernel": "k_team_setup + k_team_series<%d, float> (+ the FP64 refinement launch) of the %d-stream "
@@ -936,8 +979,9 @@ def main():
                                                         int(dg["host"]["nlayers"].max())),
                 "kernel_ms": group_ms[dom], "solves": dom_solves,
                 "kernel_time": "the group's RT launches alone on one stream, CUDA events",
-                "traffic_source": "DRAM bytes per solve of k_team_series<16, float> from one ncu capture "
-                                  "(profiles/k_team_series_16_float_cols8192.md) x the group's solves",
+                "traffic_source": "DRAM bytes per solve-layer of k_team_series<16, float> from one ncu capture "
+                                  "(profiles/k_team_series_16_float_cols8192.md) x the group's solve-layers",
+                "traffic_algorithmic": 152.0 * float((dg["host"]["nlayers"][:, None] * (dom_nf >= 0)).sum()),
                 "peak_source": "measured live: FFMA issue-rate probe (8 FMA chains/thread), of measured",
                 "note": "achieved = reference-algorithm flops (banded-LU BVP, nonsymmetric eigen-solve) of the solves "
                         "/ kernel time; the kernel executes a different, mostly FP32 operation mix",
@@ -1010,7 +1054,7 @@ def main():
         serving = serving_run(args, mie.generate_tables(list(SERVE_CHANNELS), nmom=32))
 
     cfg = bench_config(args)
-    cfg.update({"failed_solves": bad, "tuned_schedules": tuned, "launch": graph_note,
+    cfg.update({"failed_solves": bad, "tuned_schedules": tuned, "launch": graph_note, "contraction": args.contraction,
                 "groups": ("%d launch groups (stream count x layer bucket <= %s), concurrent on one CUDA stream each"
                            % (len(groups), args.buckets)) if side else "serial, one CUDA stream"})
     line = {
@@ -1020,7 +1064,7 @@ def main():
         "config": cfg, "gpu_launches": launches, "clocks": clk, "roofline": roofline, "cpu_baseline": cpu,
         "e2e": e2e, "rot_calc": rot_line, "edge_vars": edge_line, "aop": aop_line, "serving": serving,
         "config3_polarized": c3, "config0_plain_fp64": c0, "roofline_plain": roofline_plain,
-        "accuracy": acc, "accuracy_ssa_stress": stress,
+        "contraction_ab": contraction_ab, "accuracy": acc, "accuracy_ssa_stress": stress,
         "plain_fp64": {"value": plain_value, "unit": "radiances/s", "ms_per_step": rt_ms_d, "steps": args.plain_steps,
                        "mixed_over_plain": value / plain_value,
                        "mixed_vs_fp64_gpu_max": float(dev_err.max()),

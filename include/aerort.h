@@ -383,6 +383,20 @@ int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int
 int aerort_set_kernel(int nstreams, int precision, int kernel);
 int aerort_get_kernel(int nstreams, int precision);
 
+/* How the FP32 (mixed) team solve forms the moment contraction of its layer
+ * matrices, sum_l omega beta_l P_l^m(mu_i) P_l^m(mu_j) (the SAB/DAB sums of
+ * vlidort_solutions.f90:436-476): AERORT_CONTRACT_FMA (the default) on the
+ * CUDA cores; AERORT_CONTRACT_TF32X3 on the tensor cores, mma.sync m16n8k8
+ * with TF32 operands split as hi + lo (three products per pair, FP32
+ * accumulation; an error of order 2^-22 relative).  FP64 solves and the
+ * thread kernel always use the CUDA cores.  Process-wide; read when an entry
+ * point is called.  No counterpart in the reference.  aerort_get_moment_
+ * contraction returns the setting. */
+#define AERORT_CONTRACT_FMA 0
+#define AERORT_CONTRACT_TF32X3 1
+int aerort_set_moment_contraction(int mode);
+int aerort_get_moment_contraction(void);
+
 /* Allocation-free form of aerort_vlidort_scalar_lambert_batch_dev (same
  * arguments, same results).  No counterpart in the reference: it exists for
  * callers that must not have the library allocate or free device memory

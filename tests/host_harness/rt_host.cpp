@@ -62,3 +62,23 @@ extern "C" int host_scalar_lambert_mixed(int km, int nch, int nobs, int nstreams
   return dispatch<float>(km, nch, nobs, nstreams, nmom, rot, depol, tau, ssa, pmom, he, albedo, sza, raa, vza, nadir,
                          missing, max_fourier, rad, refl, nf, st);
 }
+// The mixed method's refinement decision for one Fourier series: terms sf[0..n)
+// (before the azimuth factor), relative azimuth raa; returns 1 when the solve
+// would be handed to the FP64 pass, and the last term in *mlast.
+extern "C" int host_refine_flag(int n, const double* sf, double raa, int* mlast) {
+  RtOptions opt{0, 1, 0, 1, 3, 3, kAccuracySingle, 6371.0, 1.0, -1};
+  SetupRecord r{};
+  r.raa = raa;
+  FourierSum sum;
+  int m = 0;
+  for (m = 0; m < n; ++m)
+    if (sum.add(opt, r, m, sf[m])) break;
+  *mlast = m;
+  int count = 0, list[1];
+  Worklist wl;
+  wl.out_list = list;
+  wl.out_count = &count;
+  wl.ratio = kRefineRatio;
+  wl.flag(sum, RT_OK, 0);
+  return count;
+}

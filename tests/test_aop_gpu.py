@@ -115,3 +115,25 @@ def test_bit_identical_six_elements_with_four_element_tables(tables6):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
     p = got[3]
     assert not np.array_equal(p[..., 4], p[..., 0]) and not np.array_equal(p[..., 5], p[..., 2])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("npol", [1, 6])
+def test_bit_identical_forty_tracers(tables6, npol):
+    # 40 tracers: the staged kernel's shared rows fit for nPol = 1; for
+    # nPol = 6 (two moment rows per tracer) they do not and the gathering
+    # kernel runs -- both paths give the oracle's bits
+    cols = synth.make_columns(16, [470.0, 550.0, 670.0, 865.0], seed=123 + npol)
+    names = synth.tracer_names()
+    names2 = names + names[::-1]
+    qm = np.asfortranarray(np.concatenate([cols["qm"], np.float32(0.5) * cols["qm"][:, ::-1, :]], axis=1))
+    chem = mie.ChemMie(tables6)
+    km, n = cols["km"], cols["ncol"]
+    ch = np.float32([550.0, 865.0])
+    got = mie.get_aop_vector(chem, km, n, 2, len(names2), ch, names2, 0, qm, cols["rh"], 24, npol)
+    qt, qb = zip(*[chem.query_idx(x) for x in names2])
+    want = oracle.get_aop_vector(tables6, km, n, 2, len(names2), ch, qt, qb, qm, cols["rh"], 24, npol)
+    chem.destroy()
+    assert got[4] == 0 and want[4] == 0
+    for a, b in zip(got[:4], want[:4]):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))

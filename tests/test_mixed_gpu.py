@@ -188,3 +188,28 @@ def test_team_kernel_mixed_on_long_layer_chains(N, cols):
         L.aerort_set_kernel(N, _lib.PREC_MIXED, old)
     assert rc == 0 and np.all(st == 0)
     assert np.max(np.abs(rad / orad - 1.0)) <= RTOL
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N,lo", [(8, 0.0), (12, 0.0), (16, 0.0), (16, 0.999)])
+def test_tensor_core_contraction(N, lo):
+    # AERORT_CONTRACT_TF32X3: the FP32 team solve forms the layer matrices'
+    # moment sums with mma.sync (3xTF32); same 1e-4 bar against the FP64 oracle
+    L = _lib.lib()
+    assert L.aerort_get_moment_contraction() == _lib.CONTRACT_FMA
+    assert L.aerort_set_moment_contraction(7) != 0
+    kern = L.aerort_get_kernel(N, _lib.PREC_MIXED)
+    assert L.aerort_set_kernel(N, _lib.PREC_MIXED, _lib.KERNEL_TEAM) == 0
+    try:
+        assert L.aerort_set_moment_contraction(_lib.CONTRACT_TF32X3) == 0
+        rng = (lo, 1.0) if lo > 0 else None
+        c = random_aop_case(N, 72, nobs=24, nch=2, seed=N * 13 + 5, **({"ssa_range": rng} if rng else {}))
+        rad, refl, rc, nf, st = _mixed(c, N)
+    finally:
+        L.aerort_set_moment_contraction(_lib.CONTRACT_FMA)
+        L.aerort_set_kernel(N, _lib.PREC_MIXED, kern)
+    orad, _, _, onf, ost = oracle.scalar_lambert(*rt_args(c, N), MISSING)
+    assert rc == 0 and np.all(st == 0)
+    ok = orad != MISSING
+    err = np.abs(rad[ok] / orad[ok] - 1.0)
+    assert err.max() <= RTOL, err.max()

@@ -168,3 +168,36 @@ def test_team_solver_over_modis_brdf_matches_oracle(team_lib, nstreams, km):
     assert np.array_equal(nf[ok], onf[ok]) and np.all(st == 0)
     assert np.max(np.abs(rad[ok] / orad[ok] - 1)) < 1e-9
     assert np.max(np.abs(refl[ok] / orefl[ok] - 1)) < 1e-9
+
+
+def _refine(lib, sf, raa=0.0):
+    a = np.ascontiguousarray(sf, np.float64)
+    ml = ctypes.c_int(0)
+    f = lib.host_refine_flag(len(a), a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_double(raa),
+                             ctypes.byref(ml))
+    return f, ml.value
+
+
+def test_refinement_flags_convergence_tests_at_the_threshold(host_lib):
+    # a mixed-method solve goes to the FP64 pass when a convergence test's
+    # |term / sum| lies within 1e-3 (relative) of the accuracy threshold
+    # (1e-4): its FP32 terms could decide that test the other way
+    acc = 1e-4
+
+    def series(q):  # term 1 at ratio q, then two converged terms
+        s1 = q / (1.0 - q)
+        return [1.0, s1, 1e-9, 1e-9]
+    for q, want in ((acc * (1 + 5e-4), 1), (acc * (1 - 5e-4), 1), (acc * (1 + 5e-3), 0), (acc * (1 - 5e-3), 0),
+                    (0.3, 0)):
+        f, _ = _refine(host_lib, series(q))
+        assert f == want, (q, f)
+    # the 865 nm radiance of a 12-stream, 21-layer column whose FP64 series
+    # stops after term 8 at |term / sum| = 0.99998e-4 (the FP32 one, at
+    # 1.00018e-4, ran on to term 13, 7.9e-4 away): flagged
+    terms = [2.107697e-02, 2.737219e-04, -8.405132e-04, -2.020928e-05, 2.019701e-05, 5.192561e-06, -6.980721e-06,
+             -1.281008e-07, -2.050567e-06]
+    f, ml = _refine(host_lib, terms)
+    assert ml == 8 and f == 1
+    # cancellation (sum |terms| > 10 |sum|) still flags on its own
+    f, _ = _refine(host_lib, [1.0, -0.95, 1e-9, 1e-9])
+    assert f == 1
