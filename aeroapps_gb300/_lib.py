@@ -63,6 +63,16 @@ _SIGNATURES = {
     "aerort_vlidort_scalar_landmodis_batch_dev": (c_int, [c_int] * 6 + [c_void_p] * 11 + [P_d] + [c_void_p] * 3 +
                                                   [c_double] + [c_void_p] * 6),
     "aerort_vlidort_vector_lambert_batch_dev": (c_int, [c_int] * 6 + [c_void_p] * 16 + [c_double] + [c_void_p] * 7),
+    "aerort_vlidort_scalar_cx": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 15 +
+                                 [c_double, c_int, P_d, P_d, P_d]),
+    "aerort_vlidort_scalar_cx_ex": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 15 +
+                                    [c_double, c_int, P_d, P_d, P_d, P_i, P_i]),
+    "aerort_vlidort_scalar_cx_batch_dev": (c_int, [c_int] * 6 + [c_void_p] * 16 + [c_double] + [c_void_p] * 6),
+    "aerort_vlidort_scalar_gisscx": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 15 +
+                                     [c_double, c_int, P_d, P_d, P_d]),
+    "aerort_vlidort_scalar_gisscx_ex": (c_int, [c_int, c_int, c_int, P_d, c_int, c_int, c_int, c_int] + [P_d] * 15 +
+                                        [c_double, c_int, P_d, P_d, P_d, P_i, P_i]),
+    "aerort_vlidort_scalar_gisscx_batch_dev": (c_int, [c_int] * 6 + [c_void_p] * 16 + [c_double] + [c_void_p] * 6),
     "aerort_get_edge_vars": (c_int, [c_int, c_int, P_f, P_f, ctypes.c_float, P_f, P_f, P_f]),
     "aerort_get_edge_vars_dev": (c_int, [c_int, c_int, c_void_p, c_void_p, ctypes.c_float, c_void_p, c_void_p,
                                          c_void_p, c_void_p]),

@@ -338,11 +338,15 @@ __global__ void __launch_bounds__(256) k_aop(const DevMieTable* __restrict__ tab
 // layer fastest, so qm, rh reads and output stores stay coalesced).  The
 // block first copies, for every tracer, the bext, bsca and g rows of its
 // table and size bin at this channel (all RH nodes, row stride R), then for
-// each chunk of MC moments and each element group the moment rows; the
+// each chunk of MC moments of each element group the moment rows; the
 // per-element lerps read them from shared memory instead of gathering them
-// from L1/L2.  Operations and their order are those of k_aop, so the bits
-// are too.  Shared memory: nq (3 + P MC) R + 256 EPT floats, P = 2 for
-// nPol = 6 (paired elements), else 1.
+// from L1/L2.  The first chunk's pass over the tracers also sums tau, ssa
+// and g (so nMom <= MC needs one pass over the tracers, each tracer's rows
+// and weights formed once per element); the later chunks recompute the rows
+// and read the element's ssa tau from shared memory.  Operations and their
+// order are those of k_aop for every accumulator, so the bits are too.
+// Shared memory: nq (3 + P MC) R + 256 EPT floats, P = 2 for nPol = 6
+// (paired elements), else 1.
 template <int MC, int EPT>
 __global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restrict__ tabs, int km, int nobs, int nch,
                                                     int nq, const AopMeta meta, const float* __restrict__ qm,
@@ -373,7 +377,6 @@ __global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restric
     }
     s_sc[x] = v;
   }
-  __syncthreads();
   const long total = (long)km * nch * nobs;
   auto snap = [&](int k, int i) {
     const float rhUse = fminf(rh[k + (long)km * i], 0.99f);
@@ -399,20 +402,8 @@ __global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restric
     w.ssa = __fdiv_rn(bsca, bext);
     return true;
   };
-  for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    const int k = (int)(e % km), i = (int)(e / km);
-    const int isnap = snap(k, i);
-    const float* qcol = qm + k + (long)km * (long)nq * i;
-    float ts = 0.0f, ss = 0.0f, gs = 0.0f;
-    for (int iq = 0; iq < nq; ++iq) {
-      Row w;
-      if (!row_of(iq, isnap, qcol[(long)km * iq], w)) continue;
-      const float* sc = s_sc + (long)iq * 3 * R;
-      const float gg = lerp_ref(sc[2 * R + w.r0], sc[2 * R + w.r1], w.w0, w.arh);
-      ts = __fadd_rn(ts, w.tau);
-      ss = __fadd_rn(ss, __fmul_rn(w.ssa, w.tau));
-      gs = __fadd_rn(gs, __fmul_rn(__fmul_rn(gg, w.ssa), w.tau));
-    }
+  // tau, ssa, g of an element from its sums (VLIDORT_MieMod.F90:320-334); returns ssa_out * tau_out
+  auto finish = [&](long e, int k, int i, float ts, float ss, float gs) -> float {
     const float ssa_out = ts > 0.0f ? __fdiv_rn(ss, ts) : ss;
     const float st = __fmul_rn(ssa_out, ts);
     const float g_out = st > 0.0f ? __fdiv_rn(gs, st) : gs;
@@ -421,6 +412,27 @@ __global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restric
     ssa[o] = ssa_out;
     g[o] = g_out;
     s_st[e - e0] = st;
+    return st;
+  };
+  if (nMom <= 0) {  // no moments: the scattering sums alone
+    __syncthreads();
+    for (long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+      const int k = (int)(e % km), i = (int)(e / km);
+      const int isnap = snap(k, i);
+      const float* qcol = qm + k + (long)km * (long)nq * i;
+      float ts = 0.0f, ss = 0.0f, gs = 0.0f;
+      for (int iq = 0; iq < nq; ++iq) {
+        Row w;
+        if (!row_of(iq, isnap, qcol[(long)km * iq], w)) continue;
+        const float* sc = s_sc + (long)iq * 3 * R;
+        const float gg = lerp_ref(sc[2 * R + w.r0], sc[2 * R + w.r1], w.w0, w.arh);
+        ts = __fadd_rn(ts, w.tau);
+        ss = __fadd_rn(ss, __fmul_rn(w.ssa, w.tau));
+        gs = __fadd_rn(gs, __fmul_rn(__fmul_rn(gg, w.ssa), w.tau));
+      }
+      finish(e, k, i, ts, ss, gs);
+    }
+    return;
   }
   const int ngroups = nPol == 6 ? 4 : nPol;
   for (int grp = 0; grp < ngroups; ++grp) {
@@ -428,7 +440,8 @@ __global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restric
     const int eb = nPol == 6 ? (grp == 0 ? 4 : (grp == 2 ? 5 : -1)) : -1;
     for (int m0 = 0; m0 < nMom; m0 += MC) {
       const int mc = nMom - m0 < MC ? nMom - m0 : MC;
-      __syncthreads();  // the previous chunk's readers are done
+      const bool first = grp == 0 && m0 == 0;
+      __syncthreads();  // the previous chunk's readers are done (and s_sc is written)
       for (int x = threadIdx.x; x < nq * P * MC * R; x += blockDim.x) {
         const int r = x % R, j = (x / R) % MC, p = (x / (R * MC)) % P, q = x / (R * MC * P);
         const int tb = meta.q_table[q];
@@ -453,9 +466,17 @@ __global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restric
         float a[MC], b[MC];
 #pragma unroll
         for (int j = 0; j < MC; ++j) { a[j] = 0.0f; b[j] = 0.0f; }
+        float ts = 0.0f, ss = 0.0f, gs = 0.0f;
         for (int iq = 0; iq < nq; ++iq) {
           Row w;
           if (!row_of(iq, isnap, qcol[(long)km * iq], w)) continue;
+          if (first) {
+            const float* sc = s_sc + (long)iq * 3 * R;
+            const float gg = lerp_ref(sc[2 * R + w.r0], sc[2 * R + w.r1], w.w0, w.arh);
+            ts = __fadd_rn(ts, w.tau);
+            ss = __fadd_rn(ss, __fmul_rn(w.ssa, w.tau));
+            gs = __fadd_rn(gs, __fmul_rn(__fmul_rn(gg, w.ssa), w.tau));
+          }
           const bool sph = (nPol == 6 && tabs[meta.q_table[iq]].npol == 4);
           const float* pa = s_mo + (long)iq * P * MC * R;
 #pragma unroll
@@ -481,7 +502,7 @@ __global__ void __launch_bounds__(256) k_aop_staged(const DevMieTable* __restric
             }
           }
         }
-        const float st = s_st[e - e0];
+        const float st = first ? finish(e, k, i, ts, ss, gs) : s_st[e - e0];
         const long o = k + (long)km * (n + (long)nch * i);
 #pragma unroll
         for (int j = 0; j < MC; ++j) {
@@ -619,21 +640,29 @@ int aop_launch(aerort_mie* mie, int km, int nobs, int nch, int nq, const std::ve
   long total = (long)km * nch * nobs;
   if (total == 0) return 0;
   // table rows staged in shared memory when they fit (k_aop_staged), else gathered (k_aop)
-  constexpr int kMC = 8, kEPT = 16;
+  // (16-moment chunks for one element per moment, 8 for the paired elements of nPol = 6)
+  constexpr int kEPT = 16;
+  constexpr size_t kSmemMax = 96 * 1024;
   int R = 1;
   for (int q = 0; q < nq; ++q)
     if (q_table[q] >= 0 && mie->host_desc[q_table[q]].nrh > R) R = mie->host_desc[q_table[q]].nrh;
   const int P = nPol == 6 ? 2 : 1;
-  const size_t smem = sizeof(float) * ((size_t)nq * (3 + P * kMC) * R + 256 * kEPT);
-  if (nq > 0 && smem <= 96 * 1024) {
+  const int mc = P == 1 ? 16 : 8;
+  const size_t smem = sizeof(float) * ((size_t)nq * (3 + P * mc) * R + 256 * kEPT);
+  if (nq > 0 && smem <= kSmemMax) {
     static bool attr_set = false;
     if (!attr_set) {
-      CUDA_TRY(cudaFuncSetAttribute(k_aop_staged<kMC, kEPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+      CUDA_TRY(cudaFuncSetAttribute(k_aop_staged<16, kEPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
+      CUDA_TRY(cudaFuncSetAttribute(k_aop_staged<8, kEPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemMax));
       attr_set = true;
     }
     const long nel = (long)km * nobs;
     const dim3 grid((unsigned)((nel + 256L * kEPT - 1) / (256L * kEPT)), (unsigned)nch);
-    k_aop_staged<kMC, kEPT><<<grid, 256, smem, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, R,
+    if (mc == 16)
+      k_aop_staged<16, kEPT><<<grid, 256, smem, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, R,
+                                                     tau, ssa, g, pmom);
+    else
+      k_aop_staged<8, kEPT><<<grid, 256, smem, s>>>(mie->d_tables, km, nobs, nch, nq, meta, qm, rh, nMom, nPol, R,
                                                     tau, ssa, g, pmom);
   } else {
     const int bs = 256;

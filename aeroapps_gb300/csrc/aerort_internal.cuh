@@ -123,10 +123,25 @@ int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::Lamb
 int lambert_checks(int km, int nch, int nobs, int nstreams, int nMom);
 
 // VLIDORT_Scalar_LandMODIS (RTLS BRDF surface), FP64 two-pass team solve.
+// The BRDF surface of a VLIDORT_Scalar_LandMODIS or VLIDORT_Scalar_CX call.
+struct BrdfSurface {
+  int kind = aerort::kBrdfRTLS;
+  // RTLS: kernel amplitudes (3, nch, nobs) on the device; Li-sparse
+  // parameter pairs and each solve's pair (null: one pair) on the host
+  const double* kw = nullptr;
+  const int* tab_host = nullptr;
+  const double* tpar_host = nullptr;
+  int ntab = 0;
+  // Cox-Munk: winds (nobs) and refractive index (nch) on the device
+  const double* u10 = nullptr;
+  const double* v10 = nullptr;
+  const double* mr = nullptr;
+};
+
 template <int NS>
-int launch_scalar_landmodis(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in,
-                            const double* kw, const int* tab_host, const double* tpar_host, int ntab, double* rad,
-                            double* refl, double* br, int* nf, int* st, cudaStream_t s);
+int launch_scalar_brdf(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in,
+                       const BrdfSurface& sf, double* rad, double* refl, double* br, int* nf, int* st,
+                       cudaStream_t s);
 
 // Static device arena of the allocation-free entry point (rt_static.cu):
 // address of the calling thread's current device's copy, set up on first use.

@@ -168,6 +168,87 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 
   }
 }
 
+// FP64 re-solve of a mixed launch's refinement list (wl.in_list) with each
+// solve's Fourier terms spread over the W warps of a block: warp w runs terms
+// m0 + w of each round, one thread adds the round's terms to the Fourier sum
+// in order with the convergence test, and the round that ends the series
+// ends the solve (its later terms are discarded).  Every term is the one
+// team_fourier_series would compute (team_skip_terms carries P~_m^m over the
+// terms a warp skips), so the radiances are the same bits; a short list's
+// latency drops from one whole solve on one warp to about a W-th of it.  One
+// solve per block at a time; the block's set-up thread fills its scratch.
+template <int NS, int W>
+__global__ void __launch_bounds__(32 * W, 1)
+    k_refine_terms(RtOptions opt, LambertInputs in, Quad q, void* scratch, int* counter, double* rad, double* refl,
+                   int* nf, int* st, Worklist wl) {
+  extern __shared__ __align__(16) unsigned char team_smem[];
+  __shared__ double s_sf[W];
+  __shared__ int s_tst[W];
+  __shared__ int s_idx, s_live, s_stop, s_m, s_st;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  TeamMem<NS, double>& M = reinterpret_cast<TeamMem<NS, double>*>(team_smem)[w];
+  const ScratchLayout<NS> lay(in.km, false);
+  const SolveScratch<double> S = make_scratch<NS, double>(scratch, blockIdx.x, gridDim.x, in.km, false);
+  const Team tm{lane, nullptr, nullptr};
+  const int n = *wl.in_count;
+  for (;;) {
+    if (threadIdx.x == 0) s_idx = atomicAdd(counter, 1);
+    __syncthreads();
+    const int idx = s_idx;
+    if (idx >= n) break;
+    const int sidx = wl.in_list[idx];
+    if (threadIdx.x == 0) {
+      SetupRecord r;
+      const bool ok = solve_setup<NS, double>(opt, in, sidx, q.tu, q.wu, S, rad, refl, nf, st, r);
+      if (ok) r.store(S.D, lay.rec);
+      s_live = ok ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_live) {
+      SetupRecord r;
+      r.load(S.D, lay.rec);
+      SolveCtx<NS, double> c;
+      team_series_init<NS, double>(tm, M, r, q.qx, q.qw, c);
+      FourierSum sum;  // thread 0's
+      int last = -1;
+      for (int m0 = 0;; m0 += W) {
+        const int m = m0 + w;
+        int tst = RT_OK;
+        double sf = 0.0;
+        if (m <= r.n_fouriers) {
+          team_skip_terms<NS, double>(tm, M, c, last, m);
+          tst = team_fourier_term<NS, double>(tm, M, c, opt, m, S.W, lay, &sf);
+          last = m;
+        }
+        if (lane == 0) {
+          s_sf[w] = sf;
+          s_tst[w] = tst;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          int stop = 0;
+          for (int k = 0; k < W && !stop; ++k) {
+            const int mk = m0 + k;
+            if (mk > r.n_fouriers) { stop = 1; s_m = mk; s_st = RT_OK; }
+            else if (s_tst[k] != RT_OK) { stop = 1; s_m = mk; s_st = s_tst[k]; }
+            else if (sum.add(opt, r, mk, s_sf[k])) { stop = 1; s_m = mk; s_st = RT_OK; }
+          }
+          s_stop = stop;
+        }
+        __syncthreads();
+        if (s_stop) break;
+      }
+      if (threadIdx.x == 0) solve_finish(opt, in, r, s_st, s_m, sum.stokes, rad, refl, nf, st);
+    }
+    __syncthreads();
+  }
+}
+
+// Warps per block of k_refine_terms: as many FP64 TeamMems as fit one block's
+// shared memory, at most 8.
+template <int NS>
+constexpr int kRefineWarps = (NS >= 16) ? 6 : 8;
+
 // Enqueue the two-pass team solve on storage at `base`: per-solve scratch for
 // `slice` solves and their live flags at live_off; counter and first are two
 // scheduling ints.
@@ -221,6 +302,30 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
   const int bs = 32 * WPB;
   const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
+  if (wl.in_list && sizeof(T) == sizeof(double)) {
+    // refinement list: the term-parallel FP64 re-solve, one block per SM
+    constexpr int W = kRefineWarps<NS>;
+    const size_t rsmem = sizeof(TeamMem<NS, double>) * W;
+    CUDA_TRY(cudaFuncSetAttribute(k_refine_terms<NS, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
+    long nblocks = c.num_sms;
+    if (nblocks > nsolve) nblocks = nsolve;
+    const ScratchLayout<NS> lay(in.km, false);
+    if (int rc = c.pad->scratch.ensure((size_t)lay.template bytes<double>() * nblocks)) return rc;
+    if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
+    int* counter = (int*)c.pad->counter.p;
+    int* first = counter + 1;
+    k_init_sched<<<1, 1, 0, s>>>(counter, first, in.nobs, wl.out_count);
+    k_nadir_first<<<(in.nobs + 127) / 128, 128, 0, s>>>(in.nobs, in.nch, in.sza, in.raa, in.vza, in.albedo,
+                                                         in.missing, first);
+    CUDA_TRY(cudaGetLastError());
+    LambertInputs in2 = in;
+    in2.nadir_first = first;
+    k_refine_terms<NS, W><<<(unsigned)nblocks, 32 * W, rsmem, s>>>(opt, in2, q, c.pad->scratch.p, counter, rad,
+                                                                   refl, nf, st, wl);
+    CUDA_TRY(cudaGetLastError());
+    count_launches(3);
+    return 0;
+  }
   if (!wl.in_list) {
     int per_sm = 0;
     if (int rc = team_series_blocks_per_sm<NS, T>(&per_sm)) return rc;
@@ -416,15 +521,16 @@ int launch_scalar_lambert_fixed(const RtOptions& opt, const LambertInputs& in, v
 }
 
 // ---------------------------------------------------------------------------------- RTLS BRDF surface
-// VLIDORT_Scalar_LandMODIS on the two-pass team solve (FP64): k_brdf_setup
-// runs each solve's set-up with its BRDF block (rt_brdf.cuh), k_brdf_series
-// the Fourier series with the BRDF surface.  The BRDF inputs are a
-// __grid_constant__ parameter: the kernels read them from parameter space
-// through a pointer, without a per-thread copy.
+// VLIDORT_Scalar_LandMODIS and VLIDORT_Scalar_CX on the two-pass team solve
+// (FP64): k_brdf_setup runs each solve's set-up with its BRDF block
+// (rt_brdf.cuh), k_brdf_series the Fourier series with the BRDF surface.  The
+// BRDF inputs are a __grid_constant__ parameter: the kernels read them from
+// parameter space through a pointer, without a per-thread copy.
 
-// Sticky nadir-FO flag of the BRDF wrapper (VLIDORT_BRDF_MODIS.F90:113-185):
-// the first pixel with valid angles, solar zenith exactly 0 and a channel
-// whose exact BRDF is not negative (such a call reaches Run_Scalar).
+// Sticky nadir-FO flag of the BRDF wrappers (VLIDORT_BRDF_MODIS.F90:113-185,
+// VLIDORT_BRDF_CX.F90:497-560): the first pixel with valid angles, solar
+// zenith exactly 0 and a channel that reaches Run_Scalar (RTLS: its exact
+// BRDF is not negative; Cox-Munk: its winds and refractive index are set).
 template <int NS>
 __global__ void k_brdf_nadir_first(LambertInputs in, const __grid_constant__ BrdfInputs b, int* first) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -433,8 +539,14 @@ __global__ void k_brdf_nadir_first(LambertInputs in, const __grid_constant__ Brd
   if (miss(in.sza[j]) || miss(in.vza[j]) || miss(in.raa[j]) || in.sza[j] != 0.0) return;
   for (int i = 0; i < in.nch; ++i) {
     const long w = (long)i + (long)in.nch * j;
-    const int t = b.tab ? b.tab[w] : 0;
-    if (!(brdf_exact(b.kw + 3 * w, b.tpar[2 * t], b.tpar[2 * t + 1], in.sza[j], in.vza[j], in.raa[j]) < 0.0)) {
+    bool solved;
+    if (b.kind != kBrdfRTLS) {
+      solved = !(miss(b.u10[j]) || miss(b.v10[j]) || miss(b.mr[i]));
+    } else {
+      const int t = b.tab ? b.tab[w] : 0;
+      solved = !(brdf_exact(b.kw + 3 * w, b.tpar[2 * t], b.tpar[2 * t + 1], in.sza[j], in.vza[j], in.raa[j]) < 0.0);
+    }
+    if (solved) {
       atomicMin(first, j);
       return;
     }
@@ -480,26 +592,30 @@ __global__ void __launch_bounds__(32 * WPB, 1)
   }
 }
 
-// Per call: kw (3, nch, nobs) on the device; ntab Li-sparse (h/b, b/r) pairs
+// The BRDF surface of a call (BrdfSurface, aerort_internal.cuh): RTLS kernel
+// amplitudes kw (3, nch, nobs) on the device, ntab Li-sparse (h/b, b/r) pairs
 // tpar_host and the table of every solve tab_host (nch x nobs, null when
-// ntab == 1), both on the host; br (nobs, nch) output on the device.
+// ntab == 1) on the host; or Cox-Munk winds u10, v10 (nobs) and refractive
+// index mr (nch) on the device.  br (nobs, nch) output on the device.
 template <int NS>
-int launch_scalar_landmodis(Context& c, const RtOptions& opt, const LambertInputs& in, const double* kw,
-                            const int* tab_host, const double* tpar_host, int ntab, double* rad, double* refl,
-                            double* br, int* nf, int* st, cudaStream_t s) {
+int launch_scalar_brdf(Context& c, const RtOptions& opt, const LambertInputs& in, const BrdfSurface& sf, double* rad,
+                       double* refl, double* br, int* nf, int* st, cudaStream_t s) {
   constexpr int WPB = 2;
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
+  const bool cx = sf.kind != kBrdfRTLS;  // a glint kernel
   Quad q;
   std::memset(&q, 0, sizeof(q));
   gauss_legendre01(NS, q.qx, q.qw);
   if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
   BrdfInputs b;
   std::memset(&b, 0, sizeof(b));
+  b.kind = sf.kind;
+  b.q.nb = cx ? kBrdfAzimuthCX : kBrdfAzimuth;
   {
-    double x[kBrdfAzimuth], w[kBrdfAzimuth];
-    gauss_legendre01(kBrdfAzimuth, x, w);
-    for (int k = 0; k < kBrdfAzimuth; ++k) {
+    double x[kBrdfAzimuthCX], w[kBrdfAzimuthCX];
+    gauss_legendre01(b.q.nb, x, w);
+    for (int k = 0; k < b.q.nb; ++k) {
       b.q.phi[k] = kPIE * x[k];
       b.q.a[k] = w[k];
       b.q.c[k] = std::cos(b.q.phi[k]);
@@ -507,12 +623,23 @@ int launch_scalar_landmodis(Context& c, const RtOptions& opt, const LambertInput
     }
   }
   for (int k = 0; k < NS; ++k) b.qx[k] = q.qx[k];
-  // quadrature-to-quadrature tables: Ross-thick, then Li-sparse per parameter pair
-  const size_t tab_elems = (size_t)2 * NS * NS * NS;
-  std::vector<double> qq((size_t)(1 + ntab) * tab_elems);
-  brdf_qq_table(NS, q.qx, b.q, false, 0.0, 0.0, qq.data());
-  for (int t = 0; t < ntab; ++t)
-    brdf_qq_table(NS, q.qx, b.q, true, tpar_host[2 * t], tpar_host[2 * t + 1], qq.data() + (1 + t) * tab_elems);
+  // RTLS: quadrature-to-quadrature tables, Ross-thick then Li-sparse per
+  // parameter pair; Cox-Munk: the azimuth weights a_k cos(m phi_k)
+  std::vector<double> qq;
+  const int ntab = cx ? 0 : sf.ntab;
+  if (cx) {
+    qq.resize((size_t)2 * NS * b.q.nb);
+    for (int m = 0; m < 2 * NS; ++m)
+      for (int k = 0; k < b.q.nb; ++k)
+        qq[(size_t)m * b.q.nb + k] = (m == 0) ? b.q.a[k] : b.q.a[k] * std::cos((double)m * b.q.phi[k]);
+  } else {
+    const size_t tab_elems = (size_t)2 * NS * NS * NS;
+    qq.resize((size_t)(1 + ntab) * tab_elems);
+    brdf_qq_table(NS, q.qx, b.q, false, 0.0, 0.0, qq.data());
+    for (int t = 0; t < ntab; ++t)
+      brdf_qq_table(NS, q.qx, b.q, true, sf.tpar_host[2 * t], sf.tpar_host[2 * t + 1],
+                    qq.data() + (1 + t) * tab_elems);
+  }
   int per_sm = 0;
   {
     const size_t smem = sizeof(TeamMem<NS, double>) * WPB;
@@ -520,30 +647,42 @@ int launch_scalar_landmodis(Context& c, const RtOptions& opt, const LambertInput
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_brdf_series<NS, WPB>, 32 * WPB, smem));
     if (per_sm < 1) return set_error(AERORT_RC_CUDA, "BRDF team kernel does not fit on an SM");
   }
-  const int slice = nsolve < kSetupSlice ? nsolve : kSetupSlice;
+  // Cox-Munk blocks hold each solve's 2N x N x N components: slices of at
+  // most ~2 GB of them
+  const long block = cx ? BrdfBlock<NS>::total_cx : BrdfBlock<NS>::total;
+  long max_slice = cx ? (2L << 30) / (8 * block) : kSetupSlice;
+  if (max_slice > kSetupSlice) max_slice = kSetupSlice;
+  const int slice = nsolve < max_slice ? nsolve : (int)max_slice;
   long nblocks = (long)per_sm * c.num_sms;
   if (nblocks > (slice + WPB - 1) / WPB) nblocks = (slice + WPB - 1) / WPB;
   const ScratchLayout<NS> lay(in.km, false);
   auto up256 = [](size_t v) { return (v + 255) / 256 * 256; };
   const size_t live_off = up256((size_t)lay.template bytes<double>() * slice);
   const size_t terms_off = live_off + up256((size_t)slice);
-  const size_t qq_off = terms_off + up256(sizeof(double) * (size_t)BrdfBlock<NS>::total * slice);
+  const size_t qq_off = terms_off + up256(sizeof(double) * (size_t)block * slice);
   const size_t tpar_off = qq_off + up256(sizeof(double) * qq.size());
   const size_t tab_off = tpar_off + up256(sizeof(double) * 2 * (size_t)ntab);
-  const size_t total = tab_off + (tab_host ? up256(sizeof(int) * (size_t)nsolve) : 0);
+  const size_t total = tab_off + (sf.tab_host && !cx ? up256(sizeof(int) * (size_t)nsolve) : 0);
   if (int rc = c.pad->scratch.ensure(total)) return rc;
   if (int rc = c.pad->counter.ensure(4 * sizeof(int))) return rc;
   char* base = (char*)c.pad->scratch.p;
   // pageable-memory copies: the host buffers may go once the calls return
   CUDA_TRY(cudaMemcpyAsync(base + qq_off, qq.data(), sizeof(double) * qq.size(), cudaMemcpyHostToDevice, s));
-  CUDA_TRY(cudaMemcpyAsync(base + tpar_off, tpar_host, sizeof(double) * 2 * (size_t)ntab, cudaMemcpyHostToDevice,
-                           s));
-  if (tab_host)
-    CUDA_TRY(cudaMemcpyAsync(base + tab_off, tab_host, sizeof(int) * (size_t)nsolve, cudaMemcpyHostToDevice, s));
-  b.kw = kw;
-  b.tab = tab_host ? (const int*)(base + tab_off) : nullptr;
-  b.tpar = (const double*)(base + tpar_off);
-  b.qq = (const double*)(base + qq_off);
+  if (cx) {
+    b.u10 = sf.u10;
+    b.v10 = sf.v10;
+    b.mr = sf.mr;
+    b.cf = (const double*)(base + qq_off);
+  } else {
+    CUDA_TRY(cudaMemcpyAsync(base + tpar_off, sf.tpar_host, sizeof(double) * 2 * (size_t)ntab,
+                             cudaMemcpyHostToDevice, s));
+    if (sf.tab_host)
+      CUDA_TRY(cudaMemcpyAsync(base + tab_off, sf.tab_host, sizeof(int) * (size_t)nsolve, cudaMemcpyHostToDevice, s));
+    b.kw = sf.kw;
+    b.tab = sf.tab_host ? (const int*)(base + tab_off) : nullptr;
+    b.tpar = (const double*)(base + tpar_off);
+    b.qq = (const double*)(base + qq_off);
+  }
   b.br = br;
   b.terms = (double*)(base + terms_off);
   b.stride = slice;
@@ -590,6 +729,6 @@ int launch_scalar_landmodis(Context& c, const RtOptions& opt, const LambertInput
   template int aerort_internal::launch_scalar_lambert_fixed<NS, float>(                                        \
       const aerort::RtOptions&, const aerort::LambertInputs&, void*, size_t, int*, int,                         \
       const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t, const aerort::Worklist&); \
-  template int aerort_internal::launch_scalar_landmodis<NS>(                                                   \
-      aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, const double*,          \
-      const int*, const double*, int, double*, double*, double*, int*, int*, cudaStream_t);
+  template int aerort_internal::launch_scalar_brdf<NS>(                                                        \
+      aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&,                         \
+      const aerort_internal::BrdfSurface&, double*, double*, double*, int*, int*, cudaStream_t);

@@ -1186,11 +1186,13 @@ RT_HD void solve_finish(const RtOptions& opt, const LambertInputs& in, const Set
 // first-order single scatter, beam attenuation.  Leaves the per-layer inputs of
 // the Fourier series in scratch and fills r.  Returns false when the pixel is
 // finished already (MISSING inputs or a bad layer: outputs written).
-// With `brdf` (VLIDORT_Scalar_LandMODIS, VLIDORT_BRDF_MODIS.F90:113-185) the
-// surface is the RTLS BRDF instead of the albedo: its exact direct-bounce
-// value BR feeds the first-order correction and the BR output (a negative BR
-// gives -500 in radiance, reflectance and BR and no solve), and the solve's
-// beam and view Fourier terms go to block `bidx` of brdf->terms.
+// With `brdf` the surface is a BRDF instead of the albedo: the RTLS kernels of
+// VLIDORT_Scalar_LandMODIS (VLIDORT_BRDF_MODIS.F90:113-185) or the Cox-Munk
+// glint of VLIDORT_Scalar_CX (VLIDORT_BRDF_CX.F90:497-545).  Its exact
+// direct-bounce value BR feeds the first-order correction and the BR output
+// (RTLS: a negative BR gives -500 in radiance, reflectance and BR and no
+// solve), and the solve's Fourier terms (Cox-Munk: also its quadrature-to-
+// quadrature terms) go to block `bidx` of brdf->terms.
 template <int NS, typename T>
 RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, const double* tu, const double* wu,
                        const SolveScratch<T>& SS, double* radiance, double* reflectance, int* nfourier,
@@ -1211,7 +1213,22 @@ RT_HD bool solve_setup(const RtOptions& opt, const LambertInputs& in, int sidx, 
     return false;
   }
   double refl_db = alb;  // surface reflectance of the direct bounce
-  if (brdf) {
+  if (brdf && brdf->kind != kBrdfRTLS) {
+    // VLIDORT_Scalar_CX / _GissCX (VLIDORT_BRDF_CX.F90:512-545, :1647-1690):
+    // MISSING winds or refractive index give MISSING outputs for this channel
+    const double u = brdf->u10[j], v = brdf->v10[j], m = brdf->mr[i];
+    if (is_missing(u) || is_missing(v) || is_missing(m)) {
+      radiance[o] = in.missing; reflectance[o] = in.missing;
+      brdf->br[o] = in.missing;
+      return false;
+    }
+    const CoxMunkPars p = brdf_cm_pars(brdf->kind == kBrdfGissCoxMunk, u, v, m);
+    const double b = brdf_exact_cx(p, sza, vza, raa);
+    brdf->br[o] = b;
+    refl_db = b;
+    const Scratch B{brdf->terms + bidx, brdf->stride};
+    brdf_solve_terms_cx<NS>(brdf->q, brdf->cf, brdf->qx, p, sza, vza, B);
+  } else if (brdf) {
     const long w = (long)i + (long)nch * j;
     const double* kw = brdf->kw + 3 * w;
     const int t = brdf->tab ? brdf->tab[w] : 0;

@@ -441,6 +441,23 @@ __device__ void team_contract_tf32x3(const Team& tm, TeamMem<NS, float>& M, int 
 }
 #endif
 
+// P~_k^k, which team_legendre carries from term to term, advanced over the
+// terms after `last` and before m (the same products in the same order), for
+// a warp that runs only some of a solve's terms (k_refine_terms).
+template <int NS, typename T>
+RT_HD void team_skip_terms(const Team& tm, TeamMem<NS, T>& M, const SolveCtx<NS, T>& c, int last, int m) {
+  const int i = tm.lane;
+  if (i < NS + 2) {
+    T s, *pim;
+    if (i < NS) { s = M.csin[i]; pim = &M.pimq[i]; }
+    else if (i == NS) { s = c.sin_u; pim = &M.pimu; }
+    else { s = c.sin_0; pim = &M.pim0; }
+    for (int k = last + 1; k < m; ++k)
+      if (k <= c.NM) *pim = (k == 0) ? (T)1 : *pim * s * sqrt((T)(2 * k - 1) / (T)(2 * k));
+  }
+  tm.sync();
+}
+
 // Eigen-solution of layer n for term m into P/Q/t of slot `cur`, with the
 // Green's-function norms and user-angle homogeneous solutions (layer_eigen).
 // tc: the FP32 solve forms the moment contraction on the tensor cores
@@ -1043,16 +1060,23 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
     const int fr = 1 - bl;
     using BB = BrdfBlock<NS>;
     Bb = Scratch{brdf->terms + bidx, brdf->stride};
-    const double fiso = Bb[BB::w], fvol = Bb[BB::w + 1], fgeo = Bb[BB::w + 2];
-    const int t = (int)Bb[BB::w + 3];
-    const double* qv = brdf->qq + (long)m * NS * NS;
-    const double* qg = brdf->qq + ((long)(1 + t) * 2 * NS + m) * NS * NS;
-    for (int e = tm.lane; e < N * N; e += kTeam) {
-      const int i = e / N, l = e % N;
-      double r = (m == 0) ? fiso : 0.0;
-      r += fvol * qv[i * NS + l];
-      r += fgeo * qg[i * NS + l];
-      M.Vp[i + LD * l] = (T)r;
+    if (brdf->kind != kBrdfRTLS) {  // a glint solve's own components
+      for (int e = tm.lane; e < N * N; e += kTeam) {
+        const int i = e / N, l = e % N;
+        M.Vp[i + LD * l] = (T)Bb[BB::qq + ((long)m * NS + i) * NS + l];
+      }
+    } else {
+      const double fiso = Bb[BB::w], fvol = Bb[BB::w + 1], fgeo = Bb[BB::w + 2];
+      const int t = (int)Bb[BB::w + 3];
+      const double* qv = brdf->qq + (long)m * NS * NS;
+      const double* qg = brdf->qq + ((long)(1 + t) * 2 * NS + m) * NS * NS;
+      for (int e = tm.lane; e < N * N; e += kTeam) {
+        const int i = e / N, l = e % N;
+        double r = (m == 0) ? fiso : 0.0;
+        r += fvol * qv[i * NS + l];
+        r += fgeo * qg[i * NS + l];
+        M.Vp[i + LD * l] = (T)r;
+      }
     }
     tm.sync();
     for (int e = tm.lane; e < N * N; e += kTeam) {
@@ -1162,16 +1186,15 @@ RT_HD int team_fourier_term(const Team& tm, TeamMem<NS, T>& M, SolveCtx<NS, T>& 
 
 // The Fourier series of one set-up solve, run by the whole team; lane 0 writes
 // the outputs.
-template <int NS, typename T, bool BRDF = false>
-RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOptions& opt, const LambertInputs& in,
-                               const SetupRecord& r, const double* qx, const double* qw, const ScratchT<T>& W,
-                               const ScratchLayout<NS>& lay, double* radiance, double* reflectance,
-                               int* nfourier, int* status, const Worklist& wl = Worklist(), int sidx = 0,
-                               const BrdfInputs* brdf = nullptr, long bidx = 0) {
-  SolveCtx<NS, T> c;
+// The team's per-solve state before term 0: the solve context and, in shared
+// memory for lane-indexed access, the quadrature arrays of make_ctx and the
+// Legendre P~_m^m carried across terms.
+template <int NS, typename T>
+RT_HD void team_series_init(const Team& tm, TeamMem<NS, T>& M, const SetupRecord& r, const double* qx,
+                            const double* qw, SolveCtx<NS, T>& c) {
   make_ctx<NS, T>(r, qx, qw, c);
   if (tm.lane < NS) {
-    const int q = tm.lane;  // the quadrature arrays of make_ctx, in shared memory for lane-indexed access
+    const int q = tm.lane;
     M.cqx[q] = (T)qx[q];
     M.cqw[q] = (T)qw[q];
     M.csqw[q] = (T)sqrt(qw[q]);
@@ -1180,6 +1203,16 @@ RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOption
   }
   if (tm.lane == 0) { M.pimu = 0; M.pim0 = 0; }
   tm.sync();
+}
+
+template <int NS, typename T, bool BRDF = false>
+RT_HD void team_fourier_series(const Team& tm, TeamMem<NS, T>& M, const RtOptions& opt, const LambertInputs& in,
+                               const SetupRecord& r, const double* qx, const double* qw, const ScratchT<T>& W,
+                               const ScratchLayout<NS>& lay, double* radiance, double* reflectance,
+                               int* nfourier, int* status, const Worklist& wl = Worklist(), int sidx = 0,
+                               const BrdfInputs* brdf = nullptr, long bidx = 0) {
+  SolveCtx<NS, T> c;
+  team_series_init<NS, T>(tm, M, r, qx, qw, c);
   FourierSum sum;
   int m = 0, st = RT_OK;
   for (m = 0; m <= r.n_fouriers; ++m) {

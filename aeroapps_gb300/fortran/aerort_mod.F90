@@ -7,6 +7,8 @@
 !   geo_vlidort.F90:598-603   call VLIDORT_Scalar_Lambert(...)  -> VLIDORT_Scalar_Lambert_GPU(...)
 !   geo_vlidort.F90:612-619   call VLIDORT_Vector_Lambert(...)  -> VLIDORT_Vector_Lambert_GPU(...)
 !   geo_vlidort.F90:640-646   call VLIDORT_Scalar_LandMODIS(...) -> VLIDORT_Scalar_LandMODIS_GPU(...)
+!   geo_vlidort_ocean.F90:536-544 call VLIDORT_Scalar_GissCX(...) -> VLIDORT_Scalar_GissCX_GPU(...)
+!   (VLIDORT_Scalar_CX, VLIDORT_BRDF_CX.F90:420-584, has VLIDORT_Scalar_CX_GPU)
 !   geo_vlidort.F90:558-560   call VLIDORT_ROT_CALC(...)        -> VLIDORT_ROT_CALC_GPU(...)
 ! The C prototypes are include/aerort.h; arrays pass by address in Fortran
 ! (column-major) order with the reference's shapes, scalars by value.  Every
@@ -18,6 +20,7 @@ module aerort_mod
   implicit none
   private
   public :: VLIDORT_Scalar_Lambert_GPU, VLIDORT_Vector_Lambert_GPU, VLIDORT_Scalar_LandMODIS_GPU
+  public :: VLIDORT_Scalar_CX_GPU, VLIDORT_Scalar_GissCX_GPU
   public :: VLIDORT_ROT_CALC_GPU, getEdgeVars_GPU
   public :: aerort_mie_table_desc, aerort_mie_create, aerort_mie_destroy, aerort_get_aop_vector
   public :: aerort_get_aop_scalar, aerort_mie_table_interp, aerort_last_error_string
@@ -66,6 +69,32 @@ module aerort_mod
       real(c_double), intent(in) :: relat_azymuth(*), sensor_zenith(*)
       real(c_double), value :: MISSING
       real(c_double), intent(out) :: radiance_VL_SURF(*), reflectance_VL_SURF(*), BR(*)
+    end function
+
+    integer(c_int) function aerort_vlidort_scalar_cx(km, nch, nobs, channels, nstreams, plane_parallel, &
+        nMom, nPol, ROT, depol, tau, ssa, g, pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, &
+        sensor_zenith, MISSING, verbose, radiance_VL_SURF, reflectance_VL_SURF, BRDF)                      &
+        bind(C, name="aerort_vlidort_scalar_cx")
+      import :: c_int, c_double
+      integer(c_int), value :: km, nch, nobs, nstreams, plane_parallel, nMom, nPol, verbose
+      real(c_double), intent(in) :: channels(*), ROT(*), depol(*), tau(*), ssa(*), g(*), pmom(*)
+      real(c_double), intent(in) :: pe(*), he(*), te(*), U10m(*), V10m(*), mr(*), solar_zenith(*)
+      real(c_double), intent(in) :: relat_azymuth(*), sensor_zenith(*)
+      real(c_double), value :: MISSING
+      real(c_double), intent(out) :: radiance_VL_SURF(*), reflectance_VL_SURF(*), BRDF(*)
+    end function
+
+    integer(c_int) function aerort_vlidort_scalar_gisscx(km, nch, nobs, channels, nstreams, plane_parallel, &
+        nMom, nPol, ROT, depol, tau, ssa, g, pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth,    &
+        sensor_zenith, MISSING, verbose, radiance_VL_SURF, reflectance_VL_SURF, BRDF)                         &
+        bind(C, name="aerort_vlidort_scalar_gisscx")
+      import :: c_int, c_double
+      integer(c_int), value :: km, nch, nobs, nstreams, plane_parallel, nMom, nPol, verbose
+      real(c_double), intent(in) :: channels(*), ROT(*), depol(*), tau(*), ssa(*), g(*), pmom(*)
+      real(c_double), intent(in) :: pe(*), he(*), te(*), U10m(*), V10m(*), mr(*), solar_zenith(*)
+      real(c_double), intent(in) :: relat_azymuth(*), sensor_zenith(*)
+      real(c_double), value :: MISSING
+      real(c_double), intent(out) :: radiance_VL_SURF(*), reflectance_VL_SURF(*), BRDF(*)
     end function
 
     integer(c_int) function aerort_vlidort_rot_calc(km, nch, nobs, channels, pe, he, te, MISSING, verbose, &
@@ -190,6 +219,42 @@ contains
     rc = aerort_vlidort_scalar_landmodis(km, nch, nobs, channels, nstreams, merge(1, 0, plane_parallel), nMom, nPol, &
          ROT, depol, tau, ssa, g, pmom, pe, he, te, kernel_wt, param, solar_zenith, relat_azymuth, sensor_zenith,    &
          MISSING, verbose, radiance_VL_SURF, reflectance_VL_SURF, BR)
+  end subroutine
+
+  ! Drop-in for VLIDORT_Scalar_CX (geo_vlidort/VLIDORT_BRDF_CX.F90:420-584),
+  ! Cox-Munk ocean glint: 10 m winds U10m, V10m (nobs), refractive index mr (nch)
+  subroutine VLIDORT_Scalar_CX_GPU(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, &
+      tau, ssa, g, pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith, MISSING,     &
+      verbose, radiance_VL_SURF, reflectance_VL_SURF, BRDF, rc)
+    integer, intent(in) :: km, nch, nobs, nstreams, nMom, nPol, verbose
+    logical, intent(in) :: plane_parallel
+    real*8, intent(in)  :: channels(nch), ROT(km,nobs,nch), depol(nch), tau(km,nch,nobs), ssa(km,nch,nobs)
+    real*8, intent(in)  :: g(km,nch,nobs), pmom(km,nch,nobs,nMom,nPol), pe(km+1,nobs), he(km+1,nobs)
+    real*8, intent(in)  :: te(km+1,nobs), U10m(nobs), V10m(nobs), mr(nch), solar_zenith(nobs)
+    real*8, intent(in)  :: relat_azymuth(nobs), sensor_zenith(nobs), MISSING
+    real*8, intent(out) :: radiance_VL_SURF(nobs,nch), reflectance_VL_SURF(nobs,nch), BRDF(1,nobs,nch)
+    integer, intent(out) :: rc
+    rc = aerort_vlidort_scalar_cx(km, nch, nobs, channels, nstreams, merge(1, 0, plane_parallel), nMom, nPol, &
+         ROT, depol, tau, ssa, g, pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith,  &
+         MISSING, verbose, radiance_VL_SURF, reflectance_VL_SURF, BRDF)
+  end subroutine
+
+  ! Drop-in for VLIDORT_Scalar_GissCX (geo_vlidort/VLIDORT_BRDF_CX.F90:1553-1716),
+  ! GISS Cox-Munk ocean glint, the call of geo_vlidort_ocean.F90:536
+  subroutine VLIDORT_Scalar_GissCX_GPU(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, &
+      tau, ssa, g, pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith, MISSING,         &
+      verbose, radiance_VL_SURF, reflectance_VL_SURF, BRDF, rc)
+    integer, intent(in) :: km, nch, nobs, nstreams, nMom, nPol, verbose
+    logical, intent(in) :: plane_parallel
+    real*8, intent(in)  :: channels(nch), ROT(km,nobs,nch), depol(nch), tau(km,nch,nobs), ssa(km,nch,nobs)
+    real*8, intent(in)  :: g(km,nch,nobs), pmom(km,nch,nobs,nMom,nPol), pe(km+1,nobs), he(km+1,nobs)
+    real*8, intent(in)  :: te(km+1,nobs), U10m(nobs), V10m(nobs), mr(nch), solar_zenith(nobs)
+    real*8, intent(in)  :: relat_azymuth(nobs), sensor_zenith(nobs), MISSING
+    real*8, intent(out) :: radiance_VL_SURF(nobs,nch), reflectance_VL_SURF(nobs,nch), BRDF(1,nobs,nch)
+    integer, intent(out) :: rc
+    rc = aerort_vlidort_scalar_gisscx(km, nch, nobs, channels, nstreams, merge(1, 0, plane_parallel), nMom, nPol, &
+         ROT, depol, tau, ssa, g, pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith,      &
+         MISSING, verbose, radiance_VL_SURF, reflectance_VL_SURF, BRDF)
   end subroutine
 
   ! Drop-in for VLIDORT_ROT_CALC (geo_vlidort/VLIDORT_ROT.F90:19-86)

@@ -85,6 +85,42 @@ def vlidort_scalar_landmodis(km, nch, nobs, channels, nstreams, plane_parallel, 
     return rad, refl, br, rc
 
 
+def vlidort_scalar_cx(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g, pmom,
+                      pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith, MISSING=MISSING,
+                      verbose=0, diagnostics=False, giss=False):
+    """VLIDORT_Scalar_CX: scalar TOA radiance/reflectance over the Cox-Munk
+    ocean glint (geo_vlidort/VLIDORT_BRDF_CX.F90:420-584); giss=True:
+    VLIDORT_Scalar_GissCX (:1553-1716), the GISS Cox-Munk kernel.
+
+    As vlidort_scalar_lambert with the albedo replaced by the 10 m wind
+    components U10m, V10m (nobs) and the water refractive index mr (nch).
+    Returns (radiance, reflectance, BRDF, rc), plus (nfourier, status) with
+    diagnostics=True; BRDF(nobs,nch) is the exact direct-bounce BRDF."""
+    arrs = [_f64(channels), _f64(ROT), _f64(depol), _f64(tau), _f64(ssa), _f64(g), _f64(pmom), _f64(pe), _f64(he),
+            _f64(te), _f64(U10m), _f64(V10m), _f64(mr), _f64(solar_zenith), _f64(relat_azymuth), _f64(sensor_zenith)]
+    ch, ROT, depol, tau, ssa, g, pmom, pe, he, te, u, v, mr, sza, raa, vza = arrs
+    if ROT.shape != (km, nobs, nch) or tau.shape != (km, nch, nobs) or he.shape != (km + 1, nobs):
+        raise ValueError("array shapes do not match (km, nch, nobs) = (%d, %d, %d)" % (km, nch, nobs))
+    if u.shape != (nobs,) or v.shape != (nobs,) or mr.shape != (nch,):
+        raise ValueError("U10m, V10m must have shape (nobs,) and mr (nch,)")
+    rad = np.zeros((nobs, nch), np.float64, order="F")
+    refl = np.zeros_like(rad)
+    br = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    P = lambda a: _lib.ptr(a, _lib.P_d)
+    fn = _lib.lib().aerort_vlidort_scalar_gisscx_ex if giss else _lib.lib().aerort_vlidort_scalar_cx_ex
+    rc = fn(
+        km, nch, nobs, P(ch), nstreams, int(bool(plane_parallel)), nMom, nPol, P(ROT), P(depol), P(tau), P(ssa), P(g),
+        P(pmom), P(pe), P(he), P(te), P(u), P(v), P(mr), P(sza), P(raa), P(vza), float(MISSING), int(verbose), P(rad),
+        P(refl), P(br), _lib.ptr(nf, _lib.P_i), _lib.ptr(st, _lib.P_i))
+    if rc >= 1000:
+        raise RuntimeError("aerort_vlidort_scalar_%scx rc=%d: %s" % ("giss" if giss else "", rc, _lib.last_error()))
+    if diagnostics:
+        return rad, refl, br, rc, nf, st
+    return rad, refl, br, rc
+
+
 def vlidort_scalar_lambert_dev(km, nch, nobs, nstreams, nMom, ROT, depol, tau, ssa, pmom, he, albedo, solar_zenith,
                                relat_azymuth, sensor_zenith, radiance, reflectance, nfourier=None, status=None,
                                MISSING=MISSING, plane_parallel=False, stream=0):
@@ -176,3 +212,9 @@ def rot_calc(channels, pe, he, te, MISSING, verbose=0):
                                    _lib.ptr(he, _lib.P_d), _lib.ptr(te, _lib.P_d), float(MISSING), int(verbose),
                                    _lib.ptr(rot, _lib.P_d), _lib.ptr(depol, _lib.P_d))
     return rot, depol, rc
+
+
+def vlidort_scalar_gisscx(*args, **kw):
+    """VLIDORT_Scalar_GissCX (geo_vlidort/VLIDORT_BRDF_CX.F90:1553-1716): the
+    arguments and returns of vlidort_scalar_cx over the GISS Cox-Munk kernel."""
+    return vlidort_scalar_cx(*args, giss=True, **kw)

@@ -302,6 +302,80 @@ int aerort_vlidort_scalar_landmodis_batch_dev(int km, int nch, int nobs, int nst
                                               double* reflectance_VL_SURF, double* BR, int* nfourier, int* status,
                                               void* stream);
 
+/* VLIDORT_Scalar_CX (geo_vlidort/VLIDORT_BRDF_CX.F90:420-584): the scalar
+ * solve of aerort_vlidort_scalar_lambert over the Cox-Munk ocean glint of
+ * VLIDORT_CoxMunk_SingleGeom (RTSI/VLIDORT2p8p3/VLIDORT_SurfaceMod.F90
+ * :816-1042) -- one Cox-Munk kernel with shadowing, slope variance
+ * 0.003 + 0.00512 W from the wind speed W = |(U10m, V10m)| clamped to
+ * [0, 50] m/s, refractive index squared mr(ch)^2, 100 azimuth streams -- in
+ * place of the albedo; same argument list as the reference (BRDF(nobs, nch):
+ * the exact direct-bounce BRDF of each pixel and channel).  A pixel with
+ * MISSING angles, or a channel with a MISSING wind component or refractive
+ * index, gets MISSING radiance and reflectance (and BRDF, which the reference
+ * leaves unset there).  FP64.  rc as aerort_vlidort_scalar_lambert. */
+int aerort_vlidort_scalar_cx(int km, int nch, int nobs, const double* channels, int nstreams, int plane_parallel,
+                             int nMom, int nPol, const double* ROT, const double* depol, const double* tau,
+                             const double* ssa, const double* g, const double* pmom, const double* pe,
+                             const double* he, const double* te, const double* U10m, const double* V10m,
+                             const double* mr, const double* solar_zenith, const double* relat_azymuth,
+                             const double* sensor_zenith, double MISSING, int verbose, double* radiance_VL_SURF,
+                             double* reflectance_VL_SURF, double* BRDF);
+/* Same, plus nfourier(nobs,nch) and status(nobs,nch) (either may be NULL). */
+int aerort_vlidort_scalar_cx_ex(int km, int nch, int nobs, const double* channels, int nstreams, int plane_parallel,
+                                int nMom, int nPol, const double* ROT, const double* depol, const double* tau,
+                                const double* ssa, const double* g, const double* pmom, const double* pe,
+                                const double* he, const double* te, const double* U10m, const double* V10m,
+                                const double* mr, const double* solar_zenith, const double* relat_azymuth,
+                                const double* sensor_zenith, double MISSING, int verbose, double* radiance_VL_SURF,
+                                double* reflectance_VL_SURF, double* BRDF, int* nfourier, int* status);
+/* Batched device form (no counterpart routine in the reference): arrays on
+ * the device as aerort_vlidort_scalar_lambert_batch_dev (nlay and FP32
+ * optics optional), U10m, V10m (nobs) and mr (nch) on the device, BRDF(nobs,
+ * nch) out on the device.  Each solve's quadrature-to-quadrature Cox-Munk
+ * components are formed on the device (they depend on its wind and
+ * refractive index).  Enqueued on `stream`; an azimuth-weight table goes up
+ * by a pageable-memory copy, so this call does not belong in a stream capture. */
+int aerort_vlidort_scalar_cx_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                       const int* nlay, const double* ROT, const double* depol, const double* tau,
+                                       const double* ssa, const double* pmom, const float* tau_f, const float* ssa_f,
+                                       const float* pmom_f, const double* he, const double* U10m,
+                                       const double* V10m, const double* mr, const double* solar_zenith,
+                                       const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                       double* radiance_VL_SURF, double* reflectance_VL_SURF, double* BRDF,
+                                       int* nfourier, int* status, void* stream);
+
+/* VLIDORT_Scalar_GissCX (geo_vlidort/VLIDORT_BRDF_CX.F90:1553-1716), the
+ * Cox-Munk call of the ocean driver (geo_vlidort_ocean.F90:536): the same
+ * wrapper and arguments as aerort_vlidort_scalar_cx over the GISS Cox-Munk
+ * kernel of VLIDORT_GissCoxMunk_SingleGeom (VLIDORT_SurfaceMod.F90:586-814):
+ * kernel 10 with slope parameter sigma2 / 2 and refractive index mr(ch),
+ * shadowing, 100 azimuth streams.  For a real refractive index its scalar
+ * element is the Cox-Munk kernel's (to ~1e-13). */
+int aerort_vlidort_scalar_gisscx(int km, int nch, int nobs, const double* channels, int nstreams,
+                                 int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                 const double* tau, const double* ssa, const double* g, const double* pmom,
+                                 const double* pe, const double* he, const double* te, const double* U10m,
+                                 const double* V10m, const double* mr, const double* solar_zenith,
+                                 const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                 int verbose, double* radiance_VL_SURF, double* reflectance_VL_SURF, double* BRDF);
+int aerort_vlidort_scalar_gisscx_ex(int km, int nch, int nobs, const double* channels, int nstreams,
+                                    int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                    const double* tau, const double* ssa, const double* g, const double* pmom,
+                                    const double* pe, const double* he, const double* te, const double* U10m,
+                                    const double* V10m, const double* mr, const double* solar_zenith,
+                                    const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                    int verbose, double* radiance_VL_SURF, double* reflectance_VL_SURF, double* BRDF,
+                                    int* nfourier, int* status);
+int aerort_vlidort_scalar_gisscx_batch_dev(int km, int nch, int nobs, int nstreams, int plane_parallel, int nMom,
+                                           const int* nlay, const double* ROT, const double* depol,
+                                           const double* tau, const double* ssa, const double* pmom,
+                                           const float* tau_f, const float* ssa_f, const float* pmom_f,
+                                           const double* he, const double* U10m, const double* V10m,
+                                           const double* mr, const double* solar_zenith, const double* relat_azymuth,
+                                           const double* sensor_zenith, double MISSING, double* radiance_VL_SURF,
+                                           double* reflectance_VL_SURF, double* BRDF, int* nfourier, int* status,
+                                           void* stream);
+
 /* Edge pressure pe (Pa), height above the surface ze (m) and temperature te
  * (K), each (km+1,nobs), from layer air density airdens (kg m-3) and pressure
  * thickness delp (Pa), each (km,nobs), and the top pressure ptop (Pa).

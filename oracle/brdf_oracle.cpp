@@ -112,6 +112,72 @@ double coxmunk(const double* pars, double xi, double sxi, double xj, double sxj,
   return k * (1.0 / (1.0 + shadow(xi) + shadow(xj)));
 }
 
+// GISS Cox-Munk glint, the (1,1) element (GISSCOXMUNK_VFUNCTION,
+// vbrdf_sup_kernels.f90:1145-1492): pars = (slope variance parameter sigma2p,
+// real refractive index n, shadow flag); Fresnel reflection of the facet
+// between the incident vector (SXI, 0, -XI) and the reflected one
+// (SXJ cphi, SXJ sphi, XJ), with cphi, sphi the routine's CKPHI_REF,
+// SKPHI_REF.  Cosines within 1e-9 of 1 are replaced by 0.999999999999 for
+// the call, as the routine does (it writes them back to the caller's
+// variable; here the caller's value is kept).
+double giss_coxmunk(const double* pars, double xi, double sxi, double xj, double sxj, double cphi, double sphi) {
+  const double sigma2 = pars[0];
+  if (std::fabs(xi - 1.0) < 1e-9) xi = 0.999999999999;
+  if (std::fabs(xj - 1.0) < 1e-9) xj = 0.999999999999;
+  const double vi1 = sxi * 1.0, vi2 = sxi * 0.0, vi3 = -xi;
+  const double vr1 = sxj * cphi, vr2 = sxj * sphi, vr3 = xj;
+  const double u1 = vi1 - vr1, u2 = vi2 - vr2, u3 = vi3 - vr3;
+  const double fact1 = u1 * u1 + u2 * u2 + u3 * u3;
+  const double factor = std::sqrt(1.0 / fact1);
+  const double cn1 = 1.0, cn2 = pars[1];
+  const double xi1 = factor * (u1 * vi1 + u2 * vi2 + u3 * vi3);
+  double cxi2 = 1.0 - (1.0 - xi1 * xi1) * cn1 * cn1 / (cn2 * cn2);
+  cxi2 = std::sqrt(cxi2);
+  double c1 = cn1 * xi1, c2 = cn2 * cxi2;
+  const double crper = (c1 - c2) / (c1 + c2);
+  c1 = cn2 * xi1;
+  c2 = cn1 * cxi2;
+  const double crpar = (c1 - c2) / (c1 + c2);
+  const double ti1 = -xi * 1.0, ti2 = -xi * 0.0, ti3 = -sxi;
+  const double tr1 = xj * cphi, tr2 = xj * sphi, tr3 = -sxj;
+  const double pi1 = -0.0, pi2 = 1.0, pi3 = 0.0;
+  const double pr1 = -sphi, pr2 = cphi, pr3 = 0.0;
+  const double pikr = pi1 * vr1 + pi2 * vr2 + pi3 * vr3;
+  const double prki = pr1 * vi1 + pr2 * vi2 + pr3 * vi3;
+  const double tikr = ti1 * vr1 + ti2 * vr2 + ti3 * vr3;
+  const double trki = tr1 * vi1 + tr2 * vi2 + tr3 * vi3;
+  const double e1 = pikr * prki, e2 = tikr * trki, e3 = tikr * prki, e4 = pikr * trki;
+  double cf11 = e1 * crper + e2 * crpar;
+  const double cf12 = -e3 * crper + e4 * crpar;
+  const double cf21 = -e4 * crper + e3 * crpar;
+  double cf22 = e2 * crper + e1 * crpar;
+  const double vp1 = vi2 * vr3 - vi3 * vr2, vp2 = vi3 * vr1 - vi1 * vr3, vp3 = vi1 * vr2 - vi2 * vr1;
+  double dmod = vp1 * vp1 + vp2 * vp2 + vp3 * vp3;
+  dmod = dmod * dmod;
+  if (dmod == 0.0) {
+    cf11 = crpar;
+    cf22 = crper;
+    dmod = 1.0;
+  }
+  const double rdz2 = u3 * u3, rdz4 = rdz2 * rdz2;
+  const double dcoeff0 = 1.0 / (8.0 * xi * xj * dmod * rdz4 * sigma2);
+  const double arg = (u1 * u1 + u2 * u2) / (2.0 * sigma2 * rdz2);
+  const double dex = arg > 88.0 ? 0.0 : std::exp(-arg);
+  const double dcoeff = dcoeff0 * fact1 * fact1 * dex;
+  const double af = 0.5 * dcoeff;
+  double a11 = std::fabs(cf11), a12 = std::fabs(cf12), a21 = std::fabs(cf21), a22 = std::fabs(cf22);
+  a11 *= a11; a12 *= a12; a21 *= a21; a22 *= a22;
+  double k = (a11 + a12 + a21 + a22) * af;
+  if (pars[2] == 0.0) return k;
+  const double s1 = std::sqrt(2.0 * sigma2 / PIE), s3 = 1.0 / std::sqrt(2.0 * sigma2), s2 = s3 * s3;
+  auto shadow = [&](double x) {
+    if (x == 1.0) return 0.0;
+    const double dcot = x / std::sqrt(1.0 - x * x);
+    return 0.5 * (s1 * std::exp(-dcot * dcot * s2) / dcot - erfc_nr(dcot * s3));
+  };
+  return k * (1.0 / (1.0 + shadow(xi) + shadow(xj)));
+}
+
 }  // namespace
 
 namespace orc {
@@ -135,6 +201,7 @@ double brdf_kernel(int which, const double* pars, double xi, double sxi, double 
       return P / Q / R - 2.0;
     }
     case 9: return coxmunk(pars, xi, sxi, xj, sxj, cphi);    // Cox-Munk
+    case 10: return giss_coxmunk(pars, xi, sxi, xj, sxj, cphi, sphi);  // GISS Cox-Munk
   }
   return 0.0;
 }
@@ -185,7 +252,7 @@ extern "C" int oracle_brdf_supplement(int nk, const int* which, const double* fa
   std::vector<double> kq(N * N * nb), k0(N * nb), ku(nvza * N * nb), ku0(nvza * nb);
   for (int kk = 0; kk < nk; ++kk) {
     double pars[3] = {pars_in[3 * kk], pars_in[3 * kk + 1], pars_in[3 * kk + 2]};
-    if (which[kk] == 9) pars[2] = do_shadow ? 1.0 : 0.0;
+    if (which[kk] == 9 || which[kk] == 10) pars[2] = do_shadow ? 1.0 : 0.0;
     const int w = which[kk];
     const double fac = factors[kk];
     // exact direct bounce (VBRDF_MAKER, vbrdf_sup_routines.f90:244-266)

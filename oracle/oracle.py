@@ -36,6 +36,8 @@ def lib():
         _lib.oracle_vector_lambert.restype = ctypes.c_int
         _lib.oracle_scalar_lambert.restype = ctypes.c_int
         _lib.oracle_scalar_landmodis.restype = ctypes.c_int
+        _lib.oracle_scalar_cx.restype = ctypes.c_int
+        _lib.oracle_scalar_gisscx.restype = ctypes.c_int
         _lib.oracle_get_aop_vector.restype = ctypes.c_int
         _lib.oracle_set_asymtx_tol.restype = None
         _lib.oracle_rot_calc.restype = ctypes.c_int
@@ -165,6 +167,28 @@ def scalar_landmodis(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nP
                                        *[_p(a, P_d) for a in arr[1:]], ctypes.c_double(MISSING), int(verbose),
                                        _p(rad, P_d), _p(refl, P_d), _p(br, P_d), _p(nf, P_i), _p(st, P_i),
                                        None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
+    return rad, refl, br, rc, nf, st
+
+
+def scalar_cx(km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g, pmom, pe, he,
+              te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith, MISSING, verbose=0, nlay=None,
+              giss=False):
+    """Oracle VLIDORT_Scalar_CX (Cox-Munk glint; giss=True: VLIDORT_Scalar_GissCX,
+    the GISS Cox-Munk kernel); U10m, V10m (nobs), mr (nch).
+    Returns (radiance, reflectance, BR, rc, nfourier, status)."""
+    F = lambda a: np.asfortranarray(a, np.float64)
+    arr = [F(x) for x in (channels, ROT, depol, tau, ssa, g, pmom, pe, he, te, U10m, V10m, mr, solar_zenith,
+                          relat_azymuth, sensor_zenith)]
+    rad = np.zeros((nobs, nch), order="F")
+    refl = np.zeros_like(rad)
+    br = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    fn = lib().oracle_scalar_gisscx if giss else lib().oracle_scalar_cx
+    rc = fn(km, nch, nobs, _p(arr[0], P_d), nstreams, int(plane_parallel), nMom, nPol,
+                                *[_p(a, P_d) for a in arr[1:]], ctypes.c_double(MISSING), int(verbose),
+                                _p(rad, P_d), _p(refl, P_d), _p(br, P_d), _p(nf, P_i), _p(st, P_i),
+                                None if nlay is None else _p(np.ascontiguousarray(nlay, np.int32), P_i))
     return rad, refl, br, rc, nf, st
 
 

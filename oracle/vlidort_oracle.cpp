@@ -1647,3 +1647,160 @@ extern "C" int oracle_scalar_landmodis(int km, int nch, int nobs, const double* 
   }
   return 0;
 }
+
+// VLIDORT_Scalar_CX (geo_vlidort/VLIDORT_BRDF_CX.F90:420-584): the scalar
+// solve of VLIDORT_Scalar_Lambert (same layer mixing and VLIDORT_Init
+// settings) over the Cox-Munk glint surface of VLIDORT_CoxMunk_SingleGeom
+// (VLIDORT_SurfaceMod.F90:816-1042): one Cox-Munk kernel (factor 1) with
+// shadowing, slope variance sigma2 = 0.003 + 0.00512 W from the wind speed
+// W = |(U10m, V10m)| clamped to [0, 50] m/s (:893-898), refractive index
+// squared mr(ch)^2, 100 azimuth streams, observation geometry.  BR(nobs, nch)
+// is the exact direct-bounce BRDF (BS_DBOUNCE_BRDFUNC).  Pixels with MISSING
+// angles, and channels with a MISSING wind component or refractive index,
+// get MISSING radiance and reflectance (the reference leaves its BRDF output
+// unset there; here it is MISSING too).
+// VLIDORT_Scalar_GissCX (VLIDORT_BRDF_CX.F90:1553-1716) is the same wrapper
+// over the GISS Cox-Munk kernel of VLIDORT_GissCoxMunk_SingleGeom
+// (VLIDORT_SurfaceMod.F90:586-814): index 10, parameters (sigma2 / 2, mr(ch),
+// shadowing) (:680-697); `giss` selects it.
+static int scalar_cx_impl(int giss, int km, int nch, int nobs, const double* channels, int nstreams,
+                          int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                          const double* tau, const double* ssa, const double* g, const double* pmom, const double* pe,
+                          const double* he, const double* te, const double* U10m, const double* V10m, const double* mr,
+                          const double* solar_zenith, const double* relat_azymuth, const double* sensor_zenith,
+                          double MISSING, int verbose, double* radiance, double* reflectance, double* BR,
+                          int* nfourier, int* status, const int* nlay) {
+  (void)channels; (void)nPol; (void)pe; (void)te; (void)verbose; (void)g;
+  if (nstreams > 25) return 2;
+  if (km > 72) return 3;
+  if (nMom > 1000) return 5;
+  auto is_missing = [&](double x) { return std::fabs(x / MISSING - 1.0) < 0.001; };
+  auto geo_ok = [&](int j) {
+    return !(is_missing(solar_zenith[j]) || is_missing(sensor_zenith[j]) || is_missing(relat_azymuth[j]));
+  };
+  auto surf_ok = [&](int j, int i) { return !(is_missing(U10m[j]) || is_missing(V10m[j]) || is_missing(mr[i])); };
+  auto kernel = [&](int j, int i, double* pars) {
+    double w = std::sqrt(U10m[j] * U10m[j] + V10m[j] * V10m[j]);
+    if (w < 0.0) w = 0.0;
+    if (w > 50.0) w = 50.0;
+    const double sigma2 = 0.003 + 0.00512 * w;
+    pars[0] = giss ? 0.5 * sigma2 : sigma2;
+    pars[1] = giss ? mr[i] : mr[i] * mr[i];
+    pars[2] = 1.0;  // shadowing
+  };
+  const int which = giss ? 10 : 9;
+  for (int j = 0; j < nobs; ++j)
+    for (int i = 0; i < nch; ++i) {
+      const size_t o = (size_t)j + (size_t)nobs * i;
+      if (!geo_ok(j) || !surf_ok(j, i)) { BR[o] = MISSING; continue; }
+      double pars[3];
+      kernel(j, i, pars);
+      const double mu0 = std::cos(solar_zenith[j] * DTR), mu = std::cos(sensor_zenith[j] * DTR);
+      const double phi = relat_azymuth[j] * DTR;
+      BR[o] = brdf_kernel(which, pars, mu0, std::sqrt(1.0 - mu0 * mu0), mu, std::sqrt(1.0 - mu * mu),
+                          std::cos(phi), std::sin(phi));
+    }
+  // the sticky nadir FO flag: set by the first Run_Scalar call at SZA = 0
+  std::vector<char> nadir(nobs, 0);
+  {
+    bool flag = false;
+    for (int j = 0; j < nobs; ++j) {
+      if (geo_ok(j) && solar_zenith[j] == 0.0)
+        for (int i = 0; i < nch; ++i)
+          if (surf_ok(j, i)) { flag = true; break; }
+      nadir[j] = flag;
+    }
+  }
+  const double pi_sp = (double)(4.0f * std::atan(1.0f));
+  const double height_scale = (double)1.0e-3f;
+  const double ssa_cap = (double)0.99999f;
+  const int NMOM = 2 * nstreams - 1;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int p = 0; p < nobs * nch; ++p) {
+    int j = p / nch, i = p % nch;
+    size_t o = (size_t)j + (size_t)nobs * i;
+    if (nfourier) nfourier[o] = -1;
+    if (status) status[o] = 0;
+    if (!geo_ok(j) || !surf_ok(j, i)) { radiance[o] = MISSING; reflectance[o] = MISSING; continue; }
+    const int L = nlay ? nlay[j] : km;
+    std::vector<double> dt(L), om(L), gr((size_t)(nMom + 1) * L, 0.0), hg(L + 1);
+    const double dep = depol[i];
+    const double raysmom2 = (1.0 - dep) / (2.0 + dep);
+    for (int k = 0; k < L; ++k) {
+      double ray_l = ROT[k + (size_t)km * (j + (size_t)nobs * i)];
+      size_t a = k + (size_t)km * (i + (size_t)nch * j);
+      double tau_l = tau[a], ssa_l = ssa[a];
+      double tau_ext = 0.0 + ray_l + tau_l;
+      double tau_scat = ray_l + ssa_l * tau_l;
+      double ssa_tot = tau_scat / tau_ext;
+      if (ssa_tot > ssa_cap) ssa_tot = ssa_cap;
+      dt[k] = tau_ext; om[k] = ssa_tot;
+      double aerswt = ssa_l * tau_l / tau_scat;
+      double rayswt = ray_l / tau_scat;
+      size_t nk = (size_t)km * nch * nobs;
+      auto aersmom = [&](int l) { return l < nMom ? pmom[a + nk * (size_t)l] : 0.0; };
+      double* G = &gr[(size_t)(nMom + 1) * k];
+      G[0] = 1.0;
+      G[1] = aersmom(1) * aerswt;
+      G[2] = raysmom2 * rayswt + aersmom(2) * aerswt;
+      for (int l = 3; l <= nMom; ++l) G[l] = aersmom(l) * aerswt;
+    }
+    for (int k = 0; k <= L; ++k) hg[k] = he[k + (size_t)(km + 1) * j] * height_scale;
+    OracleOpts op;
+    op.do_focorr = 1;
+    op.do_focorr_nadir = nadir[j] ? 1 : 0;
+    op.do_focorr_outgoing = nadir[j] ? 0 : 1;
+    op.do_deltam = 1;
+    op.do_plane_parallel = plane_parallel;
+    op.do_double_convtest = 1;
+    op.nfinelayers = 3;
+    op.taylor_order = 3;
+    op.accuracy = (double)0.0001f;
+    op.asymtx_tol = g_asymtx_tol;
+    op.earth_radius = 6371.0;
+    op.flux_factor = 1.0;
+    double sza = solar_zenith[j], vz = sensor_zenith[j], az = relat_azymuth[j], rad = 0.0;
+    const double fac = 1.0;
+    double pars[3];
+    kernel(j, i, pars);
+    const int N = nstreams, M1 = NMOM + 1;
+    std::vector<double> bf((size_t)M1 * N * N), bf0((size_t)M1 * N), buf((size_t)M1 * N), buf0(M1), bex(1);
+    oracle_brdf_supplement(1, &which, &fac, pars, 1, 100, N, NMOM, sza, 1, &vz, 1, &az, bf.data(), bf0.data(),
+                           buf.data(), buf0.data(), bex.data());
+    int nf = -1;
+    int rc = oracle_vlidort_solve_brdf(&op, L, nstreams, nMom, hg.data(), dt.data(), om.data(), gr.data(), 0.0, sza,
+                                       1, &vz, 1, &az, bf.data(), bf0.data(), buf.data(), buf0.data(), bex.data(),
+                                       &rad, &nf);
+    if (nfourier) nfourier[o] = nf;
+    if (status) status[o] = rc;
+    if (rc != 0) { radiance[o] = MISSING; reflectance[o] = MISSING; continue; }
+    radiance[o] = rad;
+    reflectance[o] = (pi_sp * rad) / (std::cos(sza * pi_sp / 180.0) * 1.0);
+  }
+  return 0;
+}
+
+extern "C" int oracle_scalar_cx(int km, int nch, int nobs, const double* channels, int nstreams, int plane_parallel,
+                                int nMom, int nPol, const double* ROT, const double* depol, const double* tau,
+                                const double* ssa, const double* g, const double* pmom, const double* pe,
+                                const double* he, const double* te, const double* U10m, const double* V10m,
+                                const double* mr, const double* solar_zenith, const double* relat_azymuth,
+                                const double* sensor_zenith, double MISSING, int verbose, double* radiance,
+                                double* reflectance, double* BR, int* nfourier, int* status, const int* nlay) {
+  return scalar_cx_impl(0, km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g,
+                        pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith, MISSING,
+                        verbose, radiance, reflectance, BR, nfourier, status, nlay);
+}
+
+extern "C" int oracle_scalar_gisscx(int km, int nch, int nobs, const double* channels, int nstreams,
+                                    int plane_parallel, int nMom, int nPol, const double* ROT, const double* depol,
+                                    const double* tau, const double* ssa, const double* g, const double* pmom,
+                                    const double* pe, const double* he, const double* te, const double* U10m,
+                                    const double* V10m, const double* mr, const double* solar_zenith,
+                                    const double* relat_azymuth, const double* sensor_zenith, double MISSING,
+                                    int verbose, double* radiance, double* reflectance, double* BR, int* nfourier,
+                                    int* status, const int* nlay) {
+  return scalar_cx_impl(1, km, nch, nobs, channels, nstreams, plane_parallel, nMom, nPol, ROT, depol, tau, ssa, g,
+                        pmom, pe, he, te, U10m, V10m, mr, solar_zenith, relat_azymuth, sensor_zenith, MISSING,
+                        verbose, radiance, reflectance, BR, nfourier, status, nlay);
+}

@@ -67,3 +67,13 @@ def modis_brdf(nobs, nch, seed=0, negative=()):
         kw[:, i, j] = (0.01, 5.0, 0.0)
     par = np.stack([np.full((nch, nobs), 2.0), np.full((nch, nobs), 1.0)])
     return np.asfortranarray(kw), np.asfortranarray(par)
+
+
+def ocean_cx(nobs, nch, seed=0):
+    """Cox-Munk ocean surface inputs of VLIDORT_Scalar_CX: wind components
+    U10m, V10m (nobs) in m/s and the water refractive index mr (nch)."""
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-12.0, 12.0, nobs)
+    v = rng.uniform(-12.0, 12.0, nobs)
+    mr = np.linspace(1.343, 1.330, nch) if nch > 1 else np.array([1.336])
+    return u, v, np.ascontiguousarray(mr)

@@ -1,7 +1,8 @@
-"""GPU parity of the MODIS RTLS BRDF path (aerort_vlidort_scalar_landmodis*,
-VLIDORT_Scalar_LandMODIS) against the oracle (oracle_scalar_landmodis), which
-is pinned to the reference's saved BRDF results
-(tests/test_oracle_golden_brdf.py).  Bar: identical Fourier-term counts and
+"""GPU parity of the BRDF paths -- MODIS RTLS (aerort_vlidort_scalar_landmodis*,
+VLIDORT_Scalar_LandMODIS) and Cox-Munk glint (aerort_vlidort_scalar_cx*,
+VLIDORT_Scalar_CX) -- against the oracle (oracle_scalar_landmodis,
+oracle_scalar_cx), whose kernels and BRDF solve are pinned to the reference's
+saved BRDF results (tests/test_oracle_golden_brdf.py).  Bar: identical Fourier-term counts and
 status codes; radiance and reflectance within 1e-9 relative; BR to round-off;
 -500 where the kernel combination is negative; MISSING where the angles are."""
 import numpy as np
@@ -102,6 +103,102 @@ def test_batched_device_call_reads_fp32_optics():
     rc = _lib.lib().aerort_vlidort_scalar_landmodis_batch_dev(
         c["km"], nch, nobs, N, 0, c["nmom"], P(nl), P(d["ROT"]), P(d["depol"]), None, None, None, P(t32), P(s32),
         P(p32), P(d["he"]), P(dkw), _lib.ptr(parh, _lib.P_d), P(d["sza"]), P(d["raa"]), P(d["vza"]), MISSING,
+        P(out["rad"]), P(out["refl"]), P(out["br"]), P(nf), P(st), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, _lib.last_error()
+    torch.cuda.synchronize()
+    rad = out["rad"].cpu().numpy().reshape(nobs, nch, order="F")
+    br = out["br"].cpu().numpy().reshape(nobs, nch, order="F")
+    assert np.array_equal(nf.cpu().numpy().reshape(nobs, nch, order="F"), hnf)
+    assert np.max(np.abs(rad / hrad - 1.0)) <= 1e-13 and np.max(np.abs(br - hbr)) <= 1e-15
+
+
+# ---------------------------------------------------------------- Cox-Munk glint (VLIDORT_Scalar_CX)
+
+def _both_cx(c, N, u, v, mr, giss=False):
+    a = rt_args(c, N)
+    got = vlidort.vlidort_scalar_cx(*a[:17], u, v, mr, c["sza"], c["raa"], c["vza"], MISSING=MISSING,
+                                    diagnostics=True, giss=giss)
+    ref = oracle.scalar_cx(*a[:17], u, v, mr, c["sza"], c["raa"], c["vza"], MISSING, giss=giss)
+    return got, ref
+
+
+def _check_cx(got, ref):
+    rad, refl, br, rc, nf, st = got
+    orad, orefl, obr, orc, onf, ost = ref
+    assert rc == 0 and orc == 0
+    assert np.array_equal(st, ost) and np.array_equal(nf, onf)
+    assert np.array_equal(rad == MISSING, orad == MISSING) and np.array_equal(br == MISSING, obr == MISSING)
+    ok = orad != MISSING
+    assert np.max(np.abs(rad[ok] / orad[ok] - 1.0)) <= RTOL
+    assert np.max(np.abs(refl[ok] / orefl[ok] - 1.0)) <= RTOL
+    okb = (obr != MISSING) & (obr > 1e-30)
+    assert np.max(np.abs(br[okb] / obr[okb] - 1.0)) <= 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("N,km,giss", [(4, 30, False), (8, 24, False), (12, 16, False), (16, 12, False),
+                                       (6, 20, True), (12, 40, True), (16, 24, True)])
+def test_cox_munk_matches_oracle(N, km, giss):
+    # VLIDORT_Scalar_CX, and with giss VLIDORT_Scalar_GissCX (the ocean driver's call)
+    from rt_cases import ocean_cx
+    c = random_aop_case(N, km, nobs=5, nch=2, seed=500 + N + int(giss))
+    u, v, mr = ocean_cx(5, 2, seed=N)
+    _check_cx(*_both_cx(c, N, u, v, mr, giss))
+
+
+@pytest.mark.gpu
+def test_cox_munk_missing_winds_and_angles_calm_and_storm():
+    # a MISSING wind component (both channels), a MISSING refractive index (one
+    # channel), a MISSING solar angle; calm (W = 0) and storm (W > 50 m/s,
+    # clamped) seas; 72 layers
+    from rt_cases import ocean_cx
+    N = 8
+    c = random_aop_case(N, 72, nobs=6, nch=2, seed=88)
+    u, v, mr = ocean_cx(6, 2, seed=4)
+    u[1] = MISSING
+    c["sza"][2] = MISSING
+    u[3], v[3] = 0.0, 0.0
+    u[4], v[4] = 45.0, -40.0
+    got, ref = _both_cx(c, N, u, v, mr)
+    _check_cx(got, ref)
+    assert np.all(got[0][1] == MISSING) and np.all(got[0][2] == MISSING)
+    mr2 = mr.copy()
+    mr2[1] = MISSING
+    got2, ref2 = _both_cx(c, N, u, v, mr2)
+    _check_cx(got2, ref2)
+    assert np.all(got2[0][:, 1] == MISSING) and not np.any(got2[0][[0, 3, 4, 5], 0] == MISSING)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("giss", [False, True])
+def test_cox_munk_batched_device_call(giss):
+    # aerort_vlidort_scalar_(giss)cx_batch_dev with FP32 optics equals the host
+    # call on the same (FP64-converted) optics
+    import torch
+    from rt_cases import ocean_cx
+    N = 12
+    c = random_aop_case(N, 24, nobs=6, nch=2, seed=321)
+    u, v, mr = ocean_cx(6, 2, seed=7)
+    tau32, ssa32, pm32 = [np.asfortranarray(c[k].astype(np.float32)) for k in ("tau", "ssa", "pmom")]
+    for k, x in (("tau", tau32), ("ssa", ssa32), ("pmom", pm32)):
+        c[k] = np.asfortranarray(x.astype(np.float64))
+    a = rt_args(c, N)
+    hrad, hrefl, hbr, hrc, hnf, hst = vlidort.vlidort_scalar_cx(*a[:17], u, v, mr, c["sza"], c["raa"], c["vza"],
+                                                                diagnostics=True, giss=giss)
+    dev = lambda x, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(x, dt).ravel(order="F"))).cuda()
+    d = {k: dev(c[k], np.float64) for k in ("ROT", "depol", "he", "sza", "raa", "vza")}
+    t32, s32, p32 = dev(tau32, np.float32), dev(ssa32, np.float32), dev(pm32[..., 0], np.float32)
+    du, dv, dm = dev(u, np.float64), dev(v, np.float64), dev(mr, np.float64)
+    nobs, nch = 6, 2
+    out = {k: torch.zeros(nobs * nch, dtype=torch.float64, device="cuda") for k in ("rad", "refl", "br")}
+    nf = torch.zeros(nobs * nch, dtype=torch.int32, device="cuda")
+    st = torch.zeros_like(nf)
+    nl = dev(np.full(nobs, c["km"]), np.int32)
+    P = lambda t: t.data_ptr()
+    fn = _lib.lib().aerort_vlidort_scalar_gisscx_batch_dev if giss else _lib.lib().aerort_vlidort_scalar_cx_batch_dev
+    rc = fn(
+        c["km"], nch, nobs, N, 0, c["nmom"], P(nl), P(d["ROT"]), P(d["depol"]), None, None, None, P(t32), P(s32),
+        P(p32), P(d["he"]), P(du), P(dv), P(dm), P(d["sza"]), P(d["raa"]), P(d["vza"]), MISSING,
         P(out["rad"]), P(out["refl"]), P(out["br"]), P(nf), P(st), torch.cuda.current_stream().cuda_stream)
     assert rc == 0, _lib.last_error()
     torch.cuda.synchronize()

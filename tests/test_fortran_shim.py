@@ -70,5 +70,11 @@ def test_drop_ins_keep_the_reference_argument_lists():
                  "param solar_zenith relat_azymuth sensor_zenith missing verbose radiance_vl_surf "
                  "reflectance_vl_surf br rc").split()
     assert _subroutine_args("VLIDORT_Scalar_LandMODIS_GPU", shim) == ref_modis
+    # VLIDORT_Scalar_CX / _GissCX (VLIDORT_BRDF_CX.F90:420-423, :1553-1556)
+    ref_cx = ("km nch nobs channels nstreams plane_parallel nmom npol rot depol tau ssa g pmom pe he te u10m v10m "
+              "mr solar_zenith relat_azymuth sensor_zenith missing verbose radiance_vl_surf reflectance_vl_surf "
+              "brdf rc").split()
+    assert _subroutine_args("VLIDORT_Scalar_CX_GPU", shim) == ref_cx
+    assert _subroutine_args("VLIDORT_Scalar_GissCX_GPU", shim) == ref_cx
     assert _subroutine_args("VLIDORT_ROT_CALC_GPU", shim) == ref_rot
     assert _subroutine_args("getEdgeVars_GPU", shim) == ref_edge

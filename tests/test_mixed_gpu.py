@@ -213,3 +213,47 @@ def test_tensor_core_contraction(N, lo):
     ok = orad != MISSING
     err = np.abs(rad[ok] / orad[ok] - 1.0)
     assert err.max() <= RTOL, err.max()
+
+
+@pytest.mark.gpu
+def test_refined_solves_are_the_fp64_solves():
+    # the FP64 re-solve of the refinement list (k_refine_terms: each solve's
+    # Fourier terms spread over the warps of a block) gives the plain FP64
+    # team solve's result: at least as many radiances agree with it to 1e-12,
+    # with the same Fourier-term count, as were refined (an FP32 series is
+    # ~1e-7 away).  Not bit for bit: the same device code inlined into two
+    # kernels may fuse multiply-adds differently.  The host build of the same
+    # logic is bitwise the sequential series (test_rt_core_host.py).
+    import ctypes
+    import bench
+    full = bench.make_batch(8192, seed=20261204)
+    tabs = mie.generate_tables(CH, nmom=32)
+    chem = mie.ChemMie(tabs)
+    qt, qb = zip(*[chem.query_idx(x) for x in synth.tracer_names()])
+    chem.destroy()
+    total = 0
+    for N in (8, 12, 16):
+        g = bench.subset(full, np.nonzero(full["nstreams"] == N)[0][:600])
+        km, n = g["km"], g["ncol"]
+        nl = np.ascontiguousarray(g["nlayers"], np.int32)
+        tau, ssa, gg, pm, rc = oracle.get_aop_vector(tabs, km, n, 4, 20, np.float32(CH), qt, qb, g["qm"], g["rh"],
+                                                     2 * N, 1)
+        args = (km, 4, n, N, 2 * N, nl, g["ROT"], g["depol"], tau.astype(np.float64), ssa.astype(np.float64),
+                pm[..., 0].astype(np.float64), g["he"], g["albedo"], g["sza"], g["raa"], g["vza"])
+        rm, _, rcm, nfm, stm = vlidort.vlidort_scalar_lambert_batch(*args, MISSING=MISSING, precision="mixed")
+        cnt = ctypes.c_int()
+        assert _lib.lib().aerort_refined_count(None, ctypes.byref(cnt)) == 0
+        L = _lib.lib()
+        kern = L.aerort_get_kernel(N, _lib.PREC_FP64)
+        assert L.aerort_set_kernel(N, _lib.PREC_FP64, _lib.KERNEL_TEAM) == 0
+        try:
+            rd, _, rcd, nfd, std = vlidort.vlidort_scalar_lambert_batch(*args, MISSING=MISSING, precision="fp64")
+        finally:
+            L.aerort_set_kernel(N, _lib.PREC_FP64, kern)
+        assert rcm == 0 and rcd == 0 and np.all(stm == 0) and np.all(std == 0)
+        ok = rd != MISSING
+        same = ok & (np.abs(np.where(ok, rm / np.where(ok, rd, 1.0), 1.0) - 1.0) < 1e-12) & (nfm == nfd)
+        assert same.sum() >= cnt.value, (N, int(same.sum()), cnt.value)
+        assert np.max(np.abs(rm[ok] / rd[ok] - 1.0)) <= RTOL
+        total += cnt.value
+    assert total > 0

@@ -170,6 +170,47 @@ def test_team_solver_over_modis_brdf_matches_oracle(team_lib, nstreams, km):
     assert np.max(np.abs(refl[ok] / orefl[ok] - 1)) < 1e-9
 
 
+def _host_cx(lib, c, nstreams, u10, v10, mr, giss=False):
+    P = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    keep = [np.asfortranarray(c[k], np.float64) for k in ("ROT", "depol", "tau", "ssa", "pmom", "he")]
+    surf = [np.ascontiguousarray(a, np.float64) for a in (u10, v10, mr)]
+    ang = [np.ascontiguousarray(c[k], np.float64) for k in ("sza", "raa", "vza")]
+    nobs, nch = c["ncol"], c["nch"]
+    rad = np.zeros((nobs, nch), order="F")
+    refl = np.zeros_like(rad)
+    br = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    first = np.array([nobs], np.int32)
+    Ip = ctypes.POINTER(ctypes.c_int)
+    lib.team_scalar_cx(int(giss), c["km"], nch, nobs, nstreams, c["nmom"], *[P(a) for a in keep], *[P(a) for a in surf],
+                       *[P(a) for a in ang], first.ctypes.data_as(Ip), ctypes.c_double(MISSING), P(rad), P(refl),
+                       P(br), nf.ctypes.data_as(Ip), st.ctypes.data_as(Ip))
+    return rad, refl, br, nf, st
+
+
+@pytest.mark.parametrize("nstreams,km,giss", [(4, 10, False), (8, 6, True)])
+def test_team_solver_over_cox_munk_matches_oracle(team_lib, nstreams, km, giss):
+    # the Cox-Munk glint of VLIDORT_Scalar_CX (giss: the GISS kernel of
+    # VLIDORT_Scalar_GissCX) through the team solve: same Fourier terms,
+    # radiance within 1e-9; a MISSING wind gives MISSING
+    from rt_cases import ocean_cx
+    c = random_aop_case(nstreams, km, nobs=3, nch=2, seed=km + 7 * nstreams)
+    u, v, mr = ocean_cx(3, 2, seed=nstreams)
+    u[2] = MISSING
+    rad, refl, br, nf, st = _host_cx(team_lib, c, nstreams, u, v, mr, giss)
+    a = rt_args(c, nstreams)
+    orad, orefl, obr, orc, onf, ost = oracle.scalar_cx(*a[:17], u, v, mr, c["sza"], c["raa"], c["vza"], MISSING,
+                                                       giss=giss)
+    assert orc == 0
+    assert np.all(rad[2] == MISSING) and np.all(orad[2] == MISSING) and np.all(br[2] == MISSING)
+    ok = orad != MISSING
+    assert np.max(np.abs(br[ok] / obr[ok] - 1)) < 1e-12
+    assert np.array_equal(nf[ok], onf[ok]) and np.all(st == 0)
+    assert np.max(np.abs(rad[ok] / orad[ok] - 1)) < 1e-9
+    assert np.max(np.abs(refl[ok] / orefl[ok] - 1)) < 1e-9
+
+
 def _refine(lib, sf, raa=0.0):
     a = np.ascontiguousarray(sf, np.float64)
     ml = ctypes.c_int(0)
@@ -201,3 +242,33 @@ def test_refinement_flags_convergence_tests_at_the_threshold(host_lib):
     # cancellation (sum |terms| > 10 |sum|) still flags on its own
     f, _ = _refine(host_lib, [1.0, -0.95, 1e-9, 1e-9])
     assert f == 1
+
+
+def _host_termpar(lib, c, nstreams, W):
+    keep = [np.asfortranarray(c[k], np.float64) for k in ("ROT", "depol", "tau", "ssa", "pmom", "he", "albedo", "sza",
+                                                            "raa", "vza")]
+    ptrs = [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in keep]
+    nobs, nch = c["ncol"], c["nch"]
+    rad = np.zeros((nobs, nch), order="F")
+    refl = np.zeros_like(rad)
+    nf = np.zeros((nobs, nch), np.int32, order="F")
+    st = np.zeros_like(nf)
+    first = np.array([nobs], np.int32)
+    Ip = ctypes.POINTER(ctypes.c_int)
+    lib.team_scalar_lambert_termpar(W, c["km"], nch, nobs, nstreams, c["nmom"], *ptrs, first.ctypes.data_as(Ip),
+                                    ctypes.c_double(MISSING), rad.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                    refl.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nf.ctypes.data_as(Ip),
+                                    st.ctypes.data_as(Ip))
+    return rad, nf, st
+
+
+@pytest.mark.parametrize("nstreams,km,W", [(8, 12, 3), (4, 20, 8)])
+def test_term_parallel_fp64_resolve_is_the_sequential_series(team_lib, nstreams, km, W):
+    # the refinement list's FP64 re-solve with each solve's Fourier terms
+    # spread over W teams (k_refine_terms, emulated on the host: P~_m^m
+    # carried over the skipped terms, the sum taken in term order) gives the
+    # sequential team series bit for bit, Fourier-term counts included
+    c = random_aop_case(nstreams, km, nobs=2, nch=1, seed=km + W)
+    a = _host(team_lib, c, nstreams, "team_scalar_lambert")
+    b = _host_termpar(team_lib, c, nstreams, W)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.all(b[2] == 0)
