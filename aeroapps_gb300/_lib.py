@@ -108,6 +108,7 @@ PREC_MIXED = 1
 KERNEL_THREAD = 0
 KERNEL_TEAM = 1
 KERNEL_AUTO = 2
+KERNEL_TERMS = 3
 CONTRACT_FMA = 0
 CONTRACT_TF32X3 = 1
 

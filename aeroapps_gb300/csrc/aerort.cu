@@ -791,14 +791,17 @@ int dispatch_lambert_t(Context& c, int nstreams, const RtOptions& opt, const Lam
                        double* refl, int* nf, int* st, cudaStream_t s, const Worklist& wl) {
   const int si = stream_index(nstreams);
   const int prec = sizeof(T) == sizeof(float) ? AERORT_PREC_MIXED : AERORT_PREC_FP64;
-  if (si >= 0 && resolve_kernel(c.sched[prec][si].kernel, prec, si, (long)in.nobs * in.nch, c.num_sms,
-                                wl.in_list != nullptr) == 1) {
+  const int rk = si >= 0 ? resolve_kernel(c.sched[prec][si].kernel, prec, si, (long)in.nobs * in.nch, c.num_sms,
+                                          wl.in_list != nullptr)
+                         : 0;
+  if (rk == 1 || rk == 3) {
+    const bool terms = rk == 3;
     switch (nstreams) {
-      case 4: return launch_scalar_lambert_team<4, T>(c, opt, in, rad, refl, nf, st, s, wl);
-      case 6: return launch_scalar_lambert_team<6, T>(c, opt, in, rad, refl, nf, st, s, wl);
-      case 8: return launch_scalar_lambert_team<8, T>(c, opt, in, rad, refl, nf, st, s, wl);
-      case 12: return launch_scalar_lambert_team<12, T>(c, opt, in, rad, refl, nf, st, s, wl);
-      case 16: return launch_scalar_lambert_team<16, T>(c, opt, in, rad, refl, nf, st, s, wl);
+      case 4: return launch_scalar_lambert_team<4, T>(c, opt, in, rad, refl, nf, st, s, wl, terms);
+      case 6: return launch_scalar_lambert_team<6, T>(c, opt, in, rad, refl, nf, st, s, wl, terms);
+      case 8: return launch_scalar_lambert_team<8, T>(c, opt, in, rad, refl, nf, st, s, wl, terms);
+      case 12: return launch_scalar_lambert_team<12, T>(c, opt, in, rad, refl, nf, st, s, wl, terms);
+      case 16: return launch_scalar_lambert_team<16, T>(c, opt, in, rad, refl, nf, st, s, wl, terms);
     }
   }
   switch (nstreams) {
@@ -956,7 +959,8 @@ extern "C" int aerort_set_kernel(int nstreams, int precision, int kernel) {
   const int si = stream_index(nstreams);
   if (si < 0) return set_error(AERORT_RC_UNSUPPORTED, "set_kernel: nstreams must be one of 4, 6, 8, 12, 16");
   if ((precision != AERORT_PREC_FP64 && precision != AERORT_PREC_MIXED) ||
-      (kernel != AERORT_KERNEL_THREAD && kernel != AERORT_KERNEL_TEAM && kernel != AERORT_KERNEL_AUTO))
+      (kernel != AERORT_KERNEL_THREAD && kernel != AERORT_KERNEL_TEAM && kernel != AERORT_KERNEL_AUTO &&
+       kernel != AERORT_KERNEL_TERMS))
     return set_error(AERORT_RC_ARG, "set_kernel: bad precision or kernel");
   Context& c = ctx();
   std::lock_guard<std::mutex> lk(c.mu);
@@ -1019,6 +1023,7 @@ int dispatch_fixed(int precision, int nstreams, const RtOptions& opt, const Lamb
   s32.kernel = resolve_kernel(sc.kernel, AERORT_PREC_MIXED, si, nsolve, num_sms, false);
   s64.kernel = resolve_kernel(sc64.kernel, AERORT_PREC_FP64, si, nsolve, num_sms, false);
   s64_list.kernel = resolve_kernel(sc64.kernel, AERORT_PREC_FP64, si, nsolve, num_sms, true);
+  if (s64.kernel == 3) s64.kernel = 1;  // fixed storage: the team kernel for the term-parallel choice
   if (precision == AERORT_PREC_FP64)
     return dispatch_fixed_t<double>(nstreams, opt, in, arena, bytes, sched, num_sms, s64, r, f, nf, st, s,
                                     Worklist());

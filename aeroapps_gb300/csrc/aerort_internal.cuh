@@ -36,7 +36,8 @@ struct DevBuf {
 // threads per block (a multiple of 32, <= 128) and resident blocks per SM
 // (0 = as many as the occupancy calculator allows).
 // kernel: 0 = thread per solve, 1 = team (one warp per solve for the Fourier
-// series, rt_team.cuh), 2 = automatic (resolve_kernel).
+// series, rt_team.cuh), 2 = automatic (resolve_kernel), 3 = term-parallel team
+// solve (FP64: each solve's Fourier terms over the warps of a block).
 struct Schedule {
   int threads = 32;  // one warp per block spreads small batches over more SMs
   int blocks_per_sm = 0;
@@ -54,6 +55,7 @@ int stream_index(int nstreams);  // 0..4 for 4, 6, 8, 12, 16; -1 otherwise
 constexpr int kThreadMinWarpsPerSm[2][5] = {{2, 3, 3, 0, 0}, {2, 0, 4, 0, 0}};
 inline int resolve_kernel(int kernel, int precision, int si, long nsolve, int num_sms, bool list) {
   if (list) return 1;
+  if (kernel == 3) return precision == 0 ? 3 : 1;  // the term-parallel form exists in FP64
   if (kernel == 0 || kernel == 1) return kernel;
   if (si < 0 || precision < 0 || precision > 1) return 0;
   const int w = kThreadMinWarpsPerSm[precision][si];
@@ -110,9 +112,12 @@ template <int NS, typename T>
 int launch_scalar_lambert(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
                           double* refl, int* nf, int* st, cudaStream_t s, const aerort::Worklist& wl);
 
+// terms: the term-parallel team solve (k_refine_terms) for every solve (FP64;
+// a refinement list always takes it)
 template <int NS, typename T>
 int launch_scalar_lambert_team(Context& c, const aerort::RtOptions& opt, const aerort::LambertInputs& in, double* rad,
-                               double* refl, int* nf, int* st, cudaStream_t s, const aerort::Worklist& wl);
+                               double* refl, int* nf, int* st, cudaStream_t s, const aerort::Worklist& wl,
+                               bool terms = false);
 template <int NS, typename T>
 int launch_scalar_lambert_fixed(const aerort::RtOptions& opt, const aerort::LambertInputs& in, void* arena,
                                 size_t arena_bytes, int* sched, int num_sms, const Schedule& sc, double* rad,

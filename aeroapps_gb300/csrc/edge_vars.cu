@@ -15,7 +15,10 @@
 // (km+1, nobs) outputs, so they move between HBM and shared memory as whole
 // coalesced chunks, with several loads in flight per lane; each thread then
 // walks its own column in shared memory (odd column stride, so the 32 lanes
-// hit 32 banks).
+// hit 32 banks).  Three column arrays per block: pe has its own; ze
+// overwrites delp and te overwrites airdens as each layer's input is used
+// for the last time (ze walks up from the surface, te down from the top), so
+// a block takes 27 KB at 72 layers and eight blocks fit an SM.
 #include "aerort_internal.cuh"
 
 namespace aerort_internal {
@@ -29,21 +32,19 @@ constexpr float kKappa = 2.0f / 7.0f;  // REAL parameter 2.0/7.0, a single-preci
 
 __host__ __device__ inline int odd_stride(int n) { return n | 1; }
 
-size_t edge_smem_bytes(int km) {
-  return sizeof(float) * (size_t)kEdgeCols * (2 * (size_t)odd_stride(km) + 3 * (size_t)odd_stride(km + 1));
-}
+size_t edge_smem_bytes(int km) { return sizeof(float) * (size_t)kEdgeCols * 3 * (size_t)odd_stride(km + 1); }
 
 __global__ void __launch_bounds__(kEdgeCols) k_edge_vars(int km, int nobs, const float* __restrict__ airdens,
                                                          const float* __restrict__ delp, float ptop,
                                                          float* __restrict__ pe, float* __restrict__ ze,
                                                          float* __restrict__ te) {
   extern __shared__ float sm[];
-  const int ks = odd_stride(km), es = odd_stride(km + 1);
-  float* s_rho = sm;
-  float* s_dp = s_rho + kEdgeCols * ks;
+  const int ks = odd_stride(km + 1), es = ks;  // km + 1 slots per column in every array
+  float* s_rho = sm;                  // airdens, then te
+  float* s_dp = s_rho + kEdgeCols * ks;  // delp, then ze
   float* s_pe = s_dp + kEdgeCols * ks;
-  float* s_ze = s_pe + kEdgeCols * es;
-  float* s_te = s_ze + kEdgeCols * es;
+  float* s_ze = s_dp;
+  float* s_te = s_rho;
   const int lane = threadIdx.x;
   for (long c0 = (long)blockIdx.x * kEdgeCols; c0 < nobs; c0 += (long)gridDim.x * kEdgeCols) {
     const int nc = (int)min((long)kEdgeCols, (long)nobs - c0);
@@ -74,11 +75,11 @@ __global__ void __launch_bounds__(kEdgeCols) k_edge_vars(int km, int nobs, const
     }
     __syncwarp();
     if (lane < nc) {
-      const float* R = s_rho + lane * ks;
-      const float* D = s_dp + lane * ks;
+      float* R = s_rho + lane * ks;  // airdens; te in place (T[k] after R[k]'s last use)
+      float* D = s_dp + lane * ks;   // delp; ze in place (Z[k] after D[k]'s last use)
       float* P = s_pe + lane * es;
-      float* Z = s_ze + lane * es;
-      float* T = s_te + lane * es;
+      float* Z = D;
+      float* T = R;
       P[0] = ptop;
       for (int k = 0; k < km; ++k) P[k + 1] = __fadd_rn(P[k], D[k]);
       Z[km] = 0.0f;  // height above the surface

@@ -168,19 +168,22 @@ __global__ void __launch_bounds__(32 * WPB, sizeof(T) == sizeof(float) ? (NS <= 
   }
 }
 
-// FP64 re-solve of a mixed launch's refinement list (wl.in_list) with each
-// solve's Fourier terms spread over the W warps of a block: warp w runs terms
-// m0 + w of each round, one thread adds the round's terms to the Fourier sum
-// in order with the convergence test, and the round that ends the series
-// ends the solve (its later terms are discarded).  Every term is the one
-// team_fourier_series would compute (team_skip_terms carries P~_m^m over the
-// terms a warp skips), so the radiances are the same bits; a short list's
-// latency drops from one whole solve on one warp to about a W-th of it.  One
-// solve per block at a time; the block's set-up thread fills its scratch.
+// Term-parallel FP64 team solve: each solve's Fourier terms spread over the W
+// warps of a block.  Warp w runs terms m0 + w of each round, one thread adds
+// the round's terms to the Fourier sum in order with the convergence test,
+// and the round that ends the series ends the solve (its later terms are
+// discarded).  Every term is the one team_fourier_series would compute
+// (team_skip_terms carries P~_m^m over the terms a warp skips), so the
+// results are the sequential series'.  A solve's latency drops from the whole
+// series on one warp to about a W-th of it, at the cost of up to W - 1
+// discarded terms: the form for few solves -- a mixed launch's refinement
+// list (wl.in_list), or a batch too small to fill the GPU one warp per solve
+// (AERORT_KERNEL_TERMS).  One solve per block at a time; the block's set-up
+// thread fills its scratch.
 template <int NS, int W>
 __global__ void __launch_bounds__(32 * W, 1)
-    k_refine_terms(RtOptions opt, LambertInputs in, Quad q, void* scratch, int* counter, double* rad, double* refl,
-                   int* nf, int* st, Worklist wl) {
+    k_refine_terms(RtOptions opt, LambertInputs in, Quad q, void* scratch, int nsolve, int* counter, double* rad,
+                   double* refl, int* nf, int* st, Worklist wl) {
   extern __shared__ __align__(16) unsigned char team_smem[];
   __shared__ double s_sf[W];
   __shared__ int s_tst[W];
@@ -190,13 +193,13 @@ __global__ void __launch_bounds__(32 * W, 1)
   const ScratchLayout<NS> lay(in.km, false);
   const SolveScratch<double> S = make_scratch<NS, double>(scratch, blockIdx.x, gridDim.x, in.km, false);
   const Team tm{lane, nullptr, nullptr};
-  const int n = *wl.in_count;
+  const int n = wl.count(nsolve);
   for (;;) {
     if (threadIdx.x == 0) s_idx = atomicAdd(counter, 1);
     __syncthreads();
     const int idx = s_idx;
     if (idx >= n) break;
-    const int sidx = wl.in_list[idx];
+    const int sidx = wl.solve(idx);
     if (threadIdx.x == 0) {
       SetupRecord r;
       const bool ok = solve_setup<NS, double>(opt, in, sidx, q.tu, q.wu, S, rad, refl, nf, st, r);
@@ -244,10 +247,14 @@ __global__ void __launch_bounds__(32 * W, 1)
   }
 }
 
-// Warps per block of k_refine_terms: as many FP64 TeamMems as fit one block's
-// shared memory, at most 8.
+// Warps per block of k_refine_terms.  A block's footprint is kept to that of
+// a two-warp series block (about 72 KB of shared memory at 16 streams, half
+// an SM's registers at most), so the re-solves of one launch group share the
+// SMs with the other groups' launches in flight rather than taking whole SMs
+// (measured on GB300: six-warp blocks of 215 KB cut a group's own time by
+// 0.6 s and slowed the concurrent step by as much).
 template <int NS>
-constexpr int kRefineWarps = (NS >= 16) ? 6 : 8;
+constexpr int kRefineWarps = (NS >= 16) ? 2 : (NS >= 12 ? 3 : 4);
 
 // Enqueue the two-pass team solve on storage at `base`: per-solve scratch for
 // `slice` solves and their live flags at live_off; counter and first are two
@@ -292,7 +299,7 @@ int team_series_blocks_per_sm(int* per_sm) {
 
 template <int NS, typename T>
 int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertInputs& in, double* rad, double* refl,
-                               int* nf, int* st, cudaStream_t s, const Worklist& wl) {
+                               int* nf, int* st, cudaStream_t s, const Worklist& wl, bool terms) {
   constexpr int WPB = 2;
   const int nsolve = in.nobs * in.nch;
   if (nsolve == 0) return 0;
@@ -302,12 +309,17 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
   if (opt.nfine > 0) gauss_legendre01(opt.nfine, q.tu, q.wu);
   const int bs = 32 * WPB;
   const size_t smem = sizeof(TeamMem<NS, T>) * WPB;
-  if (wl.in_list && sizeof(T) == sizeof(double)) {
-    // refinement list: the term-parallel FP64 re-solve, one block per SM
+  if (sizeof(T) == sizeof(double) && (wl.in_list || terms)) {
+    // refinement list or a small batch: the term-parallel FP64 solve, as many
+    // blocks as the occupancy calculator places (a list: at most two per SM)
     constexpr int W = kRefineWarps<NS>;
     const size_t rsmem = sizeof(TeamMem<NS, double>) * W;
     CUDA_TRY(cudaFuncSetAttribute(k_refine_terms<NS, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem));
-    long nblocks = c.num_sms;
+    int rper_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rper_sm, k_refine_terms<NS, W>, 32 * W, rsmem));
+    if (rper_sm < 1) return set_error(AERORT_RC_CUDA, "term-parallel kernel does not fit on an SM");
+    if (wl.in_list && rper_sm > 2) rper_sm = 2;
+    long nblocks = (long)rper_sm * c.num_sms;
     if (nblocks > nsolve) nblocks = nsolve;
     const ScratchLayout<NS> lay(in.km, false);
     if (int rc = c.pad->scratch.ensure((size_t)lay.template bytes<double>() * nblocks)) return rc;
@@ -320,8 +332,8 @@ int launch_scalar_lambert_team(Context& c, const RtOptions& opt, const LambertIn
     CUDA_TRY(cudaGetLastError());
     LambertInputs in2 = in;
     in2.nadir_first = first;
-    k_refine_terms<NS, W><<<(unsigned)nblocks, 32 * W, rsmem, s>>>(opt, in2, q, c.pad->scratch.p, counter, rad,
-                                                                   refl, nf, st, wl);
+    k_refine_terms<NS, W><<<(unsigned)nblocks, 32 * W, rsmem, s>>>(opt, in2, q, c.pad->scratch.p, nsolve, counter,
+                                                                   rad, refl, nf, st, wl);
     CUDA_TRY(cudaGetLastError());
     count_launches(3);
     return 0;
@@ -719,10 +731,10 @@ int launch_scalar_brdf(Context& c, const RtOptions& opt, const LambertInputs& in
       int*, cudaStream_t, const aerort::Worklist&);                                                                                      \
   template int aerort_internal::launch_scalar_lambert_team<NS, double>(                                        \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
-      int*, cudaStream_t, const aerort::Worklist&);                                                                                      \
+      int*, cudaStream_t, const aerort::Worklist&, bool);                                                                                \
   template int aerort_internal::launch_scalar_lambert_team<NS, float>(                                         \
       aerort_internal::Context&, const aerort::RtOptions&, const aerort::LambertInputs&, double*, double*, int*, \
-      int*, cudaStream_t, const aerort::Worklist&);                                                                                      \
+      int*, cudaStream_t, const aerort::Worklist&, bool);                                                                                      \
   template int aerort_internal::launch_scalar_lambert_fixed<NS, double>(                                       \
       const aerort::RtOptions&, const aerort::LambertInputs&, void*, size_t, int*, int,                         \
       const aerort_internal::Schedule&, double*, double*, int*, int*, cudaStream_t, const aerort::Worklist&);                            \

@@ -480,11 +480,30 @@ def config0(torch, L, fp64_peak, ftab, cpu=True):
     ms = e0.elapsed_time(e1) / reps
     grad = rad.cpu().numpy()
     gnf = nf.cpu().numpy()
+    # the same launches with the term-parallel team solve (each column's
+    # Fourier terms over the warps of a block), AERORT_KERNEL_TERMS
+    L.aerort_set_kernel(N, _lib.PREC_FP64, _lib.KERNEL_TERMS)
+    for _ in range(2):
+        run()
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(reps):
+        run()
+    t1.record()
+    torch.cuda.synchronize()
+    ms_terms = t0.elapsed_time(t1) / reps
+    trad = rad.cpu().numpy()
+    L.aerort_set_kernel(N, _lib.PREC_FP64, _lib.KERNEL_AUTO)
+    okt = grad != MISSING
+    kernel_ab = {"auto_ms": ms, "terms_ms": ms_terms, "terms_speedup": ms / ms_terms,
+                 "terms_vs_auto_max_rel": float(np.max(np.abs(trad[okt] / grad[okt] - 1.0))),
+                 "fourier_terms_identical": bool(np.array_equal(nf.cpu().numpy(), gnf))}
     flops = float(ftab[N][km, gnf].sum())
     ach = flops / (ms * 1e-3) / 1e12
     out = {"workload": "plain FP64 method: 1,024 columns x 72 layers, 550 nm, 8 streams, 16 moments, Lambertian; "
                        "AOP kernel + FP64 RT per launch",
-           "value": ncol / (ms * 1e-3), "unit": "columns/s", "ms_per_launch": ms,
+           "value": ncol / (ms * 1e-3), "unit": "columns/s", "ms_per_launch": ms, "kernel_ab": kernel_ab,
            "roofline": {"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
                         "frac": ach / fp64_peak,
                         "note": "reference-algorithm flops (banded-LU BVP, nonsymmetric eigen-solve) summed over the "

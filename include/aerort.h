@@ -454,6 +454,11 @@ int aerort_get_schedule(int nstreams, int precision, int* threads_per_block, int
 #define AERORT_KERNEL_THREAD 0
 #define AERORT_KERNEL_TEAM 1
 #define AERORT_KERNEL_AUTO 2
+/* AERORT_KERNEL_TERMS (FP64; the team kernel for mixed): the team solve with
+ * each solve's Fourier terms spread over the warps of a block, for batches too
+ * small to fill the GPU one warp per solve.  The FP64 re-solve of a mixed
+ * launch's refinement list always runs in this form. */
+#define AERORT_KERNEL_TERMS 3
 int aerort_set_kernel(int nstreams, int precision, int kernel);
 int aerort_get_kernel(int nstreams, int precision);
 

