@@ -382,7 +382,7 @@ int aerort_vlidort_scalar_gisscx_batch_dev(int km, int nch, int nobs, int nstrea
  * Replaces getEdgeVars (Chem_Base/MieObs_py.F90:27-83), same argument list
  * with rc as the return value.  FP32 like the reference: pe and ze
  * bit-identical, te within a few units in the last place (logf/powf).
- * rc: 0; AERORT_RC_ARG; AERORT_RC_NLAYERS when km > 318.  _dev: every array on
+ * rc: 0; AERORT_RC_ARG; AERORT_RC_NLAYERS when km > 532.  _dev: every array on
  * the device, enqueued on `stream`. */
 int aerort_get_edge_vars(int km, int nobs, const float* airdens, const float* delp, float ptop, float* pe, float* ze,
                          float* te);

@@ -86,12 +86,12 @@ def test_oracle_physics():
 def test_edge_argument_checks_without_gpu():
     L = _lib.lib()
     assert L.aerort_get_edge_vars(0, 1, None, None, 1.0, None, None, None) == 1002
-    assert L.aerort_get_edge_vars(319, 1, None, None, 1.0, None, None, None) == 3
+    assert L.aerort_get_edge_vars(533, 1, None, None, 1.0, None, None, None) == 3
     assert L.aerort_get_edge_vars(72, 1, None, None, 1.0, None, None, None) == 1002
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nobs,km", [(1, 72), (37, 72), (300, 47), (5, 1), (33, 130), (70, 318)])
+@pytest.mark.parametrize("nobs,km", [(1, 72), (37, 72), (300, 47), (5, 1), (33, 130), (70, 318), (9, 532)])
 def test_device_edge_vars_match_oracle(nobs, km):
     rho, dp, ptop = _layers(nobs, km, seed=nobs + km)
     o = oracle.get_edge_vars(rho, dp, ptop)
