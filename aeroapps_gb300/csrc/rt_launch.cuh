@@ -251,8 +251,9 @@ __global__ void __launch_bounds__(32 * W, 1)
 // a two-warp series block (about 72 KB of shared memory at 16 streams, half
 // an SM's registers at most), so the re-solves of one launch group share the
 // SMs with the other groups' launches in flight rather than taking whole SMs
-// (measured on GB300: six-warp blocks of 215 KB cut a group's own time by
-// 0.6 s and slowed the concurrent step by as much).
+// (measured on GB300 at 16 streams: six-warp blocks of 215 KB cut the
+// largest group's own time by 0.6 s but left the concurrent step at 17.3 s;
+// two-warp blocks gave 17.0 s).
 template <int NS>
 constexpr int kRefineWarps = (NS >= 16) ? 2 : (NS >= 12 ? 3 : 4);
 
