@@ -206,3 +206,62 @@ def test_cox_munk_batched_device_call(giss):
     br = out["br"].cpu().numpy().reshape(nobs, nch, order="F")
     assert np.array_equal(nf.cpu().numpy().reshape(nobs, nch, order="F"), hnf)
     assert np.max(np.abs(rad / hrad - 1.0)) <= 1e-13 and np.max(np.abs(br - hbr)) <= 1e-15
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("giss", [False, True])
+def test_glint_plane_parallel_nadir_sun_and_view(giss):
+    # plane-parallel beam attenuation; a pixel at solar zenith exactly 0 turns
+    # on the wrapper's sticky nadir single-scatter flag for it and every later
+    # pixel; a nadir view (VZA = 0, where the GISS kernel replaces the cosine
+    # 1 by 0.999999999999)
+    from rt_cases import ocean_cx
+    N = 8
+    c = random_aop_case(N, 30, nobs=6, nch=2, seed=71 + int(giss))
+    u, v, mr = ocean_cx(6, 2, seed=12)
+    c["sza"][2] = 0.0
+    c["vza"][4] = 0.0
+    for pp in (False, True):
+        a = list(rt_args(c, N))
+        a[5] = pp
+        got = vlidort.vlidort_scalar_cx(*a[:17], u, v, mr, c["sza"], c["raa"], c["vza"], MISSING=MISSING,
+                                        diagnostics=True, giss=giss)
+        ref = oracle.scalar_cx(*a[:17], u, v, mr, c["sza"], c["raa"], c["vza"], MISSING, giss=giss)
+        _check_cx(got, ref)
+
+
+@pytest.mark.gpu
+def test_gisscx_batched_ragged_columns():
+    # aerort_vlidort_scalar_gisscx_batch_dev with per-column layer counts
+    # (FP64 optics on the device) against the oracle with the same counts
+    import torch
+    from rt_cases import ocean_cx
+    N = 16
+    c = random_aop_case(N, 40, nobs=7, nch=2, seed=404)
+    u, v, mr = ocean_cx(7, 2, seed=8)
+    nl = np.array([40, 12, 25, 1, 33, 40, 7], np.int32)
+    a = rt_args(c, N)
+    orad, orefl, obr, orc, onf, ost = oracle.scalar_cx(*a[:17], u, v, mr, c["sza"], c["raa"], c["vza"], MISSING,
+                                                       nlay=nl, giss=True)
+    dev = lambda x, dt: torch.from_numpy(np.ascontiguousarray(np.asarray(x, dt).ravel(order="F"))).cuda()
+    d = {k: dev(c[k], np.float64) for k in ("ROT", "depol", "tau", "ssa", "he", "sza", "raa", "vza")}
+    pm = dev(c["pmom"][..., 0], np.float64)
+    du, dv, dm = dev(u, np.float64), dev(v, np.float64), dev(mr, np.float64)
+    nobs, nch = 7, 2
+    out = {k: torch.zeros(nobs * nch, dtype=torch.float64, device="cuda") for k in ("rad", "refl", "br")}
+    nf = torch.zeros(nobs * nch, dtype=torch.int32, device="cuda")
+    st = torch.zeros_like(nf)
+    dnl = dev(nl, np.int32)
+    P = lambda t: t.data_ptr()
+    rc = _lib.lib().aerort_vlidort_scalar_gisscx_batch_dev(
+        c["km"], nch, nobs, N, 0, c["nmom"], P(dnl), P(d["ROT"]), P(d["depol"]), P(d["tau"]), P(d["ssa"]), P(pm),
+        None, None, None, P(d["he"]), P(du), P(dv), P(dm), P(d["sza"]), P(d["raa"]), P(d["vza"]), MISSING,
+        P(out["rad"]), P(out["refl"]), P(out["br"]), P(nf), P(st), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0 and orc == 0, _lib.last_error()
+    torch.cuda.synchronize()
+    rad = out["rad"].cpu().numpy().reshape(nobs, nch, order="F")
+    gnf = nf.cpu().numpy().reshape(nobs, nch, order="F")
+    gst = st.cpu().numpy().reshape(nobs, nch, order="F")
+    assert np.array_equal(gnf, onf) and np.array_equal(gst, ost)
+    ok = orad != MISSING
+    assert np.max(np.abs(rad[ok] / orad[ok] - 1.0)) <= RTOL
