@@ -125,3 +125,25 @@ def test_giss_cox_munk_kernel_against_the_self_tester():
                  (b["uf"][m, 0, 0], w["Stream-Users"]), (b["uf0"][m, 0], w["Solars-Users"]))
         for x, y in pairs:
             assert abs(x / y - 1.0) < 1e-7, (m, x, y)
+
+
+def test_giss_and_cox_munk_scalar_elements_agree():
+    # for a real refractive index the GISS kernel's (1,1) element with
+    # parameters (sigma2 / 2, n) is the Cox-Munk kernel with (sigma2, n^2):
+    # both are the Fresnel-weighted facet-slope density with the same
+    # shadowing; the two restatements agree to rounding on random geometries
+    rng = np.random.default_rng(7)
+    for _ in range(5):
+        sigma2 = 0.003 + 0.00512 * rng.uniform(0.0, 20.0)
+        n = rng.uniform(1.32, 1.35)
+        sza, vza, raa = rng.uniform(5.0, 75.0), rng.uniform(5.0, 65.0), rng.uniform(0.0, 180.0)
+        vzas, raas = [vza], [raa]
+        a = oracle.brdf_supplement([(9, 1.0, (sigma2, n * n, 0.0))], 8, sza, vzas, raas, nstreams_brdf=100,
+                                   do_shadow=True)
+        b = oracle.brdf_supplement([(10, 1.0, (0.5 * sigma2, n, 0.0))], 8, sza, vzas, raas, nstreams_brdf=100,
+                                   do_shadow=True)
+        assert abs(b["exactdb"].ravel()[0] / a["exactdb"].ravel()[0] - 1.0) < 1e-10
+        for key in ("f", "f0", "uf", "uf0"):
+            x, y = np.asarray(a[key]), np.asarray(b[key])
+            scale = np.maximum(np.abs(x), 1e-3 * np.abs(x).max())  # components near 0 come from cancellation
+            assert np.max(np.abs(x - y) / scale) < 1e-11, key
