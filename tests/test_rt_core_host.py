@@ -74,7 +74,7 @@ def test_mixed_precision_solver_within_1e4(host_lib, nstreams, km):
     assert np.max(np.abs(rad / orad - 1)) < 1e-4
 
 
-@pytest.mark.parametrize("nstreams,km", [(4, 6), (12, 3)])
+@pytest.mark.parametrize("nstreams,km", [(4, 6), (12, 3), (16, 4), (6, 4)])
 def test_team_solver_matches_thread_solver(host_lib, team_lib, nstreams, km):
     c = random_aop_case(nstreams, km, nobs=1, nch=1, seed=km + 7 * nstreams)
     rad, nf, st = _host(host_lib, c, nstreams)
