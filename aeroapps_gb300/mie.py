@@ -16,7 +16,7 @@ import os
 
 import numpy as np
 
-from . import _lib
+from . import _lib, nc4
 
 # Five GOCART-like species: name prefix, refractive index (n, k) of the dry
 # aerosol, dry density [kg m-3], hygroscopic growth (dust does not grow).
@@ -122,6 +122,26 @@ _FIELDS3 = ("lambda", "rh", "radius")
 _FIELDS5 = ("lambda", "rh", "radius", "nMom", "nPol")
 
 
+class _OpticsFile:
+    """dimensions {name: length} and variables {name: (dimension names, loader)}
+    of one optics file, netCDF classic / 64-bit offset (scipy) or netCDF-4
+    (HDF5, nc4.Dataset)."""
+
+    def __init__(self, path):
+        with open(path, "rb") as fh:
+            hdf5 = fh.read(8) == _HDF5_MAGIC
+        if hdf5:
+            nc = nc4.Dataset(path)
+            self.dimensions = dict(nc.dimensions)
+            self.variables = {n: (tuple(v.dimensions), v.values) for n, v in nc.variables.items()}
+            return
+        from scipy.io import netcdf_file
+        with netcdf_file(path, "r", mmap=False) as nc:
+            self.dimensions = {n: int(x) for n, x in nc.dimensions.items() if x is not None}
+            data = {n: (tuple(v.dimensions), np.array(v.data)) for n, v in nc.variables.items()}
+        self.variables = {n: (dims, (lambda a=a: a)) for n, (dims, a) in data.items()}
+
+
 def read_optics_file(path):
     """The arrays Chem_MieTableRead reads from one optics_*.nc file
     (Chem_MieTableMod.F90:297-466): lambda [m], rh, and bext, bsca, g
@@ -130,50 +150,38 @@ def read_optics_file(path):
     (pmom None when the file has none).  Values are taken as stored, without
     scale/offset attributes, as nf_get_var_double does.
 
-    Reads netCDF classic and 64-bit-offset files; a netCDF-4 (HDF5) file is
-    refused with a message (convert it with `nccopy -k classic`, or read it
-    elsewhere and call `table_from_file_arrays`)."""
-    from scipy.io import netcdf_file
-    with open(path, "rb") as fh:
-        if fh.read(8) == _HDF5_MAGIC:
-            raise ValueError("%s is netCDF-4/HDF5; this reader takes netCDF classic files "
-                             "(convert with: nccopy -k classic)" % path)
-    out = {}
-    with netcdf_file(path, "r", mmap=False) as nc:
-        v = nc.variables
+    Reads netCDF classic and 64-bit-offset files (scipy) and netCDF-4 files
+    (HDF5: nc4.py)."""
+    f = _OpticsFile(path)
+    v = f.variables
 
-        def arr(name, order):
-            var = v[name]
-            dims = tuple(var.dimensions)
-            if sorted(dims) != sorted(order):
-                raise ValueError("%s: variable %s has dimensions %s, expected %s" % (path, name, dims, order))
-            a = np.asarray(var.data, np.float64)
-            return np.asfortranarray(np.transpose(a, [dims.index(d) for d in order]))
+    def arr(name, order):
+        dims, load = v[name]
+        if sorted(dims) != sorted(order):
+            raise ValueError("%s: variable %s has dimensions %s, expected %s" % (path, name, dims, order))
+        a = np.asarray(load(), np.float64)
+        return np.asfortranarray(np.transpose(a, [dims.index(d) for d in order]))
 
-        out["lambda"] = np.asarray(v["lambda"].data, np.float64).ravel().copy()
-        out["rh"] = np.asarray(v["rh"].data, np.float64).ravel().copy()
-        for name in ("bext", "bsca", "g"):
-            out[name] = arr(name, _FIELDS3)
-        out["pmom"] = arr("pmom", _FIELDS5) if "pmom" in v else None
+    out = {"lambda": np.asarray(v["lambda"][1](), np.float64).ravel().copy(),
+           "rh": np.asarray(v["rh"][1](), np.float64).ravel().copy()}
+    for name in ("bext", "bsca", "g"):
+        out[name] = arr(name, _FIELDS3)
+    out["pmom"] = arr("pmom", _FIELDS5) if "pmom" in v else None
     return out
 
 
 def get_mie_dims(path):
     """getMieDims / Chem_MieTableGetDims (MieObs_py.F90:7-23,
     Chem_MieTableMod.F90:733-800): (nCh, nRh, nBin, nMom, nPol, rc) of one
-    optics file.  A file without an nMom dimension has nMom = nPol = 0, as in
-    the reference.  rc is nonzero, with zero sizes, when the file or one of
-    the lambda/rh/radius dimensions cannot be read (netCDF-4 files included)."""
-    from scipy.io import netcdf_file
+    optics file (netCDF classic or netCDF-4).  A file without an nMom
+    dimension has nMom = nPol = 0, as in the reference.  rc is nonzero, with
+    zero sizes, when the file or one of the lambda/rh/radius dimensions
+    cannot be read."""
     try:
-        with open(path, "rb") as fh:
-            if fh.read(8) == _HDF5_MAGIC:
-                return 0, 0, 0, 0, 0, 1
-        with netcdf_file(path, "r", mmap=False) as nc:
-            d = nc.dimensions
-            nch, nrh, nbin = int(d["lambda"]), int(d["rh"]), int(d["radius"])
-            nmom = int(d["nMom"]) if "nMom" in d else 0
-            npol = int(d["nPol"]) if "nMom" in d and "nPol" in d else 0
+        d = _OpticsFile(path).dimensions
+        nch, nrh, nbin = int(d["lambda"]), int(d["rh"]), int(d["radius"])
+        nmom = int(d["nMom"]) if "nMom" in d else 0
+        npol = int(d["nPol"]) if "nMom" in d and "nPol" in d else 0
         return nch, nrh, nbin, nmom, npol, 0
     except (OSError, KeyError, TypeError, ValueError):
         return 0, 0, 0, 0, 0, 1

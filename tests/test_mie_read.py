@@ -5,7 +5,8 @@ polint :671-717) and the tracer hash of Chem_MieCreate / Chem_MieQueryIdx
 
 CPU: the C oracle against an independent numpy restatement of polint, bit for
 bit; the library's aerort_mie_table_interp (host code) against the oracle, bit
-for bit, on tables read back from netCDF classic files written here; the
+for bit, on tables read back from netCDF classic files written here (netCDF-4
+files: test_nc4.py); the
 edge cases the reference has (channels at, between, below and above the table
 wavelengths, a one-wavelength table, too many moments requested).
 GPU: AOP vectors from tables read from files, bit-identical to the oracle's.
@@ -245,14 +246,6 @@ NO3an2     kg/kg    Nitrate size bin 002
     reg = mie.registry_map(groups, list(mie.RC_SPECIES))
     assert reg["DU003"] == (0, 2) and reg["SO4"] == (2, 0) and reg["BCPHILIC"] == (4, 1)
     assert reg["NO3AN2"] == (5, 1) and "NH3" not in reg and "DMS" not in reg
-
-
-def test_netcdf4_file_is_refused_with_a_message(tmp_path):
-    path = os.path.join(tmp_path, "optics_h5.nc")
-    with open(path, "wb") as fh:
-        fh.write(b"\x89HDF\r\n\x1a\n" + bytes(64))
-    with pytest.raises(ValueError, match="nccopy"):
-        mie.read_optics_file(path)
 
 
 def test_registry_map_and_query_idx():
