@@ -6,7 +6,6 @@ references in a global heap), with a choice of chunk index (version-1
 B-tree, fixed array, single chunk, implicit) and filters (shuffle, deflate).
 Checksum fields are left zero (the reader does not check them).  Test
 infrastructure: the package never writes HDF5."""
-import struct
 import zlib
 
 import numpy as np
@@ -41,21 +40,36 @@ def _string(n):
     return bytes([0x13, 0x00, 0x00, 0x00]) + _u(n, 4)
 
 
+_LEGACY = [False]  # superblock 0, version-1 object headers and messages, symbol-table root group
+
+
+def _pad8(b):
+    return b + bytes((-len(b)) % 8)
+
+
 def _dataspace(shape):
+    if _LEGACY[0]:
+        return bytes([1, len(shape), 0, 0]) + bytes(4) + b"".join(_u(s, L) for s in shape)
     return bytes([2, len(shape), 0, 1 if shape else 0]) + b"".join(_u(s, L) for s in shape)
 
 
 def _msg(t, body):
-    return bytes([t]) + _u(len(body), 2) + b"\0" + body
+    return (t, body)
 
 
 def _ohdr(msgs):
-    body = b"".join(msgs)
+    if _LEGACY[0]:
+        body = b"".join(_u(t, 2) + _u(len(_pad8(b)), 2) + bytes(4) + _pad8(b) for t, b in msgs)
+        return bytes([1, 0]) + _u(len(msgs), 2) + _u(1, 4) + _u(len(body), 4) + bytes(4) + body
+    body = b"".join(bytes([t]) + _u(len(b), 2) + b"\0" + b for t, b in msgs)
     return b"OHDR" + bytes([2, 0x02]) + _u(len(body), 4) + body + b"\0\0\0\0"
 
 
 def _attr(name, dtype, space, data):
     nm = name.encode() + b"\0"
+    if _LEGACY[0]:
+        return _msg(0x0C, bytes([1, 0]) + _u(len(nm), 2) + _u(len(dtype), 2) + _u(len(space), 2)
+                    + _pad8(nm) + _pad8(dtype) + _pad8(space) + data)
     return _msg(0x0C, bytes([3, 0]) + _u(len(nm), 2) + _u(len(dtype), 2) + _u(len(space), 2) + b"\0"
                 + nm + dtype + space + data)
 
@@ -65,19 +79,34 @@ def _str_attr(name, s):
     return _attr(name, _string(len(v)), _dataspace(()), v)
 
 
-def write(path, dims, variables, index="btree1", chunk=None, shuffle=True, deflate=True):
+def write(path, dims, variables, index="btree1", chunk=None, shuffle=True, deflate=True, legacy=False):
     """dims: [(name, length, coordinate values or None)]; variables:
     [(name, dimension names, float64 array)].  Variables are chunked with
     chunk(shape) -> chunk shape (default: halves, rounded up) through the
-    chosen index; coordinate variables are contiguous."""
+    chosen index; coordinate variables are contiguous.  legacy: the layout
+    of files from HDF5 1.6-era writers (superblock 0, version-1 object
+    headers, a symbol-table root group; version-1 B-tree chunk index only)."""
+    assert not legacy or index == "btree1"
+    _LEGACY[0] = legacy
+    try:
+        _write(path, dims, variables, index, chunk, shuffle, deflate, legacy)
+    finally:
+        _LEGACY[0] = False
+
+
+def _write(path, dims, variables, index, chunk, shuffle, deflate, legacy):
     buf = _Buf()
-    buf.put(bytes(48))  # superblock, written last
+    buf.put(bytes(96 if legacy else 48))  # superblock, written last
     filters = []
-    if shuffle:
-        filters.append(_u(2, 2) + _u(1, 2) + _u(1, 2) + _u(8, 4))
-    if deflate:
-        filters.append(_u(1, 2) + _u(0, 2) + _u(1, 2) + _u(6, 4))
-    pipeline = bytes([2, len(filters)]) + b"".join(filters)
+    # (id, flags, client values); version 2 messages, or version 1 (with a
+    # name length field and padding to 8 bytes) in the legacy layout
+    for fid, vals in ([(2, [8])] if shuffle else []) + ([(1, [6])] if deflate else []):
+        if legacy:
+            filters.append(_u(fid, 2) + _u(0, 2) + _u(1, 2) + _u(len(vals), 2) + b"".join(_u(v, 4) for v in vals)
+                           + bytes(4 * (len(vals) % 2)))
+        else:
+            filters.append(_u(fid, 2) + _u(1, 2) + _u(len(vals), 2) + b"".join(_u(v, 4) for v in vals))
+    pipeline = (bytes([1, len(filters)]) + bytes(6) if legacy else bytes([2, len(filters)])) + b"".join(filters)
     links, dim_addr = [], {}
 
     def contiguous(values):
@@ -167,12 +196,31 @@ def write(path, dims, variables, index="btree1", chunk=None, shuffle=True, defla
             msgs.append(_msg(0x0B, pipeline))
         msgs.append(_attr("DIMENSION_LIST", vlen, _dataspace((len(vdims),)), refs))
         links.append((name, buf.put(_ohdr(msgs))))
-    lmsgs = []
-    for name, a in links:
-        nm = name.encode()
-        lmsgs.append(_msg(0x06, bytes([1, 0]) + _u(len(nm), 1) + nm + _u(a, O)))
-    root = buf.put(_ohdr(lmsgs))
-    buf.b[0:48] = b"\x89HDF\r\n\x1a\n" + bytes([2, O, L, 0]) + _u(0, O) + _u(UNDEF, O) + _u(len(buf.b), O) \
-        + _u(root, O) + bytes(4)
+    if legacy:
+        # root group: local heap of link names, one symbol table node, a
+        # one-leaf version-1 B-tree; names in ascending order
+        links.sort()
+        heap, offs = bytearray(bytes(8)), []
+        for name, _ in links:
+            offs.append(len(heap))
+            heap += _pad8(name.encode() + b"\0")
+        seg = buf.put(bytes(heap))
+        lheap = buf.put(b"HEAP" + bytes(4) + _u(len(heap), L) + _u(UNDEF, L) + _u(seg, O))
+        ents = b"".join(_u(o, O) + _u(a, O) + bytes(24) for o, (_, a) in zip(offs, links))
+        snod = buf.put(b"SNOD" + bytes([1, 0]) + _u(len(links), 2) + ents)
+        tree = buf.put(b"TREE" + bytes([0, 0]) + _u(1, 2) + _u(UNDEF, O) + _u(UNDEF, O)
+                       + _u(0, L) + _u(snod, O) + _u(offs[-1], L))
+        root = buf.put(_ohdr([_msg(0x11, _u(tree, O) + _u(lheap, O))]))
+        buf.b[0:96] = b"\x89HDF\r\n\x1a\n" + bytes([0, 0, 0, 0, 0, O, L, 0]) + _u(4, 2) + _u(16, 2) + bytes(4) \
+            + _u(0, O) + _u(UNDEF, O) + _u(len(buf.b), O) + _u(UNDEF, O) \
+            + _u(0, O) + _u(root, O) + _u(1, 4) + bytes(4) + _u(tree, O) + _u(lheap, O)
+    else:
+        lmsgs = []
+        for name, a in links:
+            nm = name.encode()
+            lmsgs.append(_msg(0x06, bytes([1, 0]) + _u(len(nm), 1) + nm + _u(a, O)))
+        root = buf.put(_ohdr(lmsgs))
+        buf.b[0:48] = b"\x89HDF\r\n\x1a\n" + bytes([2, O, L, 0]) + _u(0, O) + _u(UNDEF, O) + _u(len(buf.b), O) \
+            + _u(root, O) + bytes(4)
     with open(path, "wb") as fh:
         fh.write(bytes(buf.b))

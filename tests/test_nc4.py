@@ -10,8 +10,9 @@ files that Chem_MieTableRead opens with the netCDF library
   that tree is absent.
 - Files of tests/nc4_writer.py (the same structures, written here): every
   chunk index (version-1 B-tree, fixed array, single chunk, implicit) with
-  and without the shuffle and deflate filters, edge chunks included, read
-  back bit for bit; an optics table read from netCDF-4 equal to the same
+  and without the shuffle and deflate filters, edge chunks included, and the
+  older layout (superblock 0, version-1 object headers, symbol-table group),
+  read back bit for bit; an optics table read from netCDF-4 equal to the same
   table read from netCDF classic."""
 import os
 
@@ -47,17 +48,20 @@ def test_reads_a_library_written_netcdf4_file():
     assert np.all(np.isfinite(foq)) and 0.05 < foq.min() and foq.max() < 0.5
 
 
-@pytest.mark.parametrize("index,shuffle,deflate", [("btree1", True, True), ("btree1", False, False),
-                                                   ("farray", True, True), ("farray", False, True),
-                                                   ("single", True, True), ("implicit", False, False)])
-def test_chunk_indexes_and_filters_round_trip(tmp_path, index, shuffle, deflate):
+@pytest.mark.parametrize("index,shuffle,deflate,legacy", [("btree1", True, True, False), ("btree1", False, False, False),
+                                                          ("farray", True, True, False), ("farray", False, True, False),
+                                                          ("single", True, True, False), ("implicit", False, False, False),
+                                                          ("btree1", True, True, True), ("btree1", False, True, True)])
+def test_chunk_indexes_and_filters_round_trip(tmp_path, index, shuffle, deflate, legacy):
+    # legacy: superblock 0, version-1 object headers, attributes and filter
+    # pipeline, the root group as a symbol table
     r = np.random.default_rng(3)
     a = r.normal(size=(5, 7, 3))
     path = os.path.join(tmp_path, "t.nc")
     chunk = (lambda s: s) if index == "single" else (lambda s: (2, 3, 2))  # ragged edge chunks
     nc4_writer.write(path, [("x", 5, np.arange(5.0)), ("y", 7, None), ("z", 3, None)],
                      [("a", ("x", "y", "z"), a), ("b", ("z", "x", "y"), np.transpose(a, (2, 0, 1)))],
-                     index=index, chunk=chunk, shuffle=shuffle, deflate=deflate)
+                     index=index, chunk=chunk, shuffle=shuffle, deflate=deflate, legacy=legacy)
     ds = nc4.Dataset(path)
     assert ds.dimensions == {"x": 5, "y": 7, "z": 3}
     assert set(ds.variables) == {"x", "a", "b"}
